@@ -1,0 +1,252 @@
+/*
+ * adcgpu.h -- C ABI of the GB300 (sm_103a) ADC(2)-s hot path.
+ *
+ * One shared library, libadcgpu.so, replaces three Fortran subsystems of
+ * mschuurman/ADC_ottawa beneath the unchanged Fortran driver:
+ *
+ *   builder   write_fspace_adc2_1        source/adclib/fspacetrial.f90:533-564
+ *             (get_offdiag_adc2_save_omp source/adclib/get_matrix.f90:705-1186,
+ *              get_diag_adc2_save        source/adclib/get_matrix.f90:267-311)
+ *   solvers   davdiag_block              source/eigen/block_davidson.f90:33-145
+ *             lancdiag_block             source/eigen/block_lanczos.f90:28-81
+ *   SIL       SILStep                    source/propagation/sillib.f90:108-393
+ *             propagate_sillib           source/propagation/fvecprop.f90:365-564
+ *
+ * Conventions
+ *   - Plain C types only.  Host arrays are owned by the caller; the library
+ *     owns all device memory, held in an adcgpu_ctx.
+ *   - Matrices and vector blocks are Fortran column-major (leading dimension
+ *     = number of rows), exactly as the reference keeps vmat/wmat/qmat.
+ *   - Orbital and configuration indices in kpq and in exported COO triples are
+ *     1-based, as in the reference.
+ *   - Every entry point returns an adcgpu_status; nothing calls exit()/abort().
+ *     adcgpu_last_error() gives a one-line description of the last failure.
+ *   - A context is used from one host thread; it owns one CUDA stream.
+ */
+#ifndef ADCGPU_H
+#define ADCGPU_H
+
+#include <stdint.h>
+
+#ifdef __cplusplus
+extern "C" {
+#endif
+
+/* Status codes.  1-4 are the SIL error codes of sillib.f90:84-89. */
+enum adcgpu_status {
+  ADCGPU_OK = 0,
+  ADCGPU_SIL_BAD_ORDER = 1,       /* "Illegal integration order"  */
+  ADCGPU_SIL_STEP_UNDERFLOW = 2,  /* "Stepsize underflow"         */
+  ADCGPU_SIL_DIAG_FAILED = 3,     /* "Diagonalisation failed"     */
+  ADCGPU_SIL_BAD_RESTART = 4,     /* "Illegal initial stepsize"   */
+  ADCGPU_NOT_CONVERGED = 10,      /* block_davidson.f90:767-770   */
+  ADCGPU_OUT_OF_MEMORY = 11,
+  ADCGPU_BAD_INPUT = 12,
+  ADCGPU_CUDA_ERROR = 13,
+  ADCGPU_DEVICE_TIMEOUT = 14,     /* a bounded device wait gave up */
+  ADCGPU_NO_MATRIX = 15,          /* solver called before the builder */
+  ADCGPU_UNSUPPORTED = 16,        /* e.g. a kpq that is not C1 ADC(2)-s */
+  ADCGPU_EIGEN_FAILED = 17        /* dsyev/dsbev/dsteqr equivalent failed */
+};
+
+/* Storage precision of the stored matrix used by the sigma-vector product. */
+enum adcgpu_precision {
+  ADCGPU_FP64 = 0,   /* FP64 values, FP64 vectors: the plain drop-in path      */
+  ADCGPU_MIXED = 1   /* BF16/FP32 values, FP32 vectors and subspace GEMMs,
+                        FP64 Rayleigh-Ritz, Gram-Schmidt and residual norms    */
+};
+
+/* Preconditioners (parameters.f90 precon; block_davidson.f90:1119-1123). */
+enum adcgpu_precon {
+  ADCGPU_PRECON_DPR = 1,    /* dpr   block_davidson.f90:1288-1342 */
+  ADCGPU_PRECON_OLSEN = 2,  /* olsen block_davidson.f90:1346-1419 */
+  ADCGPU_PRECON_MLP = 3     /* learned correction, DPR as fallback */
+};
+
+typedef struct adcgpu_ctx adcgpu_ctx;
+
+/* ---------------------------------------------------------------------------
+ * Seeded synthetic system (stands in for the GAMESS/MO-integral producer,
+ * source/qclib/load_electronic_structure.f90:153-342).  Host only.
+ * ------------------------------------------------------------------------- */
+
+/* Orbital energies e[nocc+nvirt]: occupied ~ U(-1.4,-0.4) Ha first, then
+   virtual ~ U(0.1,3.0) Ha, each block sorted ascending. */
+int adcgpu_synth_orbitals(int nocc, int nvirt, uint64_t seed, double* e);
+
+/* Number of doubles in the canonical 8-fold packed ERI array for nbas MOs. */
+int64_t adcgpu_eri_packed_size(int nbas);
+
+/* Real MO ERIs (pq|rs) with 8-fold symmetry, one draw per canonical
+   quadruple p>=q, r>=s, pq>=rs (1-based):
+   N(0,1) * 0.3 * exp(-0.15|p-r| - 0.15|q-s|).  nthreads<=0: all cores. */
+int adcgpu_synth_eri_packed(int nbas, uint64_t seed, double* eri, int nthreads);
+
+/* Seeded "dipole-like" start block: nrow x ncol uniform(0,1) values
+   (the random_number draws of init_vecs_random, block_lanczos.f90:402-439). */
+int adcgpu_synth_uniform_block(int64_t nrow, int ncol, uint64_t seed, double* out);
+
+/* ---------------------------------------------------------------------------
+ * Configuration list kpq (select_atom_is select_fano.f90:16-60 and
+ * select_atom_d flag -1 select_fano.f90:539-718; C1 symmetry, no frozen core).
+ * ------------------------------------------------------------------------- */
+
+/* Returns ndim = n1 + n2; counts5 (may be NULL) receives kpq(1..5,0). */
+int64_t adcgpu_adc2s_dim(int nocc, int nvirt, int32_t* counts5);
+
+/* Fills kpq(7, 0:ndim), column-major int32, column 0 holding the counts. */
+int adcgpu_select_adc2s(int nocc, int nvirt, int32_t* kpq);
+
+/* ---------------------------------------------------------------------------
+ * Context.
+ * ------------------------------------------------------------------------- */
+int adcgpu_ctx_create(int device, adcgpu_ctx** out);
+int adcgpu_ctx_destroy(adcgpu_ctx* ctx);
+const char* adcgpu_last_error(const adcgpu_ctx* ctx);
+
+/* Orbital data (parameters.f90:21-32: e, nOcc, nVirt; occupied first). */
+int adcgpu_set_orbitals(adcgpu_ctx* ctx, int nocc, int nvirt, const double* e);
+
+/* ERIs as the canonical 8-fold packed real array (adcgpu_eri_packed_size). */
+int adcgpu_set_eri_packed(adcgpu_ctx* ctx, const double* eri);
+
+/* ERIs in the reference layout: moIntegrals%buffer_real, complex(8)
+   (nmo,nmo,nmo,nmo) column-major, read through vpqrs (vpqrsmod.f90:13-27):
+   the real part of element (r,s,u,v) is (rs|uv). */
+int adcgpu_set_eri_mo_complex(adcgpu_ctx* ctx, const double* buffer_real);
+
+/* ---------------------------------------------------------------------------
+ * Builder: write_fspace_adc2_1(ndim,kpq,noffdel,chr), fspacetrial.f90:533-564.
+ * Keeps H resident on the device.  kpq must be the ADC(2)-s list that
+ * adcgpu_select_adc2s produces (checked; ADCGPU_UNSUPPORTED otherwise).
+ * noffd_out = number of upper-triangle elements with |h| > minc = 1e-12
+ * (the reference's count, get_matrix.f90:904,1059-1063).
+ * precision: adcgpu_precision of the stored sigma-vector matrix.
+ * ------------------------------------------------------------------------- */
+int adcgpu_build_adc2s(adcgpu_ctx* ctx, int ndim, const int32_t* kpq,
+                       int64_t* noffd_out, char flag, int precision);
+
+/* Diagonal hii(ndim) (get_diag_adc2_save, get_matrix.f90:267-311). */
+int adcgpu_get_diag(adcgpu_ctx* ctx, double* hii);
+
+/* The kept off-diagonal elements as COO (h, oi<oj, 1-based), the content of
+   SCRATCH/hmlt.off<flag>.  Order: row oi ascending, then oj ascending.
+   cap must be >= noffd. */
+int adcgpu_export_coo(adcgpu_ctx* ctx, int64_t cap, double* h, int32_t* oi,
+                      int32_t* oj);
+
+/* Writes SCRATCH-style files <dir>/hmlt.dia<flag> and <dir>/hmlt.off<flag>
+   with the reference's Fortran unformatted sequential record layout
+   (filetools.f90:24-44, buf_size = 655360). */
+int adcgpu_write_hmlt_files(adcgpu_ctx* ctx, const char* dir, char flag);
+
+/* ---------------------------------------------------------------------------
+ * Sigma-vector product W = H V for m columns (hxvec_incore,
+ * block_davidson.f90:844-883; hxq_incore block_lanczos.f90:1325-1361).
+ * Host arrays, ndim x m column-major.
+ * ------------------------------------------------------------------------- */
+int adcgpu_sigma(adcgpu_ctx* ctx, int m, const double* v, double* w);
+
+/* Same on device buffers (leading dimension ld >= ndim), on the context's
+   stream.  For ADCGPU_MIXED the device arrays are float. */
+int adcgpu_sigma_device(adcgpu_ctx* ctx, int m, const void* dv, void* dw, int64_t ld);
+
+/* ---------------------------------------------------------------------------
+ * Block Davidson: davdiag_block(matdim,noffd), block_davidson.f90:33-145.
+ * Parameters mirror the module globals read in davinitialise (:163-183).
+ * ------------------------------------------------------------------------- */
+typedef struct {
+  int davstates;     /* nstates                                     */
+  int dmain;         /* blocksize; 0 -> max(nstates+5, 2*nstates)   */
+  int maxsubdim;     /* maxvec; <0 -> 4*blocksize                   */
+  int maxiter;       /* niter                                       */
+  int precon;        /* adcgpu_precon                               */
+  int ldfl;          /* deflation of converged vectors (1/0)        */
+  int lsubdiag;      /* 1: initvec_subdiag, 0: initvec_ondiag       */
+  int guessdim;      /* subspace dimension for initvec_subdiag      */
+  double davtol;     /* residual-norm tolerance                     */
+  int precision;     /* adcgpu_precision for the iterations         */
+  int refine;        /* MIXED only: FP64 refinement sweeps at the end */
+} adcgpu_dav_params;
+
+typedef struct {
+  int iterations;    /* Davidson iterations performed             */
+  int64_t nmult;     /* sigma-vector columns computed             */
+  int nconv;         /* converged roots                           */
+  double seconds;    /* wall time inside the solver               */
+  double sigma_seconds;  /* time in the sigma-vector kernels      */
+  double max_residual;   /* FP64 residual norm of the worst root  */
+} adcgpu_dav_info;
+
+/* evals[davstates] ascending; evecs ndim x davstates column-major (may be
+   NULL).  Returns ADCGPU_NOT_CONVERGED when maxiter is exhausted (results are
+   still written). */
+int adcgpu_davidson(adcgpu_ctx* ctx, const adcgpu_dav_params* p, double* evals,
+                    double* evecs, adcgpu_dav_info* info);
+
+/* Writes the eigenpair records (i, E_i, x_i) like wreigenpairs
+   (block_davidson.f90:1469-1532) to a Fortran unformatted sequential file. */
+int adcgpu_write_davidson_file(const char* path, int ndim, int nstates,
+                               const double* evals, const double* evecs);
+
+/* ---------------------------------------------------------------------------
+ * Block Lanczos: lancdiag_block(dimf,noff,flag), block_lanczos.f90:28-81.
+ * q0: ndim x lmain start block of raw values; it is normalised and
+ * orthonormalised by double MGS exactly as init_vecs_random (:402-439).
+ * orthotype: 0 none, 1 PRO (:1474-1526).
+ * tmat (nvec x nvec, nvec = lmain*ncycles) receives T as assembled at
+ * :1197-1219; evals (nvec) the dsbev eigenvalues (calc_pseudospec :1941).
+ * ritz (ndim x nvec, may be NULL): normalised Ritz vectors (:2237-2316).
+ * ------------------------------------------------------------------------- */
+int adcgpu_block_lanczos(adcgpu_ctx* ctx, int lmain, int ncycles, int orthotype,
+                         const double* q0, double* tmat, double* evals,
+                         double* ritz);
+
+/* ---------------------------------------------------------------------------
+ * SIL propagation.
+ * ------------------------------------------------------------------------- */
+
+/* The reference's SAVE variables of SILStep (sillib.f90:131-133) made
+   explicit, one per wavepacket. */
+typedef struct {
+  int old_order;
+  double old_error;
+  double old_stepsize;
+} adcgpu_sil_state;
+
+/* One SILStep (sillib.f90:108-393) with Func = matxvec_treal
+   (tdselib.f90:323-437, v2 = -i H v1) on the built matrix.
+   psi, dtpsi: complex(8) arrays of length psidim (interleaved re,im) on the
+   host; dtpsi must hold -iH psi on entry (as in fvecprop.f90:496).
+   krylov: complex(8) psidim x (intorder-1) host work array (may be NULL:
+   then the library keeps the Krylov vectors on the device; non-restart
+   calls then need the same context).  Returns 0 or a SIL error code 1-4. */
+int adcgpu_silstep(adcgpu_ctx* ctx, double* psi, double* dtpsi, int psidim,
+                   double intperiod, int intorder, double tol, int relax,
+                   int restart, int stdform, double* stepsize_out,
+                   int* trueorder_out, adcgpu_sil_state* st);
+
+/* propagate_sillib (fvecprop.f90:365-564) for nwp wavepackets at once.
+   f: ndim x nwp real start vectors (f-vectors, normalised internally as in
+   init_wavepacket :338-357).  Autocorrelation a(t) = sum_j psi_j(t/2)^2 *
+   ||f||^2 at t = 0, tout, 2 tout, ... (ntimes = int(tfinal/(tout/2)) + 1
+   values per wavepacket), written to auto_out as complex interleaved,
+   layout [wavepacket][time].  nmult_out (may be NULL): matvecs per packet. */
+int adcgpu_autocorr(adcgpu_ctx* ctx, int nwp, const double* f, double tout,
+                    double tfinal, int kdim, double tol, double* auto_out,
+                    int* ntimes_out, int64_t* nmult_out);
+
+/* ---------------------------------------------------------------------------
+ * Timing helpers for benchmarks: device milliseconds of the last sigma
+ * call as measured by CUDA events on the context's stream.
+ * ------------------------------------------------------------------------- */
+double adcgpu_last_sigma_ms(const adcgpu_ctx* ctx);
+
+/* Device bytes held by the context (matrix, ERI blocks, work spaces). */
+int64_t adcgpu_device_bytes(const adcgpu_ctx* ctx);
+
+#ifdef __cplusplus
+}
+#endif
+
+#endif /* ADCGPU_H */

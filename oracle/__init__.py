@@ -1,0 +1,194 @@
+"""ORACLE -- test infrastructure only.
+
+CPU FP64 restatement of mschuurman/ADC_ottawa's ADC(2)-s path (oracle.cpp),
+loaded through ctypes.  Only tests/, ``__graft_entry__.smoke()`` and the
+CPU-baseline leg of ``bench.py`` may use this module, and only as the checker;
+the product package never imports it.
+
+Parity status: unpinned against the reference's own outputs (the reference is
+Fortran, no Fortran compiler is available, and the reference ships no test
+vectors for this path).  It is pinned by independent checks instead: dense
+eigendecomposition of the assembled matrix, exact propagation, and structural
+rules (tests/test_oracle.py).
+"""
+from __future__ import annotations
+
+import ctypes as C
+import os
+import subprocess
+
+import numpy as np
+
+_HERE = os.path.dirname(os.path.abspath(__file__))
+_LIB_PATH = os.path.join(_HERE, "_build", "liboracle.so")
+_lib = None
+
+_dp = C.POINTER(C.c_double)
+_ip = C.POINTER(C.c_int32)
+_i64p = C.POINTER(C.c_int64)
+
+
+def build(force: bool = False) -> str:
+    """Compile oracle.cpp with the committed Makefile (strict IEEE flags)."""
+    src = os.path.join(_HERE, "oracle.cpp")
+    if force or not os.path.exists(_LIB_PATH) or os.path.getmtime(_LIB_PATH) < os.path.getmtime(src):
+        subprocess.run(["make", "-s", "-C", _HERE], check=True)
+    return _LIB_PATH
+
+
+def lib():
+    global _lib
+    if _lib is None:
+        build()
+        L = C.CDLL(_LIB_PATH)
+        L.orc_select.argtypes = [C.c_int, C.c_int, _ip]
+        L.orc_select.restype = C.c_int
+        L.orc_build.argtypes = [C.c_int, C.c_int, _dp, _dp, C.c_int]
+        L.orc_build.restype = C.c_void_p
+        L.orc_matrix_ndim.argtypes = [C.c_void_p]
+        L.orc_matrix_ndim.restype = C.c_int64
+        L.orc_matrix_nnz.argtypes = [C.c_void_p]
+        L.orc_matrix_nnz.restype = C.c_int64
+        L.orc_matrix_copy.argtypes = [C.c_void_p, _dp, _dp, _ip, _ip]
+        L.orc_matrix_from_coo.argtypes = [C.c_int64, _dp, C.c_int64, _dp, _ip, _ip]
+        L.orc_matrix_from_coo.restype = C.c_void_p
+        L.orc_matrix_free.argtypes = [C.c_void_p]
+        L.orc_structure_hash.argtypes = [C.c_int64, _ip, _ip, C.POINTER(C.c_uint64)]
+        L.orc_matvec.argtypes = [C.c_void_p, C.c_int, _dp, _dp, C.c_int]
+        L.orc_eigh.argtypes = [C.c_int, _dp, _dp, _dp]
+        L.orc_heapsort_index.argtypes = [C.c_int, _dp, _ip]
+        L.orc_davidson.argtypes = [C.c_void_p, _ip, C.c_double, C.c_int, _dp, _dp, _ip]
+        L.orc_davidson.restype = C.c_int
+        L.orc_block_lanczos.argtypes = [C.c_void_p, C.c_int, C.c_int, C.c_int, _dp, C.c_int, _dp, _dp]
+        L.orc_block_lanczos.restype = C.c_int
+        L.orc_autocorr.argtypes = [C.c_void_p, _dp, C.c_double, C.c_double, C.c_int, C.c_double,
+                                   _dp, C.POINTER(C.c_int), _i64p]
+        L.orc_autocorr.restype = C.c_int
+        _lib = L
+    return _lib
+
+
+def _p(a, t=_dp):
+    return a.ctypes.data_as(t)
+
+
+def select(no: int, nv: int) -> np.ndarray:
+    """kpq(7, 0:ndim) as a (ndim+1, 7) int32 array (row c = Fortran column c)."""
+    n1 = no * nv
+    ndim = n1 + n1 + nv * (nv - 1) // 2 * no + no * (no - 1) // 2 * nv + 2 * (no * (no - 1) // 2) * (nv * (nv - 1) // 2)
+    kpq = np.zeros((ndim + 1, 7), dtype=np.int32)
+    got = lib().orc_select(no, nv, _p(kpq, _ip))
+    assert got == ndim
+    return kpq
+
+
+class Matrix:
+    """The stored ADC(2)-s matrix: diagonal + upper-triangle COO (1-based)."""
+
+    def __init__(self, handle):
+        self.h = handle
+
+    @classmethod
+    def build(cls, no, nv, e, eri, nthreads=0):
+        e = np.ascontiguousarray(e, dtype=np.float64)
+        eri = np.ascontiguousarray(eri, dtype=np.float64)
+        return cls(lib().orc_build(no, nv, _p(e), _p(eri), nthreads))
+
+    @classmethod
+    def from_coo(cls, diag, h, oi, oj):
+        diag = np.ascontiguousarray(diag, np.float64)
+        h = np.ascontiguousarray(h, np.float64)
+        oi = np.ascontiguousarray(oi, np.int32)
+        oj = np.ascontiguousarray(oj, np.int32)
+        return cls(lib().orc_matrix_from_coo(len(diag), _p(diag), len(h), _p(h), _p(oi, _ip), _p(oj, _ip)))
+
+    @property
+    def ndim(self):
+        return lib().orc_matrix_ndim(self.h)
+
+    @property
+    def nnz(self):
+        return lib().orc_matrix_nnz(self.h)
+
+    def coo(self):
+        n, z = self.ndim, self.nnz
+        diag = np.empty(n)
+        h = np.empty(z)
+        oi = np.empty(z, np.int32)
+        oj = np.empty(z, np.int32)
+        lib().orc_matrix_copy(self.h, _p(diag), _p(h), _p(oi, _ip), _p(oj, _ip))
+        return diag, h, oi, oj
+
+    def dense(self):
+        diag, h, oi, oj = self.coo()
+        H = np.diag(diag)
+        H[oi - 1, oj - 1] = h
+        H[oj - 1, oi - 1] = h
+        return H
+
+    def matvec(self, V, nthreads=0):
+        V = np.asfortranarray(V, dtype=np.float64)
+        if V.ndim == 1:
+            V = V.reshape(-1, 1, order="F")
+        W = np.empty_like(V, order="F")
+        lib().orc_matvec(self.h, V.shape[1], _p(V), _p(W), nthreads)
+        return W
+
+    def davidson(self, nstates, tol, blocksize=0, maxvec=-1, niter=100, precon=1, deflate=True,
+                 subdiag=False, guessdim=800, nthreads=0, want_vectors=False):
+        ip = np.array([nstates, blocksize, maxvec, niter, precon, int(deflate), int(subdiag), guessdim],
+                      dtype=np.int32)
+        ev = np.empty(nstates)
+        vecs = np.empty((self.ndim, nstates), order="F") if want_vectors else None
+        iout = np.zeros(3, np.int32)
+        st = lib().orc_davidson(self.h, _p(ip, _ip), tol, nthreads, _p(ev),
+                                _p(vecs) if want_vectors else None, _p(iout, _ip))
+        return st, ev, vecs, dict(iterations=int(iout[0]), nmult=int(iout[1]), nconv=int(iout[2]))
+
+    def block_lanczos(self, q0, ncycles, orthotype=0, nthreads=0):
+        q0 = np.asfortranarray(q0, dtype=np.float64)
+        b = q0.shape[1]
+        nvec = b * ncycles
+        T = np.empty((nvec, nvec), order="F")
+        ev = np.empty(nvec)
+        lib().orc_block_lanczos(self.h, b, ncycles, orthotype, _p(q0), nthreads, _p(T), _p(ev))
+        return T, ev
+
+    def autocorr(self, f, tout, tfinal, kdim, tol):
+        f = np.ascontiguousarray(f, np.float64)
+        nt = int(tfinal / (0.5 * tout)) + 1
+        out = np.zeros(2 * nt)
+        ntimes = C.c_int(0)
+        nmult = C.c_int64(0)
+        st = lib().orc_autocorr(self.h, _p(f), tout, tfinal, kdim, tol, _p(out), C.byref(ntimes), C.byref(nmult))
+        a = out[0::2] + 1j * out[1::2]
+        return st, a[: ntimes.value], nmult.value
+
+    def __del__(self):
+        if getattr(self, "h", None) and _lib is not None:
+            _lib.orc_matrix_free(self.h)
+            self.h = None
+
+
+def structure_hash(oi, oj):
+    oi = np.ascontiguousarray(oi, np.int32)
+    oj = np.ascontiguousarray(oj, np.int32)
+    out = np.zeros(3, np.uint64)
+    lib().orc_structure_hash(len(oi), _p(oi, _ip), _p(oj, _ip), out.ctypes.data_as(C.POINTER(C.c_uint64)))
+    return tuple(int(x) for x in out)
+
+
+def heapsort_index(arr):
+    arr = np.ascontiguousarray(arr, np.float64)
+    out = np.empty(len(arr), np.int32)
+    lib().orc_heapsort_index(len(arr), _p(arr), _p(out, _ip))
+    return out
+
+
+def eigh(A):
+    A = np.asfortranarray(A, np.float64)
+    n = A.shape[0]
+    w = np.empty(n)
+    V = np.empty((n, n), order="F")
+    lib().orc_eigh(n, _p(A), _p(w), _p(V))
+    return w, V
