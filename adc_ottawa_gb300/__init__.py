@@ -1,0 +1,9 @@
+"""GB300-native (sm_103a) ADC(2)-s hot path of mschuurman/ADC_ottawa.
+
+The compute lives in libadcgpu.so (csrc/, C ABI in include/adcgpu.h);
+this package is its host-side mirror (api.py) and build recipe (build.py).
+"""
+from .api import (  # noqa: F401
+    ADCGPU_FP64, ADCGPU_MIXED, PRECON_DPR, PRECON_MLP, PRECON_OLSEN, AdcGpu, AdcGpuError, adc2s_dim,
+    eri_packed_size, select_adc2s, synth_eri_packed, synth_orbitals, synth_system, synth_uniform_block,
+)

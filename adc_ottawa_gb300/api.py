@@ -1,0 +1,252 @@
+"""Host-side mirror of the reference's interfaces for the ADC(2)-s hot path.
+
+Each method wraps one C-ABI entry point of libadcgpu.so and keeps the name
+and argument meaning of the Fortran routine it replaces:
+
+  write_fspace_adc2_1  source/adclib/fspacetrial.f90:533-564
+  davdiag_block        source/eigen/block_davidson.f90:33-145
+  lancdiag_block       source/eigen/block_lanczos.f90:28-81
+  silstep              source/propagation/sillib.f90:108-393
+  propagate_fvec       source/propagation/fvecprop.f90:27-105 (autocorrelation)
+
+Failures raise AdcGpuError carrying the library status code; the reference
+calls error_control/STOP in the same places (iomod.f90:94-112).
+"""
+from __future__ import annotations
+
+import ctypes as C
+from dataclasses import dataclass
+
+import numpy as np
+
+from ._native import DavInfo, DavParams, SilState, lib, ptr
+
+ADCGPU_FP64 = 0
+ADCGPU_MIXED = 1
+PRECON_DPR, PRECON_OLSEN, PRECON_MLP = 1, 2, 3
+
+STATUS = {
+    0: "ok", 1: "Illegal integration order", 2: "Stepsize underflow", 3: "Diagonalisation failed",
+    4: "Illegal initial stepsize", 10: "Not all vectors have converged", 11: "out of device memory",
+    12: "bad input", 13: "CUDA error", 14: "device wait timed out", 15: "no matrix built",
+    16: "unsupported", 17: "eigensolver failed",
+}
+
+
+class AdcGpuError(RuntimeError):
+    def __init__(self, code: int, msg: str):
+        super().__init__(f"[{code}] {STATUS.get(code, 'error')}: {msg}")
+        self.code = code
+
+
+_ip = C.POINTER(C.c_int32)
+_i64p = C.POINTER(C.c_int64)
+
+
+def synth_orbitals(nocc: int, nvirt: int, seed: int) -> np.ndarray:
+    e = np.empty(nocc + nvirt)
+    st = lib().adcgpu_synth_orbitals(nocc, nvirt, seed, ptr(e))
+    if st:
+        raise AdcGpuError(st, "synth_orbitals")
+    return e
+
+
+def eri_packed_size(nbas: int) -> int:
+    return int(lib().adcgpu_eri_packed_size(nbas))
+
+
+def synth_eri_packed(nbas: int, seed: int, nthreads: int = 0) -> np.ndarray:
+    eri = np.empty(eri_packed_size(nbas))
+    st = lib().adcgpu_synth_eri_packed(nbas, seed, ptr(eri), nthreads)
+    if st:
+        raise AdcGpuError(st, "synth_eri_packed")
+    return eri
+
+
+def synth_system(nocc: int, nvirt: int, seed: int, nthreads: int = 0):
+    """Seeded synthetic closed-shell system: (e, packed ERIs)."""
+    return synth_orbitals(nocc, nvirt, seed), synth_eri_packed(nocc + nvirt, seed, nthreads)
+
+
+def synth_uniform_block(nrow: int, ncol: int, seed: int) -> np.ndarray:
+    out = np.empty((nrow, ncol), order="F")
+    st = lib().adcgpu_synth_uniform_block(nrow, ncol, seed, ptr(out))
+    if st:
+        raise AdcGpuError(st, "synth_uniform_block")
+    return out
+
+
+def adc2s_dim(nocc: int, nvirt: int):
+    cnt = np.zeros(5, np.int32)
+    n = lib().adcgpu_adc2s_dim(nocc, nvirt, ptr(cnt, _ip))
+    return int(n), cnt
+
+
+def select_adc2s(nocc: int, nvirt: int) -> np.ndarray:
+    """kpq(7, 0:ndim) as an (ndim+1, 7) int32 array: row c is Fortran column c."""
+    ndim, _ = adc2s_dim(nocc, nvirt)
+    kpq = np.zeros((ndim + 1, 7), np.int32)
+    st = lib().adcgpu_select_adc2s(nocc, nvirt, ptr(kpq, _ip))
+    if st:
+        raise AdcGpuError(st, "select_adc2s")
+    return kpq
+
+
+@dataclass
+class DavidsonResult:
+    evals: np.ndarray
+    evecs: np.ndarray | None
+    status: int
+    iterations: int
+    nmult: int
+    nconv: int
+    seconds: float
+    sigma_seconds: float
+
+
+class AdcGpu:
+    """One device-resident ADC(2)-s problem (an adcgpu_ctx)."""
+
+    def __init__(self, device: int = 0):
+        h = C.c_void_p()
+        st = lib().adcgpu_ctx_create(device, C.byref(h))
+        if st:
+            raise AdcGpuError(st, "adcgpu_ctx_create (is a GPU visible?)")
+        self._h = h
+        self.nocc = self.nvirt = 0
+        self.ndim = 0
+        self.noffd = 0
+
+    def _check(self, st: int, what: str):
+        if st:
+            msg = lib().adcgpu_last_error(self._h)
+            raise AdcGpuError(st, f"{what}: {msg.decode() if msg else ''}")
+
+    def close(self):
+        if getattr(self, "_h", None):
+            lib().adcgpu_ctx_destroy(self._h)
+            self._h = None
+
+    def __del__(self):
+        try:
+            self.close()
+        except Exception:
+            pass
+
+    # -- inputs ---------------------------------------------------------------
+    def set_orbitals(self, nocc: int, nvirt: int, e: np.ndarray):
+        e = np.ascontiguousarray(e, np.float64)
+        self._check(lib().adcgpu_set_orbitals(self._h, nocc, nvirt, ptr(e)), "set_orbitals")
+        self.nocc, self.nvirt = nocc, nvirt
+        self.ndim = adc2s_dim(nocc, nvirt)[0]
+
+    def set_eri_packed(self, eri: np.ndarray):
+        eri = np.ascontiguousarray(eri, np.float64)
+        self._check(lib().adcgpu_set_eri_packed(self._h, ptr(eri)), "set_eri_packed")
+
+    def set_eri_mo_complex(self, buffer_real: np.ndarray):
+        """moIntegrals%buffer_real: complex (nmo,nmo,nmo,nmo), Fortran order."""
+        b = np.asarray(buffer_real, dtype=np.complex128)
+        flat = np.ascontiguousarray(b.reshape(-1, order="F")).view(np.float64)
+        self._check(lib().adcgpu_set_eri_mo_complex(self._h, ptr(flat)), "set_eri_mo_complex")
+
+    # -- builder --------------------------------------------------------------
+    def write_fspace_adc2_1(self, kpq: np.ndarray | None = None, chr: str = "i", precision: int = ADCGPU_FP64) -> int:
+        """Build H on the device; returns noffdel (kept off-diagonal count)."""
+        noff = C.c_int64(0)
+        kp = None if kpq is None else ptr(np.ascontiguousarray(kpq, np.int32), _ip)
+        self._check(lib().adcgpu_build_adc2s(self._h, self.ndim, kp, C.byref(noff), chr.encode(), precision),
+                    "write_fspace_adc2_1")
+        self.noffd = int(noff.value)
+        return self.noffd
+
+    def get_diag(self) -> np.ndarray:
+        d = np.empty(self.ndim)
+        self._check(lib().adcgpu_get_diag(self._h, ptr(d)), "get_diag")
+        return d
+
+    def export_coo(self):
+        n = self.noffd
+        h = np.empty(n)
+        oi = np.empty(n, np.int32)
+        oj = np.empty(n, np.int32)
+        self._check(lib().adcgpu_export_coo(self._h, n, ptr(h), ptr(oi, _ip), ptr(oj, _ip)), "export_coo")
+        return h, oi, oj
+
+    def write_hmlt_files(self, directory: str, flag: str = "i"):
+        self._check(lib().adcgpu_write_hmlt_files(self._h, directory.encode(), flag.encode()), "write_hmlt_files")
+
+    # -- sigma ----------------------------------------------------------------
+    def sigma(self, V: np.ndarray) -> np.ndarray:
+        V = np.asfortranarray(V, dtype=np.float64)
+        one = V.ndim == 1
+        if one:
+            V = V.reshape(-1, 1, order="F")
+        W = np.empty_like(V, order="F")
+        self._check(lib().adcgpu_sigma(self._h, V.shape[1], ptr(V), ptr(W)), "sigma")
+        return W[:, 0] if one else W
+
+    def sigma_device(self, m: int, dv: int, dw: int, ld: int):
+        self._check(lib().adcgpu_sigma_device(self._h, m, C.c_void_p(dv), C.c_void_p(dw), ld), "sigma_device")
+
+    def last_sigma_ms(self) -> float:
+        return float(lib().adcgpu_last_sigma_ms(self._h))
+
+    def device_bytes(self) -> int:
+        return int(lib().adcgpu_device_bytes(self._h))
+
+    # -- solvers --------------------------------------------------------------
+    def davdiag_block(self, davstates: int, davtol: float, dmain: int = 0, maxsubdim: int = -1, maxiter: int = 100,
+                      precon: int = PRECON_DPR, ldfl: bool = True, lsubdiag: bool = False, guessdim: int = 800,
+                      precision: int = ADCGPU_FP64, refine: int = 3, want_vectors: bool = True,
+                      raise_on_nonconv: bool = True) -> DavidsonResult:
+        p = DavParams(davstates=davstates, dmain=dmain, maxsubdim=maxsubdim, maxiter=maxiter, precon=precon,
+                      ldfl=int(ldfl), lsubdiag=int(lsubdiag), guessdim=guessdim, davtol=davtol,
+                      precision=precision, refine=refine)
+        ev = np.empty(davstates)
+        vec = np.empty((self.ndim, davstates), order="F") if want_vectors else None
+        info = DavInfo()
+        st = lib().adcgpu_davidson(self._h, C.byref(p), ptr(ev), ptr(vec), C.byref(info))
+        if st and not (st == 10 and not raise_on_nonconv):
+            self._check(st, "davdiag_block")
+        return DavidsonResult(ev, vec, st, info.iterations, info.nmult, info.nconv, info.seconds, info.sigma_seconds)
+
+    def lancdiag_block(self, q0: np.ndarray, ncycles: int, orthotype: int = 0, want_tmat: bool = True,
+                       want_evals: bool = True, want_ritz: bool = False):
+        q0 = np.asfortranarray(q0, np.float64)
+        b = q0.shape[1]
+        nvec = b * ncycles
+        T = np.empty((nvec, nvec), order="F") if want_tmat else None
+        ev = np.empty(nvec) if want_evals else None
+        R = np.empty((self.ndim, nvec), order="F") if want_ritz else None
+        self._check(lib().adcgpu_block_lanczos(self._h, b, ncycles, orthotype, ptr(q0), ptr(T), ptr(ev), ptr(R)),
+                    "lancdiag_block")
+        return T, ev, R
+
+    def silstep(self, psi: np.ndarray, dtpsi: np.ndarray, intperiod: float, intorder: int, tol: float,
+                relax: bool = False, restart: bool = True, stdform: bool = True):
+        psi = np.ascontiguousarray(psi, np.complex128)
+        dtpsi = np.ascontiguousarray(dtpsi, np.complex128)
+        step = C.c_double(0.0)
+        order = C.c_int(0)
+        state = SilState()
+        st = lib().adcgpu_silstep(self._h, ptr(psi.view(np.float64)), ptr(dtpsi.view(np.float64)), len(psi),
+                                  intperiod, intorder, tol, int(relax), int(restart), int(stdform), C.byref(step),
+                                  C.byref(order), C.byref(state))
+        self._check(st, "silstep")
+        return psi, dtpsi, step.value, order.value, state
+
+    def propagate_fvec(self, fvecs: np.ndarray, tout: float, tfinal: float, kdim: int, autotol: float):
+        """Autocorrelation a(t) of each column of fvecs (t = 0, tout, 2 tout, ...)."""
+        f = np.asfortranarray(fvecs, np.float64)
+        if f.ndim == 1:
+            f = f.reshape(-1, 1, order="F")
+        nwp = f.shape[1]
+        nt = int(tfinal / (0.5 * tout)) + 1
+        out = np.zeros((nwp, nt, 2))
+        ntimes = C.c_int(0)
+        nmult = C.c_int64(0)
+        self._check(lib().adcgpu_autocorr(self._h, nwp, ptr(f), tout, tfinal, kdim, autotol, ptr(out),
+                                          C.byref(ntimes), C.byref(nmult)), "propagate_fvec")
+        a = out[..., 0] + 1j * out[..., 1]
+        return a[:, : ntimes.value], int(nmult.value)

@@ -1,0 +1,451 @@
+// ADC(2)-s matrix build on the GPU (compiled with --fmad=false).
+//
+// Replaces get_diag_adc2_save (get_matrix.f90:267-311) and
+// get_offdiag_adc2_save_omp (get_matrix.f90:705-1186).  Every matrix element
+// is evaluated with the reference's operation order (adc_ph.f90), each
+// product and sum rounded separately, so an element lands on the same side
+// of minc = 1e-12 as in the reference and the kept structure is bit-exact.
+//
+// ERIs are read from four dense blocks gathered once from the caller's
+// integrals (8-fold symmetry makes every (pq|rs) the reference touches one of
+// (vo|vo), (vv|oo), (oo|ov), (vv|ov)).
+#include <cub/cub.cuh>
+
+#include "internal.h"
+
+namespace adcgpu {
+
+namespace {
+
+struct Eri {
+  const double* vovo;
+  const double* vvoo;
+  const double* ooov;
+  const double* vvov;
+  int no, nv;
+  __device__ double VOVO(int a, int i, int b, int j) const {
+    return vovo[(((int64_t)a * no + i) * nv + b) * no + j];
+  }
+  __device__ double VVOO(int a, int b, int i, int j) const {
+    return vvoo[(((int64_t)a * nv + b) * no + i) * no + j];
+  }
+  __device__ double OOOV(int i, int j, int k, int a) const {
+    return ooov[(((int64_t)i * no + j) * no + k) * nv + a];
+  }
+  __device__ double VVOV(int a, int b, int i, int c) const {
+    return vvov[(((int64_t)a * nv + b) * no + i) * nv + c];
+  }
+};
+
+__host__ __device__ inline int64_t canon(int64_t p, int64_t q, int64_t r, int64_t s) {
+  int64_t pq = p >= q ? p * (p + 1) / 2 + q : q * (q + 1) / 2 + p;
+  int64_t rs = r >= s ? r * (r + 1) / 2 + s : s * (s + 1) / 2 + r;
+  return pq >= rs ? pq * (pq + 1) / 2 + rs : rs * (rs + 1) / 2 + pq;
+}
+
+// Gather one ERI block from the canonical packed array.
+// kind 0: (a i|b j) 1: (a b|i j) 2: (i j|k a) 3: (a b|i c)
+__global__ void k_gather_block(const double* __restrict__ packed, double* __restrict__ out, int kind,
+                               int no, int nv, int64_t total) {
+  for (int64_t t = blockIdx.x * (int64_t)blockDim.x + threadIdx.x; t < total;
+       t += (int64_t)gridDim.x * blockDim.x) {
+    int64_t x = t;
+    int p, q, r, s;
+    switch (kind) {
+      case 0: { int j = x % no; x /= no; int b = x % nv; x /= nv; int i = x % no; int a = (int)(x / no);
+                p = no + a; q = i; r = no + b; s = j; } break;
+      case 1: { int j = x % no; x /= no; int i = x % no; x /= no; int b = x % nv; int a = (int)(x / nv);
+                p = no + a; q = no + b; r = i; s = j; } break;
+      case 2: { int a = x % nv; x /= nv; int k = x % no; x /= no; int j = x % no; int i = (int)(x / no);
+                p = i; q = j; r = k; s = no + a; } break;
+      default: { int c = x % nv; x /= nv; int i = x % no; x /= no; int b = x % nv; int a = (int)(x / nv);
+                 p = no + a; q = no + b; r = i; s = no + c; } break;
+    }
+    out[t] = packed[canon(p, q, r, s)];
+  }
+}
+
+// CA_ph_ph(a,a1), adc_ph.f90:769-812, for a <= a1 (0-based virtuals).
+__global__ void k_ca(Eri E, const double* __restrict__ e, double* __restrict__ ca) {
+  const int no = E.no, nv = E.nv;
+  int64_t t = blockIdx.x * (int64_t)blockDim.x + threadIdx.x;
+  if (t >= (int64_t)nv * nv) return;
+  int a = (int)(t / nv), a1 = (int)(t % nv);
+  if (a > a1) return;
+  const double ea = e[no + a], ea1 = e[no + a1];
+  double acc = 0.0;
+  for (int r = 0; r < nv; ++r)
+    for (int u = 0; u < no; ++u)
+      for (int v = 0; v < no; ++v) {
+        double eijc = e[u] + e[v] - e[no + r];
+        double DA = (eijc - 0.5 * (ea + ea1)) / ((eijc - ea) * (eijc - ea1));
+        double term = 0.0;
+        term = term + E.VOVO(a, u, r, v) * (2.0 * E.VOVO(a1, u, r, v) - E.VOVO(r, u, a1, v));
+        term = term + E.VOVO(a, v, r, u) * (2.0 * E.VOVO(r, u, a1, v) - E.VOVO(a1, u, r, v));
+        term = DA * term;
+        acc = acc + term;
+      }
+  double x = -0.5 * acc;
+  ca[(int64_t)a * nv + a1] = x;
+  ca[(int64_t)a1 * nv + a] = x;
+}
+
+// CB_ph_ph(k,k1), adc_ph.f90:819-912 ("dumbed down" branch), k <= k1.
+__global__ void k_cb(Eri E, const double* __restrict__ e, double* __restrict__ cb) {
+  const int no = E.no, nv = E.nv;
+  int t = blockIdx.x * blockDim.x + threadIdx.x;
+  if (t >= no * no) return;
+  int k = t / no, k1 = t % no;
+  if (k > k1) return;
+  const double ek = e[k], ek1 = e[k1];
+  double acc = 0.0;
+  for (int r = 0; r < nv; ++r)
+    for (int s = 0; s < nv; ++s)
+      for (int u = 0; u < no; ++u) {
+        double eicd = e[u] - e[no + r] - e[no + s];
+        double DB = (eicd + 0.5 * (ek + ek1)) / ((eicd + ek) * (eicd + ek1));
+        double term = 0.0;
+        term = term + E.VOVO(r, k, s, u) * (2.0 * E.VOVO(r, k1, s, u) - E.VOVO(s, k1, r, u));
+        term = term + E.VOVO(r, u, s, k) * (2.0 * E.VOVO(s, k1, r, u) - E.VOVO(r, k1, s, u));
+        term = DB * term;
+        acc = acc + term;
+      }
+  double x = -0.5 * acc;
+  cb[k * no + k1] = x;
+  cb[k1 * no + k] = x;
+}
+
+// Per (single, (c,i)) tables for CC_ph_ph (adc_ph.f90:918-957):
+//   X[s][t]  = 2 (a k|c i) - (a i|c k)       the first factor of term
+//   D1[s][t] = e(k) - e(a) + (e(i) - e(c))   one factor of the DC denominator
+// with t = c*no + i (c outer, i inner: the reference's loop order).
+__global__ void k_cc_tables(Eri E, const double* __restrict__ e, double* __restrict__ X,
+                            double* __restrict__ D1) {
+  const int no = E.no, nv = E.nv;
+  const int64_t n1 = (int64_t)no * nv, nt = n1;
+  for (int64_t idx = blockIdx.x * (int64_t)blockDim.x + threadIdx.x; idx < n1 * nt;
+       idx += (int64_t)gridDim.x * blockDim.x) {
+    int64_t s = idx / nt, t = idx % nt;
+    int a = (int)(s / no), k = (int)(s % no);
+    int c = (int)(t / no), i = (int)(t % no);
+    X[idx] = 2.0 * E.VOVO(a, k, c, i) - E.VOVO(a, i, c, k);
+    double eic = e[i] - e[no + c];
+    D1[idx] = e[k] - e[no + a] + eic;
+  }
+}
+
+constexpr int PT = 16;   // ph-ph tile (PT x PT elements per block)
+constexpr int TK = 32;   // t-chunk staged in shared memory
+
+// ph-ph block (get_matrix.f90:848-884) and singles diagonal (:286-294).
+// Each thread evaluates one element (s1 <= s2) with the exact serial CC sum.
+__global__ void __launch_bounds__(PT * PT) k_phph(Eri E, const double* __restrict__ e,
+                                                  const double* __restrict__ X, const double* __restrict__ D1,
+                                                  const double* __restrict__ ca, const double* __restrict__ cb,
+                                                  double* __restrict__ A, double* __restrict__ hii,
+                                                  unsigned long long* __restrict__ kept) {
+  const int no = E.no, nv = E.nv;
+  const int n1 = no * nv, nt = n1;
+  const int bi = blockIdx.y, bj = blockIdx.x;
+  if (bj < bi) return;                 // upper-triangle tiles only
+  __shared__ double sX1[PT][TK + 1], sD1[PT][TK + 1], sX2[PT][TK + 1], sD2[PT][TK + 1], sEic[TK];
+  const int ty = threadIdx.y, tx = threadIdx.x;
+  const int s1 = bi * PT + ty, s2 = bj * PT + tx;
+  const int tid = ty * PT + tx;
+  double hv = 0.0;
+  if (s1 < n1 && s2 < n1) {
+    int a = s1 / no, k = s1 % no, a1 = s2 / no, k1 = s2 % no;
+    hv = 0.5 * (e[k] + e[k1] - e[no + a] - e[no + a1]);
+  }
+  double cc = 0.0;
+  for (int t0 = 0; t0 < nt; t0 += TK) {
+    __syncthreads();
+    for (int l = tid; l < PT * TK; l += PT * PT) {
+      int r = l / TK, c = l % TK;
+      int t = t0 + c;
+      int r1 = bi * PT + r, r2 = bj * PT + r;
+      bool ok = t < nt;
+      sX1[r][c] = (ok && r1 < n1) ? X[(int64_t)r1 * nt + t] : 0.0;
+      sD1[r][c] = (ok && r1 < n1) ? D1[(int64_t)r1 * nt + t] : 1.0;
+      sX2[r][c] = (ok && r2 < n1) ? X[(int64_t)r2 * nt + t] : 0.0;
+      sD2[r][c] = (ok && r2 < n1) ? D1[(int64_t)r2 * nt + t] : 1.0;
+    }
+    for (int l = tid; l < TK; l += PT * PT) {
+      int t = t0 + l;
+      sEic[l] = t < nt ? (e[t % no] - e[no + t / no]) : 0.0;
+    }
+    __syncthreads();
+    const int tl = min(TK, nt - t0);
+    for (int c = 0; c < tl; ++c) {
+      double DC = (hv + sEic[c]) / (sD1[ty][c] * sD2[tx][c]);
+      double term = sX1[ty][c] * sX2[tx][c];
+      term = term * DC;
+      cc = cc + term;
+    }
+  }
+  if (s1 >= n1 || s2 >= n1 || s2 < s1) return;
+  const int a = s1 / no, k = s1 % no, a1 = s2 / no, k1 = s2 % no;
+  if (s1 == s2) {
+    double x = e[no + a] - e[k];                                   // K_ph_ph
+    x = x + (2.0 * E.VOVO(a, k, a, k) - E.VVOO(a, a, k, k));       // C1_ph_ph
+    x = x + ca[(int64_t)a * nv + a];                               // CA_ph_ph(a,a)
+    x = x + cb[k * no + k];                                        // CB_ph_ph(k,k)
+    x = x + cc;                                                    // CC_ph_ph
+    hii[s1] = x;
+    A[(int64_t)s1 * n1 + s1] = 0.0;
+    return;
+  }
+  double x = 2.0 * E.VOVO(a, k, a1, k1) - E.VVOO(a, a1, k, k1);  // C1_ph_ph
+  if (k == k1) x = x + ca[(int64_t)a * nv + a1];
+  if (a == a1) x = x + cb[k * no + k1];
+  x = x + cc;
+  double keep = fabs(x) > MINC ? x : 0.0;
+  A[(int64_t)s1 * n1 + s2] = keep;
+  A[(int64_t)s2 * n1 + s1] = keep;
+  if (keep != 0.0) atomicAdd(kept, 1ull);
+}
+
+// 2p2h diagonal K_2p2h_2p2h (get_matrix.f90:303-306, adc_ph.f90:1090-1096).
+__global__ void k_diag2(GeomDev g, const double* __restrict__ e, double* __restrict__ hii) {
+  for (int64_t d = blockIdx.x * (int64_t)blockDim.x + threadIdx.x; d < g.n2;
+       d += (int64_t)gridDim.x * blockDim.x) {
+    Double r = decode_double(g, d);
+    const int no = g.no;
+    hii[g.n1 + d] = e[no + r.ap] + e[no + r.bp] - e[r.kp] - e[r.lp];
+  }
+}
+
+// ph-2p2h coupling value of single (a,k) with double r (adc_ph.f90:974-1073),
+// in the argument mapping of get_matrix.f90:900,931,964,997,1030.
+__device__ inline double coupling(const Eri& E, int a, int k, const Double& r) {
+  const int ap = r.ap, bp = r.bp, kp = r.kp, lp = r.lp;
+  double f = 0.0;
+  switch (r.cls) {
+    case 0:   // C5_ph_2p2h(a,k,a',k')
+      if (a == ap) f = f + E.OOOV(kp, k, kp, ap);
+      if (k == kp) f = f - E.VVOV(a, ap, kp, ap);
+      return sqrt(2.0) * f;
+    case 1:   // C4_ph_2p2h(a,k,a',b',k')
+      if (a == ap) f = f + E.OOOV(kp, k, kp, bp);
+      if (a == bp) f = f + E.OOOV(kp, k, kp, ap);
+      if (k == kp) f = f - (E.VVOV(a, ap, kp, bp) + E.VVOV(a, bp, kp, ap));
+      return f;
+    case 2:   // C3_ph_2p2h(a,k,a',k',l')
+      if (a == ap) f = f - (E.OOOV(kp, k, lp, ap) + E.OOOV(lp, k, kp, ap));
+      if (k == kp) f = f + E.VVOV(a, ap, lp, ap);
+      if (k == lp) f = f + E.VVOV(a, ap, kp, ap);
+      return f;
+    case 3:   // C1_ph_2p2h(a,k,a',b',k',l')
+      if (a == ap) f = f - (E.OOOV(kp, k, lp, bp) + E.OOOV(lp, k, kp, bp));
+      if (a == bp) f = f - (E.OOOV(kp, k, lp, ap) + E.OOOV(lp, k, kp, ap));
+      if (k == kp) f = f + (E.VVOV(a, ap, lp, bp) + E.VVOV(a, bp, lp, ap));
+      if (k == lp) f = f + (E.VVOV(a, ap, kp, bp) + E.VVOV(a, bp, kp, ap));
+      return f / sqrt(2.0);
+    default:  // C2_ph_2p2h(a,k,a',b',k',l')
+      if (a == ap) f = f - (E.OOOV(kp, k, lp, bp) - E.OOOV(lp, k, kp, bp));
+      if (a == bp) f = f + (E.OOOV(kp, k, lp, ap) - E.OOOV(lp, k, kp, ap));
+      if (k == kp) f = f + (E.VVOV(a, ap, lp, bp) - E.VVOV(a, bp, lp, ap));
+      if (k == lp) f = f - (E.VVOV(a, ap, kp, bp) - E.VVOV(a, bp, kp, ap));
+      return sqrt(3.0) * f / sqrt(2.0);
+  }
+}
+
+// One warp per double row: evaluates its structural entries, applies the
+// minc threshold (get_matrix.f90:904 etc.) and counts the kept ones.
+__global__ void k_coupling(Eri E, GeomDev g, double* __restrict__ Bt, int64_t* __restrict__ rowcount) {
+  const int lane = threadIdx.x & 31;
+  const int64_t warp = (blockIdx.x * (int64_t)blockDim.x + threadIdx.x) >> 5;
+  const int64_t nwarps = ((int64_t)gridDim.x * blockDim.x) >> 5;
+  for (int64_t d = warp; d < g.n2; d += nwarps) {
+    Double r = decode_double(g, d);
+    const int64_t L = g.len[r.cls];
+    double* row = Bt + g.off[r.cls] + (d - g.start[r.cls]) * L;
+    int cnt = 0;
+    for (int e = lane; e < L; e += 32) {
+      int64_t s = entry_single(g, r, e);
+      int a = (int)(s / g.no), k = (int)(s % g.no);
+      double x = coupling(E, a, k, r);
+      bool keep = fabs(x) > MINC;
+      row[e] = keep ? x : 0.0;
+      cnt += keep;
+    }
+    for (int o = 16; o; o >>= 1) cnt += __shfl_xor_sync(0xffffffffu, cnt, o);
+    if (lane == 0) rowcount[d] = cnt;
+  }
+}
+
+// COO export -----------------------------------------------------------------
+__global__ void k_count_phph_rows(const double* __restrict__ A, int n1, int64_t* __restrict__ cnt) {
+  int s1 = blockIdx.x;
+  int c = 0;
+  for (int s2 = s1 + 1 + threadIdx.x; s2 < n1; s2 += blockDim.x) c += A[(int64_t)s1 * n1 + s2] != 0.0;
+  __shared__ int red[32];
+  for (int o = 16; o; o >>= 1) c += __shfl_xor_sync(0xffffffffu, c, o);
+  if ((threadIdx.x & 31) == 0) red[threadIdx.x >> 5] = c;
+  __syncthreads();
+  if (threadIdx.x == 0) {
+    int t = 0;
+    for (int w = 0; w < (int)(blockDim.x >> 5); ++w) t += red[w];
+    cnt[s1] = t;
+  }
+}
+
+__global__ void k_export_phph(const double* __restrict__ A, int n1, const int64_t* __restrict__ pos,
+                              double* __restrict__ h, int32_t* __restrict__ oi, int32_t* __restrict__ oj) {
+  // one block per row; the block compacts in order with a warp-ballot scan
+  int s1 = blockIdx.x;
+  __shared__ int64_t base;
+  __shared__ int wsum[32];
+  if (threadIdx.x == 0) base = pos[s1];
+  __syncthreads();
+  const int lane = threadIdx.x & 31, w = threadIdx.x >> 5, nw = blockDim.x >> 5;
+  for (int s0 = s1 + 1; s0 < n1; s0 += blockDim.x) {
+    int s2 = s0 + threadIdx.x;
+    double x = s2 < n1 ? A[(int64_t)s1 * n1 + s2] : 0.0;
+    bool k = s2 < n1 && x != 0.0;
+    unsigned m = __ballot_sync(0xffffffffu, k);
+    int before = __popc(m & ((1u << lane) - 1));
+    if (lane == 0) wsum[w] = __popc(m);
+    __syncthreads();
+    int64_t off = base;
+    for (int q = 0; q < w; ++q) off += wsum[q];
+    if (k) { h[off + before] = x; oi[off + before] = s1 + 1; oj[off + before] = s2 + 1; }
+    __syncthreads();
+    if (threadIdx.x == 0) { int64_t t = 0; for (int q = 0; q < nw; ++q) t += wsum[q]; base += t; }
+    __syncthreads();
+  }
+}
+
+__global__ void k_export_coupling(GeomDev g, const double* __restrict__ Bt, const int64_t* __restrict__ pos,
+                                  double* __restrict__ h, int32_t* __restrict__ oi, int32_t* __restrict__ oj) {
+  const int lane = threadIdx.x & 31;
+  const int64_t warp = (blockIdx.x * (int64_t)blockDim.x + threadIdx.x) >> 5;
+  const int64_t nwarps = ((int64_t)gridDim.x * blockDim.x) >> 5;
+  for (int64_t d = warp; d < g.n2; d += nwarps) {
+    Double r = decode_double(g, d);
+    const int64_t L = g.len[r.cls];
+    const double* row = Bt + g.off[r.cls] + (d - g.start[r.cls]) * L;
+    int64_t base = pos[d];
+    for (int e0 = 0; e0 < L; e0 += 32) {
+      int e = e0 + lane;
+      double x = e < L ? row[e] : 0.0;
+      bool k = e < L && x != 0.0;
+      unsigned m = __ballot_sync(0xffffffffu, k);
+      if (k) {
+        int64_t o = base + __popc(m & ((1u << lane) - 1));
+        h[o] = x;
+        oi[o] = (int32_t)(entry_single(g, r, e) + 1);
+        oj[o] = (int32_t)(g.n1 + d + 1);
+      }
+      base += __popc(m);
+    }
+  }
+}
+
+inline int grid_for(int64_t n, int block) {
+  int64_t g = (n + block - 1) / block;
+  return (int)std::min<int64_t>(std::max<int64_t>(g, 1), 152LL * 32);
+}
+
+}  // namespace
+
+int build_eri_blocks_from_packed(Ctx* c, const double* d_packed) {
+  const int no = c->geom.no, nv = c->geom.nv;
+  const int64_t sz[4] = {(int64_t)nv * no * nv * no, (int64_t)nv * nv * no * no,
+                         (int64_t)no * no * no * nv, (int64_t)nv * nv * no * nv};
+  double** dst[4] = {&c->d_vovo, &c->d_vvoo, &c->d_ooov, &c->d_vvov};
+  for (int k = 0; k < 4; ++k) {
+    if (*dst[k]) { dfree(c, *dst[k], 0); *dst[k] = nullptr; }
+    int st = dmalloc(c, (void**)dst[k], sizeof(double) * sz[k]);
+    if (st) return st;
+    k_gather_block<<<grid_for(sz[k], 256), 256, 0, c->stream>>>(d_packed, *dst[k], k, no, nv, sz[k]);
+    ADC_CUDA(c, cudaGetLastError());
+  }
+  ADC_CUDA(c, cudaStreamSynchronize(c->stream));
+  return ADCGPU_OK;
+}
+
+int build_matrix(Ctx* c) {
+  const Geometry& G = c->geom;
+  const int no = G.no, nv = G.nv;
+  const int64_t n1 = G.n1;
+  GeomDev g = to_dev(G);
+  Eri E{c->d_vovo, c->d_vvoo, c->d_ooov, c->d_vvov, no, nv};
+  cudaStream_t s = c->stream;
+  double *d_ca = nullptr, *d_cb = nullptr, *d_X = nullptr, *d_D1 = nullptr;
+  unsigned long long* d_kept = nullptr;
+  int st;
+  if ((st = dmalloc(c, (void**)&d_ca, sizeof(double) * nv * nv))) return st;
+  if ((st = dmalloc(c, (void**)&d_cb, sizeof(double) * no * no))) return st;
+  if ((st = dmalloc(c, (void**)&d_X, sizeof(double) * n1 * n1))) return st;
+  if ((st = dmalloc(c, (void**)&d_D1, sizeof(double) * n1 * n1))) return st;
+  if ((st = dmalloc(c, (void**)&d_kept, sizeof(unsigned long long)))) return st;
+  ADC_CUDA(c, cudaMemsetAsync(d_kept, 0, sizeof(unsigned long long), s));
+  if (!c->d_diag && (st = dmalloc(c, (void**)&c->d_diag, sizeof(double) * G.N))) return st;
+  if (!c->d_A && (st = dmalloc(c, (void**)&c->d_A, sizeof(double) * n1 * n1))) return st;
+  if (!c->d_Bt && (st = dmalloc(c, (void**)&c->d_Bt, sizeof(double) * G.off[5]))) return st;
+  if (!c->d_rowcount && (st = dmalloc(c, (void**)&c->d_rowcount, sizeof(int64_t) * (G.n2 + n1 + 1))))
+    return st;
+
+  k_ca<<<(int)((nv * (int64_t)nv + 127) / 128), 128, 0, s>>>(E, c->d_e, d_ca);
+  k_cb<<<(no * no + 63) / 64, 64, 0, s>>>(E, c->d_e, d_cb);
+  k_cc_tables<<<grid_for(n1 * n1, 256), 256, 0, s>>>(E, c->d_e, d_X, d_D1);
+  ADC_CUDA(c, cudaGetLastError());
+  dim3 tiles((unsigned)((n1 + PT - 1) / PT), (unsigned)((n1 + PT - 1) / PT));
+  k_phph<<<tiles, dim3(PT, PT), 0, s>>>(E, c->d_e, d_X, d_D1, d_ca, d_cb, c->d_A, c->d_diag, d_kept);
+  ADC_CUDA(c, cudaGetLastError());
+  k_diag2<<<grid_for(G.n2, 256), 256, 0, s>>>(g, c->d_e, c->d_diag);
+  k_coupling<<<152 * 8, 256, 0, s>>>(E, g, c->d_Bt, c->d_rowcount + n1);
+  ADC_CUDA(c, cudaGetLastError());
+  unsigned long long kept_ph = 0;
+  ADC_CUDA(c, cudaMemcpyAsync(&kept_ph, d_kept, sizeof(kept_ph), cudaMemcpyDeviceToHost, s));
+  // total kept coupling entries
+  int64_t* d_sum = nullptr;
+  if ((st = dmalloc(c, (void**)&d_sum, sizeof(int64_t)))) return st;
+  size_t tmp_bytes = 0;
+  cub::DeviceReduce::Sum(nullptr, tmp_bytes, c->d_rowcount + n1, d_sum, G.n2, s);
+  void* d_tmp = nullptr;
+  if ((st = dmalloc(c, &d_tmp, tmp_bytes))) return st;
+  cub::DeviceReduce::Sum(d_tmp, tmp_bytes, c->d_rowcount + n1, d_sum, G.n2, s);
+  int64_t kept_b = 0;
+  ADC_CUDA(c, cudaMemcpyAsync(&kept_b, d_sum, sizeof(int64_t), cudaMemcpyDeviceToHost, s));
+  ADC_CUDA(c, cudaStreamSynchronize(s));
+  c->nnz_ph = (int64_t)kept_ph;
+  c->nnz_kept = (int64_t)kept_ph + kept_b;
+  dfree(c, d_tmp, tmp_bytes);
+  dfree(c, d_sum, sizeof(int64_t));
+  dfree(c, d_ca, sizeof(double) * nv * nv);
+  dfree(c, d_cb, sizeof(double) * no * no);
+  dfree(c, d_X, sizeof(double) * n1 * n1);
+  dfree(c, d_D1, sizeof(double) * n1 * n1);
+  dfree(c, d_kept, sizeof(unsigned long long));
+  return ADCGPU_OK;
+}
+
+int export_coo_device(Ctx* c, double* d_h, int32_t* d_oi, int32_t* d_oj) {
+  const Geometry& G = c->geom;
+  const int n1 = (int)G.n1;
+  GeomDev g = to_dev(G);
+  cudaStream_t s = c->stream;
+  int64_t* d_cnt = c->d_rowcount;      // [0,n1): ph-ph rows, [n1, n1+n2): doubles
+  k_count_phph_rows<<<n1, 256, 0, s>>>(c->d_A, n1, d_cnt);
+  ADC_CUDA(c, cudaGetLastError());
+  int64_t* d_pos = nullptr;
+  int st;
+  const int64_t nrows = G.n1 + G.n2;
+  if ((st = dmalloc(c, (void**)&d_pos, sizeof(int64_t) * (nrows + 1)))) return st;
+  size_t tmp_bytes = 0;
+  cub::DeviceScan::ExclusiveSum(nullptr, tmp_bytes, d_cnt, d_pos, nrows, s);
+  void* d_tmp = nullptr;
+  if ((st = dmalloc(c, &d_tmp, tmp_bytes))) return st;
+  cub::DeviceScan::ExclusiveSum(d_tmp, tmp_bytes, d_cnt, d_pos, nrows, s);
+  k_export_phph<<<n1, 256, 0, s>>>(c->d_A, n1, d_pos, d_h, d_oi, d_oj);
+  k_export_coupling<<<152 * 8, 256, 0, s>>>(g, c->d_Bt, d_pos + n1, d_h, d_oi, d_oj);
+  ADC_CUDA(c, cudaGetLastError());
+  ADC_CUDA(c, cudaStreamSynchronize(s));
+  dfree(c, d_tmp, tmp_bytes);
+  dfree(c, d_pos, sizeof(int64_t) * (nrows + 1));
+  return ADCGPU_OK;
+}
+
+}  // namespace adcgpu

@@ -1,0 +1,387 @@
+// Context management, integral upload and the builder / sigma entry points
+// of the C ABI (include/adcgpu.h).
+#include <algorithm>
+#include <cstdio>
+#include <cstring>
+#include <vector>
+
+#include "internal.h"
+
+namespace adcgpu {
+
+int set_err(Ctx* c, int code, const std::string& msg) {
+  if (c) c->err = msg;
+  return code;
+}
+
+int dmalloc(Ctx* c, void** p, size_t bytes) {
+  *p = nullptr;
+  if (bytes == 0) bytes = 16;
+  cudaError_t e = cudaMalloc(p, bytes);
+  if (e != cudaSuccess) {
+    cudaGetLastError();
+    char buf[160];
+    snprintf(buf, sizeof buf, "cudaMalloc(%zu bytes): %s", bytes, cudaGetErrorString(e));
+    return set_err(c, e == cudaErrorMemoryAllocation ? ADCGPU_OUT_OF_MEMORY : ADCGPU_CUDA_ERROR, buf);
+  }
+  c->dev_bytes += (int64_t)bytes;
+  return ADCGPU_OK;
+}
+
+void dfree(Ctx* c, void* p, size_t bytes) {
+  if (!p) return;
+  cudaFree(p);
+  if (bytes) c->dev_bytes -= (int64_t)bytes;
+}
+
+int prepare_desc(Ctx* c);
+
+static void free_matrix(Ctx* c) {
+  void** ps[] = {(void**)&c->d_diag, (void**)&c->d_A, (void**)&c->d_Bt, (void**)&c->d_A32, (void**)&c->d_Bt16,
+                 (void**)&c->d_Bt32, (void**)&c->d_diag32, (void**)&c->d_rowcount, &c->d_ws};
+  for (void** p : ps) {
+    if (*p) cudaFree(*p);
+    *p = nullptr;
+  }
+  c->ws_bytes = 0;
+  c->have_matrix = false;
+}
+
+static void free_eri(Ctx* c) {
+  double** ps[] = {&c->d_vovo, &c->d_vvoo, &c->d_ooov, &c->d_vvov};
+  for (double** p : ps) {
+    if (*p) cudaFree(*p);
+    *p = nullptr;
+  }
+  c->have_eri = false;
+}
+
+}  // namespace adcgpu
+
+using namespace adcgpu;
+
+#define CTX_CHECK(ctx)                     \
+  do {                                     \
+    if (!(ctx)) return ADCGPU_BAD_INPUT;   \
+    cudaSetDevice((ctx)->device);          \
+  } while (0)
+
+extern "C" {
+
+int adcgpu_ctx_create(int device, adcgpu_ctx** out) {
+  if (!out) return ADCGPU_BAD_INPUT;
+  *out = nullptr;
+  int ndev = 0;
+  if (cudaGetDeviceCount(&ndev) != cudaSuccess || ndev == 0) {
+    cudaGetLastError();
+    return ADCGPU_CUDA_ERROR;
+  }
+  if (device < 0 || device >= ndev) return ADCGPU_BAD_INPUT;
+  if (cudaSetDevice(device) != cudaSuccess) return ADCGPU_CUDA_ERROR;
+  Ctx* c = new Ctx;
+  c->device = device;
+  if (cudaStreamCreateWithFlags(&c->stream, cudaStreamNonBlocking) != cudaSuccess ||
+      cudaEventCreate(&c->ev0) != cudaSuccess || cudaEventCreate(&c->ev1) != cudaSuccess) {
+    delete c;
+    return ADCGPU_CUDA_ERROR;
+  }
+  *out = reinterpret_cast<adcgpu_ctx*>(c);
+  return ADCGPU_OK;
+}
+
+int adcgpu_ctx_destroy(adcgpu_ctx* h) {
+  Ctx* c = reinterpret_cast<Ctx*>(h);
+  if (!c) return ADCGPU_OK;
+  cudaSetDevice(c->device);
+  cudaStreamSynchronize(c->stream);
+  free_matrix(c);
+  free_eri(c);
+  if (c->d_e) cudaFree(c->d_e);
+  if (c->d_sil) cudaFree(c->d_sil);
+  cudaEventDestroy(c->ev0);
+  cudaEventDestroy(c->ev1);
+  cudaStreamDestroy(c->stream);
+  delete c;
+  return ADCGPU_OK;
+}
+
+const char* adcgpu_last_error(const adcgpu_ctx* h) {
+  const Ctx* c = reinterpret_cast<const Ctx*>(h);
+  return c ? c->err.c_str() : "null context";
+}
+
+int adcgpu_set_orbitals(adcgpu_ctx* h, int nocc, int nvirt, const double* e) {
+  Ctx* c = reinterpret_cast<Ctx*>(h);
+  CTX_CHECK(c);
+  if (nocc <= 0 || nvirt <= 1 || nocc > 255 || nvirt > 65535 || !e)
+    return set_err(c, ADCGPU_BAD_INPUT, "nocc in [1,255], nvirt in [2,65535] and e required");
+  Geometry g;
+  g.init(nocc, nvirt);
+  if (g.N > INT32_MAX) return set_err(c, ADCGPU_UNSUPPORTED, "ADC(2) dimension exceeds int32 kpq indexing");
+  free_matrix(c);
+  free_eri(c);
+  c->geom = g;
+  c->e.assign(e, e + nocc + nvirt);
+  if (c->d_e) cudaFree(c->d_e);
+  c->d_e = nullptr;
+  int st = dmalloc(c, (void**)&c->d_e, sizeof(double) * (nocc + nvirt));
+  if (st) return st;
+  ADC_CUDA(c, cudaMemcpy(c->d_e, e, sizeof(double) * (nocc + nvirt), cudaMemcpyHostToDevice));
+  c->have_orb = true;
+  return ADCGPU_OK;
+}
+
+int adcgpu_set_eri_packed(adcgpu_ctx* h, const double* eri) {
+  Ctx* c = reinterpret_cast<Ctx*>(h);
+  CTX_CHECK(c);
+  if (!c->have_orb) return set_err(c, ADCGPU_BAD_INPUT, "set orbitals first");
+  if (!eri) return set_err(c, ADCGPU_BAD_INPUT, "null eri");
+  free_eri(c);
+  const int nbas = c->geom.no + c->geom.nv;
+  const int64_t n = adcgpu_eri_packed_size(nbas);
+  double* d_packed = nullptr;
+  int st = dmalloc(c, (void**)&d_packed, sizeof(double) * n);
+  if (st) return st;
+  ADC_CUDA(c, cudaMemcpyAsync(d_packed, eri, sizeof(double) * n, cudaMemcpyHostToDevice, c->stream));
+  st = build_eri_blocks_from_packed(c, d_packed);
+  dfree(c, d_packed, sizeof(double) * n);
+  if (st) return st;
+  c->have_eri = true;
+  return ADCGPU_OK;
+}
+
+int adcgpu_set_eri_mo_complex(adcgpu_ctx* h, const double* buf) {
+  Ctx* c = reinterpret_cast<Ctx*>(h);
+  CTX_CHECK(c);
+  if (!c->have_orb) return set_err(c, ADCGPU_BAD_INPUT, "set orbitals first");
+  if (!buf) return set_err(c, ADCGPU_BAD_INPUT, "null buffer");
+  free_eri(c);
+  const int no = c->geom.no, nv = c->geom.nv;
+  const int64_t n = no + nv;
+  // Real part of buffer_real(r,s,u,v), column-major complex (vpqrsmod.f90:24)
+  auto V = [&](int64_t r, int64_t s, int64_t u, int64_t v) {
+    return buf[2 * (((v * n + u) * n + s) * n + r)];
+  };
+  const int64_t sz[4] = {(int64_t)nv * no * nv * no, (int64_t)nv * nv * no * no, (int64_t)no * no * no * nv,
+                         (int64_t)nv * nv * no * nv};
+  double** dst[4] = {&c->d_vovo, &c->d_vvoo, &c->d_ooov, &c->d_vvov};
+  for (int k = 0; k < 4; ++k) {
+    std::vector<double> hb(sz[k]);
+#pragma omp parallel for schedule(static)
+    for (int64_t t = 0; t < sz[k]; ++t) {
+      int64_t x = t;
+      int64_t p, q, r, s;
+      switch (k) {
+        case 0: { int64_t j = x % no; x /= no; int64_t b = x % nv; x /= nv; int64_t i = x % no; int64_t a = x / no;
+                  p = no + a; q = i; r = no + b; s = j; } break;
+        case 1: { int64_t j = x % no; x /= no; int64_t i = x % no; x /= no; int64_t b = x % nv; int64_t a = x / nv;
+                  p = no + a; q = no + b; r = i; s = j; } break;
+        case 2: { int64_t a = x % nv; x /= nv; int64_t kk = x % no; x /= no; int64_t j = x % no; int64_t i = x / no;
+                  p = i; q = j; r = kk; s = no + a; } break;
+        default: { int64_t cc = x % nv; x /= nv; int64_t i = x % no; x /= no; int64_t b = x % nv; int64_t a = x / nv;
+                   p = no + a; q = no + b; r = i; s = no + cc; } break;
+      }
+      hb[t] = V(p, q, r, s);
+    }
+    int st = dmalloc(c, (void**)dst[k], sizeof(double) * sz[k]);
+    if (st) return st;
+    ADC_CUDA(c, cudaMemcpy(*dst[k], hb.data(), sizeof(double) * sz[k], cudaMemcpyHostToDevice));
+  }
+  c->have_eri = true;
+  return ADCGPU_OK;
+}
+
+int adcgpu_build_adc2s(adcgpu_ctx* h, int ndim, const int32_t* kpq, int64_t* noffd_out, char flag, int precision) {
+  Ctx* c = reinterpret_cast<Ctx*>(h);
+  CTX_CHECK(c);
+  if (!c->have_orb || !c->have_eri) return set_err(c, ADCGPU_BAD_INPUT, "orbitals and ERIs must be set");
+  if (ndim != c->geom.N) return set_err(c, ADCGPU_BAD_INPUT, "ndim does not match nocc/nvirt");
+  if (precision != ADCGPU_FP64 && precision != ADCGPU_MIXED) return set_err(c, ADCGPU_BAD_INPUT, "precision");
+  if (kpq) {
+    std::vector<int32_t> ref((size_t)7 * (ndim + 1));
+    adcgpu_select_adc2s(c->geom.no, c->geom.nv, ref.data());
+    for (size_t i = 0; i < ref.size(); ++i)
+      if (ref[i] != kpq[i] && !(i >= 5 && i < 7))
+        return set_err(c, ADCGPU_UNSUPPORTED,
+                       "kpq is not the C1 ADC(2)-s list of select_atom_is/select_atom_d (flag -1)");
+  }
+  free_matrix(c);
+  int st = build_matrix(c);
+  if (st) return st;
+  st = prepare_desc(c);
+  if (st) return st;
+  c->precision = precision;
+  if (precision == ADCGPU_MIXED) {
+    st = prepare_mixed(c);
+    if (st) return st;
+  }
+  ADC_CUDA(c, cudaStreamSynchronize(c->stream));
+  c->flag = flag;
+  c->have_matrix = true;
+  if (noffd_out) *noffd_out = c->nnz_kept;
+  return ADCGPU_OK;
+}
+
+int adcgpu_get_diag(adcgpu_ctx* h, double* hii) {
+  Ctx* c = reinterpret_cast<Ctx*>(h);
+  CTX_CHECK(c);
+  if (!c->have_matrix) return set_err(c, ADCGPU_NO_MATRIX, "no matrix");
+  ADC_CUDA(c, cudaMemcpy(hii, c->d_diag, sizeof(double) * c->geom.N, cudaMemcpyDeviceToHost));
+  return ADCGPU_OK;
+}
+
+int adcgpu_export_coo(adcgpu_ctx* h, int64_t cap, double* hv, int32_t* oi, int32_t* oj) {
+  Ctx* c = reinterpret_cast<Ctx*>(h);
+  CTX_CHECK(c);
+  if (!c->have_matrix) return set_err(c, ADCGPU_NO_MATRIX, "no matrix");
+  if (cap < c->nnz_kept || !hv || !oi || !oj) return set_err(c, ADCGPU_BAD_INPUT, "cap < noffd");
+  const int64_t n = c->nnz_kept;
+  double* d_h = nullptr;
+  int32_t *d_i = nullptr, *d_j = nullptr;
+  int st;
+  if ((st = dmalloc(c, (void**)&d_h, sizeof(double) * n))) return st;
+  if ((st = dmalloc(c, (void**)&d_i, sizeof(int32_t) * n))) { dfree(c, d_h, sizeof(double) * n); return st; }
+  if ((st = dmalloc(c, (void**)&d_j, sizeof(int32_t) * n))) {
+    dfree(c, d_h, sizeof(double) * n); dfree(c, d_i, sizeof(int32_t) * n); return st;
+  }
+  st = export_coo_device(c, d_h, d_i, d_j);
+  if (!st) {
+    cudaMemcpy(hv, d_h, sizeof(double) * n, cudaMemcpyDeviceToHost);
+    cudaMemcpy(oi, d_i, sizeof(int32_t) * n, cudaMemcpyDeviceToHost);
+    cudaError_t e = cudaMemcpy(oj, d_j, sizeof(int32_t) * n, cudaMemcpyDeviceToHost);
+    if (e != cudaSuccess) st = set_err(c, ADCGPU_CUDA_ERROR, cudaGetErrorString(e));
+  }
+  dfree(c, d_h, sizeof(double) * n);
+  dfree(c, d_i, sizeof(int32_t) * n);
+  dfree(c, d_j, sizeof(int32_t) * n);
+  return st;
+}
+
+// Fortran unformatted sequential record: 4-byte length, payload, 4-byte length.
+static bool write_record(FILE* f, const void* const* parts, const size_t* sizes, int nparts) {
+  size_t total = 0;
+  for (int i = 0; i < nparts; ++i) total += sizes[i];
+  if (total > 0x7FFFFFFFu) return false;
+  int32_t len = (int32_t)total;
+  if (fwrite(&len, 4, 1, f) != 1) return false;
+  for (int i = 0; i < nparts; ++i)
+    if (sizes[i] && fwrite(parts[i], 1, sizes[i], f) != sizes[i]) return false;
+  return fwrite(&len, 4, 1, f) == 1;
+}
+
+int adcgpu_write_hmlt_files(adcgpu_ctx* h, const char* dir, char flag) {
+  Ctx* c = reinterpret_cast<Ctx*>(h);
+  CTX_CHECK(c);
+  if (!c->have_matrix) return set_err(c, ADCGPU_NO_MATRIX, "no matrix");
+  const int64_t n = c->nnz_kept, N = c->geom.N;
+  std::vector<double> hv(n), diag(N);
+  std::vector<int32_t> oi(n), oj(n);
+  int st = adcgpu_export_coo(h, n, hv.data(), oi.data(), oj.data());
+  if (st) return st;
+  if ((st = adcgpu_get_diag(h, diag.data()))) return st;
+  std::string base = std::string(dir ? dir : ".") + "/hmlt.";
+  // hmlt.off<flag>: records of buf_size triples + nlim (filetools.f90:36-44);
+  // the last record may be incomplete (get_matrix.f90:1124-1126).
+  std::string offname = base + "off" + flag;
+  FILE* f = fopen(offname.c_str(), "wb");
+  if (!f) return set_err(c, ADCGPU_BAD_INPUT, "cannot open " + offname);
+  std::vector<double> bh(BUF_SIZE);
+  std::vector<int32_t> bi(BUF_SIZE), bj(BUF_SIZE);
+  int32_t nrec = 0;
+  for (int64_t k0 = 0;; k0 += BUF_SIZE) {
+    int64_t nlim64 = std::min<int64_t>(BUF_SIZE, n - k0);
+    if (nlim64 < 0) nlim64 = 0;
+    std::fill(bh.begin(), bh.end(), 0.0);
+    std::fill(bi.begin(), bi.end(), 0);
+    std::fill(bj.begin(), bj.end(), 0);
+    std::copy(hv.begin() + k0, hv.begin() + k0 + nlim64, bh.begin());
+    std::copy(oi.begin() + k0, oi.begin() + k0 + nlim64, bi.begin());
+    std::copy(oj.begin() + k0, oj.begin() + k0 + nlim64, bj.begin());
+    int32_t nlim = (int32_t)nlim64;
+    const void* parts[4] = {bh.data(), bi.data(), bj.data(), &nlim};
+    size_t sizes[4] = {sizeof(double) * BUF_SIZE, sizeof(int32_t) * BUF_SIZE, sizeof(int32_t) * BUF_SIZE, 4};
+    if (!write_record(f, parts, sizes, 4)) { fclose(f); return set_err(c, ADCGPU_BAD_INPUT, "write failed"); }
+    ++nrec;
+    if (nlim64 < BUF_SIZE) break;
+  }
+  fclose(f);
+  // hmlt.dia<flag>: (buf_size, nbuf) then hii(ndim) (filetools.f90:24-34)
+  std::string dianame = base + "dia" + flag;
+  f = fopen(dianame.c_str(), "wb");
+  if (!f) return set_err(c, ADCGPU_BAD_INPUT, "cannot open " + dianame);
+  int32_t hdr[2] = {BUF_SIZE, nrec};
+  const void* p1[1] = {hdr};
+  size_t s1[1] = {8};
+  const void* p2[1] = {diag.data()};
+  size_t s2[1] = {sizeof(double) * (size_t)N};
+  bool ok = write_record(f, p1, s1, 1) && write_record(f, p2, s2, 1);
+  fclose(f);
+  if (!ok) return set_err(c, ADCGPU_BAD_INPUT, "write failed");
+  return ADCGPU_OK;
+}
+
+int adcgpu_sigma_device(adcgpu_ctx* h, int m, const void* dv, void* dw, int64_t ld) {
+  Ctx* c = reinterpret_cast<Ctx*>(h);
+  CTX_CHECK(c);
+  if (!c->have_matrix) return set_err(c, ADCGPU_NO_MATRIX, "no matrix");
+  if (m <= 0 || ld < c->geom.N || !dv || !dw) return set_err(c, ADCGPU_BAD_INPUT, "sigma arguments");
+  ADC_CUDA(c, cudaEventRecord(c->ev0, c->stream));
+  int st = c->precision == ADCGPU_MIXED
+               ? sigma_fp32(c, m, (const float*)dv, ld, (float*)dw, ld)
+               : sigma_fp64(c, m, (const double*)dv, ld, (double*)dw, ld);
+  if (st) return st;
+  ADC_CUDA(c, cudaEventRecord(c->ev1, c->stream));
+  ADC_CUDA(c, cudaEventSynchronize(c->ev1));
+  float ms = 0.f;
+  cudaEventElapsedTime(&ms, c->ev0, c->ev1);
+  c->last_sigma_ms = ms;
+  return ADCGPU_OK;
+}
+
+int adcgpu_sigma(adcgpu_ctx* h, int m, const double* v, double* w) {
+  Ctx* c = reinterpret_cast<Ctx*>(h);
+  CTX_CHECK(c);
+  if (!c->have_matrix) return set_err(c, ADCGPU_NO_MATRIX, "no matrix");
+  if (m <= 0 || !v || !w) return set_err(c, ADCGPU_BAD_INPUT, "sigma arguments");
+  const int64_t N = c->geom.N;
+  const size_t n = (size_t)N * m;
+  int st;
+  if (c->precision == ADCGPU_FP64) {
+    double *dv = nullptr, *dw = nullptr;
+    if ((st = dmalloc(c, (void**)&dv, sizeof(double) * n))) return st;
+    if ((st = dmalloc(c, (void**)&dw, sizeof(double) * n))) { dfree(c, dv, sizeof(double) * n); return st; }
+    ADC_CUDA(c, cudaMemcpyAsync(dv, v, sizeof(double) * n, cudaMemcpyHostToDevice, c->stream));
+    st = adcgpu_sigma_device(h, m, dv, dw, N);
+    if (!st) ADC_CUDA(c, cudaMemcpy(w, dw, sizeof(double) * n, cudaMemcpyDeviceToHost));
+    dfree(c, dv, sizeof(double) * n);
+    dfree(c, dw, sizeof(double) * n);
+    return st;
+  }
+  // mixed: host FP64 in/out, FP32 on the device
+  std::vector<float> hv(n);
+  for (size_t i = 0; i < n; ++i) hv[i] = (float)v[i];
+  float *dv = nullptr, *dw = nullptr;
+  if ((st = dmalloc(c, (void**)&dv, sizeof(float) * n))) return st;
+  if ((st = dmalloc(c, (void**)&dw, sizeof(float) * n))) { dfree(c, dv, sizeof(float) * n); return st; }
+  ADC_CUDA(c, cudaMemcpy(dv, hv.data(), sizeof(float) * n, cudaMemcpyHostToDevice));
+  st = adcgpu_sigma_device(h, m, dv, dw, N);
+  if (!st) {
+    ADC_CUDA(c, cudaMemcpy(hv.data(), dw, sizeof(float) * n, cudaMemcpyDeviceToHost));
+    for (size_t i = 0; i < n; ++i) w[i] = hv[i];
+  }
+  dfree(c, dv, sizeof(float) * n);
+  dfree(c, dw, sizeof(float) * n);
+  return st;
+}
+
+double adcgpu_last_sigma_ms(const adcgpu_ctx* h) {
+  const Ctx* c = reinterpret_cast<const Ctx*>(h);
+  return c ? c->last_sigma_ms : 0.0;
+}
+
+int64_t adcgpu_device_bytes(const adcgpu_ctx* h) {
+  const Ctx* c = reinterpret_cast<const Ctx*>(h);
+  return c ? c->dev_bytes : 0;
+}
+
+}  // extern "C"

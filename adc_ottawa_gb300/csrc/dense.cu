@@ -1,0 +1,364 @@
+// Tall-skinny dense kernels of the solvers (N rows, <= a few hundred columns):
+//
+//   gemm_tn : C(p x q) = A(N x p)^T B(N x q)      calcrmat dgemm :961, the
+//             Gram matrices of the orthogonalisation, Lanczos A_j = Q^T U
+//   gemm_nn : C(N x q) = beta C + alpha A(N x p) B(p x q)    calcritzvec :1018,
+//             calcres :1056, projections, Lanczos updates, Ritz vectors
+//   precond : dpr (block_davidson.f90:1288-1342) and olsen (:1346-1419)
+//   resid   : r_i = lambda_i x_i - (W y)_i and ||r_i|| (calcres :1029-1085)
+//
+// Reductions over N are two-pass (per-block partials, then a fixed-order
+// sum), so results do not depend on scheduling.
+#include "internal.h"
+#include "dense.h"
+
+namespace adcgpu {
+
+namespace {
+
+constexpr int TN_ROWS = 32;     // rows staged per step
+constexpr int TN_P = 64, TN_Q = 32;   // output tile
+
+// Partial C tiles: part[(blk * ntile + tile) * TN_P * TN_Q + ...]
+template <typename T, typename TA>
+__global__ void __launch_bounds__(256) k_gemm_tn_part(int64_t N, int p, int q, const T* __restrict__ A,
+                                                      int64_t lda, const T* __restrict__ B, int64_t ldb,
+                                                      TA* __restrict__ part, int64_t rows_per_blk) {
+  __shared__ T sA[TN_ROWS][TN_P + 1];
+  __shared__ T sB[TN_ROWS][TN_Q + 1];
+  const int ntq = (q + TN_Q - 1) / TN_Q;
+  const int tile = blockIdx.y;
+  const int tp = tile / ntq, tq = tile % ntq;
+  const int p0 = tp * TN_P, q0 = tq * TN_Q;
+  const int tid = threadIdx.x;
+  // thread -> 8 outputs: rows i = (tid % 16) + 16*u (u<4), cols j = (tid / 16) + 16*v (v<2)
+  const int ti = tid & 15, tj = tid >> 4;
+  TA acc[4][2];
+#pragma unroll
+  for (int u = 0; u < 4; ++u) { acc[u][0] = TA(0); acc[u][1] = TA(0); }
+  const int64_t r_begin = blockIdx.x * rows_per_blk;
+  const int64_t r_end = min(N, r_begin + rows_per_blk);
+  for (int64_t r0 = r_begin; r0 < r_end; r0 += TN_ROWS) {
+    __syncthreads();
+    for (int l = tid; l < TN_ROWS * TN_P; l += 256) {
+      int c = l / TN_ROWS, rr = l % TN_ROWS;
+      int64_t r = r0 + rr;
+      sA[rr][c] = (r < r_end && p0 + c < p) ? A[(int64_t)(p0 + c) * lda + r] : T(0);
+    }
+    for (int l = tid; l < TN_ROWS * TN_Q; l += 256) {
+      int c = l / TN_ROWS, rr = l % TN_ROWS;
+      int64_t r = r0 + rr;
+      sB[rr][c] = (r < r_end && q0 + c < q) ? B[(int64_t)(q0 + c) * ldb + r] : T(0);
+    }
+    __syncthreads();
+#pragma unroll 4
+    for (int rr = 0; rr < TN_ROWS; ++rr) {
+      TA b0 = (TA)sB[rr][tj], b1 = (TA)sB[rr][tj + 16];
+#pragma unroll
+      for (int u = 0; u < 4; ++u) {
+        TA a = (TA)sA[rr][ti + 16 * u];
+        acc[u][0] += a * b0;
+        acc[u][1] += a * b1;
+      }
+    }
+  }
+  TA* out = part + ((int64_t)blockIdx.x * gridDim.y + tile) * (TN_P * TN_Q);
+#pragma unroll
+  for (int u = 0; u < 4; ++u) {
+    out[(ti + 16 * u) * TN_Q + tj] = acc[u][0];
+    out[(ti + 16 * u) * TN_Q + tj + 16] = acc[u][1];
+  }
+}
+
+template <typename TA, typename TC>
+__global__ void k_gemm_tn_reduce(int p, int q, int nblk, int ntile, const TA* __restrict__ part,
+                                 TC* __restrict__ C, int ldc, TC alpha, TC beta) {
+  const int ntq = (q + TN_Q - 1) / TN_Q;
+  for (int o = blockIdx.x * blockDim.x + threadIdx.x; o < p * q; o += gridDim.x * blockDim.x) {
+    int i = o % p, j = o / p;
+    int tile = (i / TN_P) * ntq + (j / TN_Q);
+    int ii = i % TN_P, jj = j % TN_Q;
+    TA s = TA(0);
+    for (int b = 0; b < nblk; ++b) s += part[((int64_t)b * ntile + tile) * (TN_P * TN_Q) + ii * TN_Q + jj];
+    TC prev = beta == TC(0) ? TC(0) : beta * C[(int64_t)j * ldc + i];
+    C[(int64_t)j * ldc + i] = prev + alpha * (TC)s;
+  }
+}
+
+// C(N x q) = beta C + alpha A(N x p) B(p x q); B (p x q, ldb) staged in smem.
+template <typename T, typename TB>
+__global__ void __launch_bounds__(256) k_gemm_nn(int64_t N, int p, int q, T alpha, const T* __restrict__ A,
+                                                 int64_t lda, const TB* __restrict__ B, int ldb, T beta,
+                                                 T* __restrict__ C, int64_t ldc) {
+  extern __shared__ unsigned char smem_raw[];
+  T* sB = reinterpret_cast<T*>(smem_raw);   // [p][q] column-major: sB[j*p + t]
+  for (int l = threadIdx.x; l < p * q; l += blockDim.x) {
+    int t = l % p, j = l / p;
+    sB[l] = (T)B[(int64_t)j * ldb + t];
+  }
+  __syncthreads();
+  constexpr int JC = 8;
+  for (int64_t r = blockIdx.x * (int64_t)blockDim.x + threadIdx.x; r < N; r += (int64_t)gridDim.x * blockDim.x) {
+    for (int j0 = 0; j0 < q; j0 += JC) {
+      T acc[JC];
+#pragma unroll
+      for (int jj = 0; jj < JC; ++jj) acc[jj] = T(0);
+      for (int t = 0; t < p; ++t) {
+        T a = A[(int64_t)t * lda + r];
+#pragma unroll
+        for (int jj = 0; jj < JC; ++jj)
+          if (j0 + jj < q) acc[jj] += a * sB[(j0 + jj) * p + t];
+      }
+#pragma unroll
+      for (int jj = 0; jj < JC; ++jj) {
+        int j = j0 + jj;
+        if (j < q) {
+          T prev = beta == T(0) ? T(0) : beta * C[(int64_t)j * ldc + r];
+          C[(int64_t)j * ldc + r] = prev + alpha * acc[jj];
+        }
+      }
+    }
+  }
+}
+
+// dpr: t_i(j) = r_i(j) / (lambda_i - hii(j)); exact zero denominators give 0.
+template <typename T, typename TD>
+__global__ void k_dpr(int64_t N, int nb, const T* __restrict__ R, int64_t ldr, const double* __restrict__ lam,
+                      const TD* __restrict__ hii, T* __restrict__ Tout, int64_t ldt) {
+  for (int64_t r = blockIdx.x * (int64_t)blockDim.x + threadIdx.x; r < N; r += (int64_t)gridDim.x * blockDim.x) {
+    T h = (T)hii[r];
+    for (int i = 0; i < nb; ++i) {
+      T den = (T)lam[i] - h;
+      Tout[(int64_t)i * ldt + r] = den == T(0) ? T(0) : R[(int64_t)i * ldr + r] * (T(1) / den);
+    }
+  }
+}
+
+// olsen, pass 1: per-block partial sums of x.(r*cd) and x.(x*cd)
+template <typename T, typename TD>
+__global__ void k_olsen_dots(int64_t N, int nb, const T* __restrict__ X, const T* __restrict__ R, int64_t ld,
+                             const double* __restrict__ lam, const TD* __restrict__ hii, double* __restrict__ part) {
+  __shared__ double red[2][8][32];
+  const int lane = threadIdx.x & 31, w = threadIdx.x >> 5;
+  for (int i = 0; i < nb; ++i) {
+    double xz = 0.0, xy = 0.0;
+    for (int64_t r = blockIdx.x * (int64_t)blockDim.x + threadIdx.x; r < N; r += (int64_t)gridDim.x * blockDim.x) {
+      double den = (double)hii[r] - lam[i];
+      double cd = den == 0.0 ? 0.0 : 1.0 / den;
+      double x = X[(int64_t)i * ld + r], rr = R[(int64_t)i * ld + r];
+      xz += x * (rr * cd);
+      xy += x * (x * cd);
+    }
+    for (int o = 16; o; o >>= 1) { xz += __shfl_xor_sync(0xffffffffu, xz, o); xy += __shfl_xor_sync(0xffffffffu, xy, o); }
+    if (lane == 0) { red[0][w][0] = xz; red[1][w][0] = xy; }
+    __syncthreads();
+    if (threadIdx.x == 0) {
+      double a = 0.0, b = 0.0;
+      for (int q = 0; q < (int)(blockDim.x >> 5); ++q) { a += red[0][q][0]; b += red[1][q][0]; }
+      part[((int64_t)blockIdx.x * nb + i) * 2 + 0] = a;
+      part[((int64_t)blockIdx.x * nb + i) * 2 + 1] = b;
+    }
+    __syncthreads();
+  }
+}
+
+template <typename T, typename TD>
+__global__ void k_olsen_apply(int64_t N, int nb, const T* __restrict__ X, const T* __restrict__ R, int64_t ld,
+                              const double* __restrict__ lam, const double* __restrict__ alpha,
+                              const TD* __restrict__ hii, T* __restrict__ Tout, int64_t ldt) {
+  for (int64_t r = blockIdx.x * (int64_t)blockDim.x + threadIdx.x; r < N; r += (int64_t)gridDim.x * blockDim.x) {
+    for (int i = 0; i < nb; ++i) {
+      T den = (T)hii[r] - (T)lam[i];
+      T cd = den == T(0) ? T(0) : T(1) / den;
+      Tout[(int64_t)i * ldt + r] = (T)alpha[i] * cd * X[(int64_t)i * ld + r] - cd * R[(int64_t)i * ld + r];
+    }
+  }
+}
+
+// res_i = -(WY)_i + lambda_i X_i, and per-block partial ||res_i||^2 (FP64).
+template <typename T>
+__global__ void k_resid(int64_t N, int nb, const T* __restrict__ X, const T* __restrict__ WY, int64_t ld,
+                        const double* __restrict__ lam, T* __restrict__ Rout, double* __restrict__ part) {
+  __shared__ double red[8];
+  const int lane = threadIdx.x & 31, w = threadIdx.x >> 5;
+  for (int i = 0; i < nb; ++i) {
+    double s2 = 0.0;
+    for (int64_t r = blockIdx.x * (int64_t)blockDim.x + threadIdx.x; r < N; r += (int64_t)gridDim.x * blockDim.x) {
+      T v = -WY[(int64_t)i * ld + r] + (T)lam[i] * X[(int64_t)i * ld + r];
+      Rout[(int64_t)i * ld + r] = v;
+      s2 += (double)v * (double)v;
+    }
+    for (int o = 16; o; o >>= 1) s2 += __shfl_xor_sync(0xffffffffu, s2, o);
+    if (lane == 0) red[w] = s2;
+    __syncthreads();
+    if (threadIdx.x == 0) {
+      double a = 0.0;
+      for (int q = 0; q < (int)(blockDim.x >> 5); ++q) a += red[q];
+      part[(int64_t)blockIdx.x * nb + i] = a;
+    }
+    __syncthreads();
+  }
+}
+
+__global__ void k_sum_parts(int nblk, int n, int stride, const double* __restrict__ part, double* __restrict__ out) {
+  int i = blockIdx.x * blockDim.x + threadIdx.x;
+  if (i >= n) return;
+  double s = 0.0;
+  for (int b = 0; b < nblk; ++b) s += part[(int64_t)b * stride + i];
+  out[i] = s;
+}
+
+template <typename TS, typename TD>
+__global__ void k_convert(const TS* __restrict__ x, TD* __restrict__ y, int64_t n) {
+  for (int64_t i = blockIdx.x * (int64_t)blockDim.x + threadIdx.x; i < n; i += (int64_t)gridDim.x * blockDim.x)
+    y[i] = (TD)x[i];
+}
+
+}  // namespace
+
+// ---------------------------------------------------------------------------
+// Host wrappers
+// ---------------------------------------------------------------------------
+Workspace::~Workspace() { release(); }
+void Workspace::release() {
+  if (p && ctx) dfree(ctx, p, bytes);
+  p = nullptr; bytes = 0;
+}
+int Workspace::reserve(Ctx* c, size_t need) {
+  ctx = c;
+  if (bytes >= need) return ADCGPU_OK;
+  release();
+  ctx = c;
+  int st = dmalloc(c, &p, need);
+  if (st) return st;
+  bytes = need;
+  return ADCGPU_OK;
+}
+
+static int tn_blocks(int64_t N) {
+  int64_t b = (N + 4095) / 4096;
+  return (int)std::max<int64_t>(1, std::min<int64_t>(b, 152 * 2));
+}
+
+template <typename T, typename TA, typename TC>
+int gemm_tn(Ctx* c, Workspace& ws, int64_t N, int p, int q, const T* A, int64_t lda, const T* B, int64_t ldb,
+            TC* C, int ldc, TC alpha, TC beta) {
+  if (p <= 0 || q <= 0) return ADCGPU_OK;
+  const int ntile = ((p + TN_P - 1) / TN_P) * ((q + TN_Q - 1) / TN_Q);
+  const int nblk = tn_blocks(N);
+  const int64_t rows = (N + nblk - 1) / nblk;
+  size_t need = sizeof(TA) * (size_t)nblk * ntile * TN_P * TN_Q;
+  int st = ws.reserve(c, need);
+  if (st) return st;
+  k_gemm_tn_part<T, TA><<<dim3(nblk, ntile), 256, 0, c->stream>>>(N, p, q, A, lda, B, ldb, (TA*)ws.p, rows);
+  k_gemm_tn_reduce<TA, TC><<<(p * q + 255) / 256, 256, 0, c->stream>>>(p, q, nblk, ntile, (TA*)ws.p, C, ldc,
+                                                                       alpha, beta);
+  ADC_CUDA(c, cudaGetLastError());
+  return ADCGPU_OK;
+}
+
+template <typename T, typename TB>
+int gemm_nn(Ctx* c, int64_t N, int p, int q, T alpha, const T* A, int64_t lda, const TB* B, int ldb, T beta, T* C,
+            int64_t ldc) {
+  if (q <= 0) return ADCGPU_OK;
+  if (p <= 0) {
+    // C = beta C
+    if (beta == T(0)) {
+      for (int j = 0; j < q; ++j) ADC_CUDA(c, cudaMemsetAsync(C + (int64_t)j * ldc, 0, sizeof(T) * N, c->stream));
+    }
+    return ADCGPU_OK;
+  }
+  size_t smem = sizeof(T) * (size_t)p * q;
+  if (smem > 200 * 1024) return set_err(c, ADCGPU_UNSUPPORTED, "gemm_nn: small operand exceeds shared memory");
+  auto kern = k_gemm_nn<T, TB>;
+  ADC_CUDA(c, cudaFuncSetAttribute(kern, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem));
+  int64_t nb = (N + 255) / 256;
+  int grid = (int)std::min<int64_t>(nb, 152 * 8);
+  kern<<<grid, 256, smem, c->stream>>>(N, p, q, alpha, A, lda, B, ldb, beta, C, ldc);
+  ADC_CUDA(c, cudaGetLastError());
+  return ADCGPU_OK;
+}
+
+template <typename T, typename TD>
+int precond_dpr(Ctx* c, int64_t N, int nb, const T* R, int64_t ldr, const double* d_lam, const TD* hii, T* Tout,
+                int64_t ldt) {
+  k_dpr<T, TD><<<152 * 8, 256, 0, c->stream>>>(N, nb, R, ldr, d_lam, hii, Tout, ldt);
+  ADC_CUDA(c, cudaGetLastError());
+  return ADCGPU_OK;
+}
+
+template <typename T, typename TD>
+int precond_olsen(Ctx* c, Workspace& ws, int64_t N, int nb, const T* X, const T* R, int64_t ld, const double* d_lam,
+                  const TD* hii, T* Tout, int64_t ldt, double* h_alpha_out) {
+  const int nblk = 152 * 2;
+  int st = ws.reserve(c, sizeof(double) * (size_t)nblk * nb * 2 + sizeof(double) * 4 * nb);
+  if (st) return st;
+  double* part = (double*)ws.p;
+  double* sums = part + (size_t)nblk * nb * 2;
+  k_olsen_dots<T, TD><<<nblk, 256, 0, c->stream>>>(N, nb, X, R, ld, d_lam, hii, part);
+  k_sum_parts<<<(2 * nb + 127) / 128, 128, 0, c->stream>>>(nblk, 2 * nb, 2 * nb, part, sums);
+  std::vector<double> h(2 * nb), alpha(nb);
+  ADC_CUDA(c, cudaMemcpyAsync(h.data(), sums, sizeof(double) * 2 * nb, cudaMemcpyDeviceToHost, c->stream));
+  ADC_CUDA(c, cudaStreamSynchronize(c->stream));
+  for (int i = 0; i < nb; ++i) alpha[i] = h[2 * i + 1] == 0.0 ? 0.0 : h[2 * i] / h[2 * i + 1];
+  double* d_alpha = sums + 2 * nb;
+  ADC_CUDA(c, cudaMemcpyAsync(d_alpha, alpha.data(), sizeof(double) * nb, cudaMemcpyHostToDevice, c->stream));
+  k_olsen_apply<T, TD><<<152 * 8, 256, 0, c->stream>>>(N, nb, X, R, ld, d_lam, d_alpha, hii, Tout, ldt);
+  ADC_CUDA(c, cudaGetLastError());
+  if (h_alpha_out) std::copy(alpha.begin(), alpha.end(), h_alpha_out);
+  ADC_CUDA(c, cudaStreamSynchronize(c->stream));
+  return ADCGPU_OK;
+}
+
+template <typename T>
+int residuals(Ctx* c, Workspace& ws, int64_t N, int nb, const T* X, const T* WY, int64_t ld, const double* d_lam,
+              T* Rout, double* h_norm2) {
+  const int nblk = 152 * 2;
+  int st = ws.reserve(c, sizeof(double) * ((size_t)nblk * nb + nb));
+  if (st) return st;
+  double* part = (double*)ws.p;
+  double* sums = part + (size_t)nblk * nb;
+  k_resid<T><<<nblk, 256, 0, c->stream>>>(N, nb, X, WY, ld, d_lam, Rout, part);
+  k_sum_parts<<<(nb + 127) / 128, 128, 0, c->stream>>>(nblk, nb, nb, part, sums);
+  ADC_CUDA(c, cudaGetLastError());
+  ADC_CUDA(c, cudaMemcpyAsync(h_norm2, sums, sizeof(double) * nb, cudaMemcpyDeviceToHost, c->stream));
+  ADC_CUDA(c, cudaStreamSynchronize(c->stream));
+  return ADCGPU_OK;
+}
+
+template <typename TS, typename TD>
+int convert(Ctx* c, const TS* x, TD* y, int64_t n) {
+  k_convert<TS, TD><<<152 * 8, 256, 0, c->stream>>>(x, y, n);
+  ADC_CUDA(c, cudaGetLastError());
+  return ADCGPU_OK;
+}
+
+// explicit instantiations
+template int gemm_tn<double, double, double>(Ctx*, Workspace&, int64_t, int, int, const double*, int64_t,
+                                             const double*, int64_t, double*, int, double, double);
+template int gemm_tn<float, float, double>(Ctx*, Workspace&, int64_t, int, int, const float*, int64_t, const float*,
+                                           int64_t, double*, int, double, double);
+template int gemm_tn<float, double, double>(Ctx*, Workspace&, int64_t, int, int, const float*, int64_t, const float*,
+                                            int64_t, double*, int, double, double);
+template int gemm_nn<double, double>(Ctx*, int64_t, int, int, double, const double*, int64_t, const double*, int,
+                                     double, double*, int64_t);
+template int gemm_nn<float, double>(Ctx*, int64_t, int, int, float, const float*, int64_t, const double*, int, float,
+                                    float*, int64_t);
+template int gemm_nn<float, float>(Ctx*, int64_t, int, int, float, const float*, int64_t, const float*, int, float,
+                                   float*, int64_t);
+template int precond_dpr<double, double>(Ctx*, int64_t, int, const double*, int64_t, const double*, const double*,
+                                         double*, int64_t);
+template int precond_dpr<float, float>(Ctx*, int64_t, int, const float*, int64_t, const double*, const float*,
+                                       float*, int64_t);
+template int precond_olsen<double, double>(Ctx*, Workspace&, int64_t, int, const double*, const double*, int64_t,
+                                           const double*, const double*, double*, int64_t, double*);
+template int precond_olsen<float, float>(Ctx*, Workspace&, int64_t, int, const float*, const float*, int64_t,
+                                         const double*, const float*, float*, int64_t, double*);
+template int residuals<double>(Ctx*, Workspace&, int64_t, int, const double*, const double*, int64_t, const double*,
+                               double*, double*);
+template int residuals<float>(Ctx*, Workspace&, int64_t, int, const float*, const float*, int64_t, const double*,
+                              float*, double*);
+template int convert<double, float>(Ctx*, const double*, float*, int64_t);
+template int convert<float, double>(Ctx*, const float*, double*, int64_t);
+
+}  // namespace adcgpu

@@ -1,0 +1,246 @@
+// Internal declarations of libadcgpu: the device-resident problem, the
+// configuration index maps and the layout of the stored matrix.
+//
+// Stored matrix (ADC(2)-s, C1 symmetry):
+//
+//     H = | A    B |   A  : n1 x n1 dense ph-ph block (symmetric, FP64)
+//         | B^T  D |   B  : n1 x n2 ph-2p2h coupling
+//                      D  : diagonal 2p2h block (get_matrix.f90:303-306)
+//
+// B is stored index-free.  A double d = (a',b',k',l') couples only to singles
+// (a,k) with a in {a',b'} or k in {k',l'} (the coincidence tests of
+// C1..C5_ph_2p2h, adc_ph.f90:974-1073), so the column pattern of each row of
+// B^T is a closed-form function of d.  Each row holds its structural entries
+// in a fixed segment order and values with |h| <= minc are stored as 0.0, so
+// the matrix equals the reference's thresholded COO exactly while the sigma
+// product streams 8 bytes per entry instead of 16.
+//
+//   segment A : singles (a',k), k = 0..no-1           (always)
+//   segment B : singles (b',k), k = 0..no-1           (a' != b')
+//   segment C : singles (a,k'),  a = 0..nv-1, a not in {a',b'}
+//   segment D : singles (a,l'),  a = 0..nv-1, a not in {a',b'}   (k' != l')
+//
+// Row lengths: class 1 (a'=b',k'=l') no+nv-1; class 2 (a'<b',k'=l') 2no+nv-2;
+// class 3 (a'=b',k'<l') no+2nv-2; classes 4I/4II 2no+2nv-4.
+//
+// All indices below are 0-based: occupied i in [0,no), virtual a in [0,nv)
+// (orbital no+a), single s = a*no + k (select_atom_is order), doubles in the
+// select_atom_d order of select_fano.f90:539-718.
+#pragma once
+
+#include <cuda_runtime.h>
+#include <stdint.h>
+#include <string>
+#include <vector>
+
+#include "../../include/adcgpu.h"
+
+namespace adcgpu {
+
+constexpr double MINC = 1e-12;   // parameters.f90:139
+constexpr int BUF_SIZE = 655360; // parameters.f90:425
+
+// ---------------------------------------------------------------------------
+// Configuration space geometry.
+// ---------------------------------------------------------------------------
+struct Geometry {
+  int no = 0, nv = 0;
+  int64_t n1 = 0;         // singles
+  int64_t c1 = 0, c2 = 0, c3 = 0, c4 = 0;   // class sizes (4 = each of 4I, 4II)
+  int64_t n2 = 0, N = 0;
+  int64_t start[6];       // first doubles-local index of class 1,2,3,4I,4II and n2
+  int64_t len[5];         // row length of B^T per class (4I and 4II equal)
+  int64_t off[6];         // value offset of class c in the B^T store; off[5] = total
+  int64_t npair_v = 0, npair_o = 0;   // nv(nv-1)/2, no(no-1)/2
+
+  void init(int no_, int nv_) {
+    no = no_; nv = nv_;
+    n1 = (int64_t)no * nv;
+    npair_v = (int64_t)nv * (nv - 1) / 2;
+    npair_o = (int64_t)no * (no - 1) / 2;
+    c1 = (int64_t)no * nv;
+    c2 = npair_v * no;
+    c3 = npair_o * nv;
+    c4 = npair_o * npair_v;
+    n2 = c1 + c2 + c3 + 2 * c4;
+    N = n1 + n2;
+    start[0] = 0; start[1] = c1; start[2] = c1 + c2; start[3] = c1 + c2 + c3;
+    start[4] = start[3] + c4; start[5] = n2;
+    len[0] = no + nv - 1;
+    len[1] = 2 * no + nv - 2;
+    len[2] = no + 2 * nv - 2;
+    len[3] = 2 * no + 2 * nv - 4;
+    len[4] = len[3];
+    off[0] = 0;
+    for (int c = 0; c < 5; ++c) off[c + 1] = off[c] + (start[c + 1] - start[c]) * len[c];
+  }
+  int64_t structural_nnz() const { return n1 * (n1 - 1) / 2 + off[5]; }
+};
+
+// Decoded double: virtuals a' <= b', occupied k' <= l', class 0..4.
+struct Double {
+  int ap, bp, kp, lp, cls;
+};
+
+// Index of pair (x<y) among pairs of n items in lexicographic order.
+__host__ __device__ inline int64_t pair_index(int x, int y, int n) {
+  return (int64_t)x * n - (int64_t)x * (x + 1) / 2 + (y - x - 1);
+}
+
+__host__ __device__ inline void pair_decode(int64_t p, int n, int& x, int& y) {
+  // invert pair_index by walking rows; n is small (<= a few hundred)
+  int xx = 0;
+  int64_t rowlen = n - 1;
+  while (p >= rowlen) { p -= rowlen; ++xx; --rowlen; }
+  x = xx; y = xx + 1 + (int)p;
+}
+
+struct GeomDev {
+  int no, nv;
+  int64_t n1, n2, N;
+  int64_t start[6];
+  int64_t len[5];
+  int64_t off[6];
+  int64_t npair_v, npair_o;
+};
+
+inline GeomDev to_dev(const Geometry& g) {
+  GeomDev d;
+  d.no = g.no; d.nv = g.nv; d.n1 = g.n1; d.n2 = g.n2; d.N = g.N;
+  for (int i = 0; i < 6; ++i) { d.start[i] = g.start[i]; d.off[i] = g.off[i]; }
+  for (int i = 0; i < 5; ++i) d.len[i] = g.len[i];
+  d.npair_v = g.npair_v; d.npair_o = g.npair_o;
+  return d;
+}
+
+// Doubles-local index d in [0,n2) -> configuration, following select_atom_d.
+__host__ __device__ inline Double decode_double(const GeomDev& g, int64_t d) {
+  Double r;
+  if (d < g.start[1]) {                       // class 1: hole outer, particle inner
+    r.cls = 0; r.kp = r.lp = (int)(d / g.nv); r.ap = r.bp = (int)(d % g.nv);
+  } else if (d < g.start[2]) {                // class 2: pair (a<b) outer, hole inner
+    int64_t t = d - g.start[1];
+    r.cls = 1; r.kp = r.lp = (int)(t % g.no);
+    pair_decode(t / g.no, g.nv, r.ap, r.bp);
+  } else if (d < g.start[3]) {                // class 3: hole pair outer, particle inner
+    int64_t t = d - g.start[2];
+    r.cls = 2; r.ap = r.bp = (int)(t % g.nv);
+    pair_decode(t / g.nv, g.no, r.kp, r.lp);
+  } else {                                     // classes 4I / 4II
+    int64_t t = d - g.start[3];
+    r.cls = 3;
+    if (t >= g.start[4] - g.start[3]) { t -= g.start[4] - g.start[3]; r.cls = 4; }
+    pair_decode(t / g.npair_v, g.no, r.kp, r.lp);
+    pair_decode(t % g.npair_v, g.nv, r.ap, r.bp);
+  }
+  return r;
+}
+
+// Single index of entry e of the B^T row of double r (segment order above).
+__host__ __device__ inline int64_t entry_single(const GeomDev& g, const Double& r, int e) {
+  const int no = g.no;
+  if (e < no) return (int64_t)r.ap * no + e;                   // segment A
+  e -= no;
+  const bool twoa = r.ap != r.bp;
+  if (twoa) {
+    if (e < no) return (int64_t)r.bp * no + e;                 // segment B
+    e -= no;
+  }
+  const int nseg = g.nv - (twoa ? 2 : 1);
+  int seg = e / nseg;                                           // 0: C (k'), 1: D (l')
+  int t = e - seg * nseg;
+  // t-th virtual not in {a',b'}
+  int a = t;
+  if (a >= r.ap) ++a;
+  if (twoa && a >= r.bp) ++a;
+  int occ = seg == 0 ? r.kp : r.lp;
+  return (int64_t)a * no + occ;
+}
+
+// ---------------------------------------------------------------------------
+// Context.
+// ---------------------------------------------------------------------------
+struct DevBuf {
+  void* p = nullptr;
+  size_t bytes = 0;
+};
+
+struct Ctx {
+  int device = 0;
+  cudaStream_t stream = nullptr;
+  cudaEvent_t ev0 = nullptr, ev1 = nullptr;
+  std::string err;
+  Geometry geom;
+  bool have_orb = false, have_eri = false, have_matrix = false;
+  int precision = ADCGPU_FP64;
+  char flag = 'i';
+  std::vector<double> e;          // orbital energies (host copy)
+  double* d_e = nullptr;          // device orbital energies [nbas]
+  // ERI blocks (0-based, see eri accessors in build_kernels.cu)
+  double* d_vovo = nullptr;       // (a i|b j) [nv][no][nv][no]
+  double* d_vvoo = nullptr;       // (a b|i j) [nv][nv][no][no]
+  double* d_ooov = nullptr;       // (i j|k a) [no][no][no][nv]
+  double* d_vvov = nullptr;       // (a b|i c) [nv][nv][no][nv]
+  // matrix
+  double* d_diag = nullptr;       // hii [N]
+  double* d_A = nullptr;          // ph-ph block, n1 x n1 dense symmetric (0 where |h|<=minc)
+  double* d_Bt = nullptr;         // structured B^T values (geom.off[5] entries)
+  float* d_A32 = nullptr;         // mixed-precision copies
+  uint16_t* d_Bt16 = nullptr;     // bf16 bits of B^T values
+  float* d_Bt32 = nullptr;        // fp32 B^T values (when bf16 is not safe)
+  float* d_diag32 = nullptr;
+  int mixed_bf16 = 1;             // 1: B^T stored as bf16, 0: fp32
+  int64_t nnz_kept = 0;           // reference noffd
+  int64_t nnz_ph = 0;             // kept ph-ph entries
+  int64_t* d_rowcount = nullptr;  // kept entries per double row (for COO export)
+  // sigma workspace
+  void* d_ws = nullptr;
+  size_t ws_bytes = 0;
+  double last_sigma_ms = 0.0;
+  int64_t dev_bytes = 0;
+  // SIL persistent state for adcgpu_silstep (device Krylov vectors)
+  double* d_sil = nullptr;
+  int64_t sil_cap = 0;
+};
+
+// error helpers
+int set_err(Ctx* c, int code, const std::string& msg);
+#define ADC_CUDA(ctx, call)                                                     \
+  do {                                                                         \
+    cudaError_t _e = (call);                                                   \
+    if (_e != cudaSuccess)                                                     \
+      return ::adcgpu::set_err((ctx), _e == cudaErrorMemoryAllocation          \
+                                         ? ADCGPU_OUT_OF_MEMORY                \
+                                         : ADCGPU_CUDA_ERROR,                  \
+                               std::string(#call) + ": " + cudaGetErrorString(_e)); \
+  } while (0)
+
+int dmalloc(Ctx* c, void** p, size_t bytes);
+void dfree(Ctx* c, void* p, size_t bytes);
+
+// ---------------------------------------------------------------------------
+// Kernels launched from other translation units.
+// ---------------------------------------------------------------------------
+// build_kernels.cu
+int build_eri_blocks_from_packed(Ctx* c, const double* d_packed);
+int build_matrix(Ctx* c);
+int export_coo_device(Ctx* c, double* d_h, int32_t* d_oi, int32_t* d_oj);
+
+// sigma.cu : W = H V for m columns (column-major, leading dim ld), FP64 or FP32.
+int sigma_fp64(Ctx* c, int m, const double* dV, int64_t ldv, double* dW, int64_t ldw);
+int sigma_fp32(Ctx* c, int m, const float* dV, int64_t ldv, float* dW, int64_t ldw);
+int prepare_mixed(Ctx* c);
+
+// hostla.cpp : dense host linear algebra (FP64)
+// Symmetric eigen-decomposition (Householder tridiagonalisation + implicit QL).
+// A: n x n column-major (upper triangle used); w ascending; V eigenvectors.
+bool host_syev(int n, const double* A, int lda, double* w, double* V);
+// Cholesky of SPD G (n x n col-major) -> upper R with G = R^T R; returns the
+// first column whose pivot fell below rel_tol * max diag (or -1 on success).
+int host_cholesky_upper(int n, const double* G, double* R, double rel_tol);
+// Inverse of an upper-triangular n x n matrix.
+void host_triu_inverse(int n, const double* R, double* Rinv);
+// NR heapsort index (dsortindxa1 'A', misc.f90:492+); indx 1-based.
+void host_heapsort_index(int64_t n, const double* arr, std::vector<int64_t>& indx);
+
+}  // namespace adcgpu

@@ -1,0 +1,112 @@
+"""GPU Davidson, block Lanczos and SIL against the oracle."""
+import numpy as np
+import pytest
+
+import oracle
+from tests.conftest import system
+from tests.test_gpu_build import make
+
+pytestmark = pytest.mark.gpu
+
+
+@pytest.fixture(scope="module")
+def cfg1(gpu):
+    no, nv, seed = 5, 19, 1234
+    g, e, eri = make(no, nv, seed)
+    ref = oracle.Matrix.build(no, nv, e, eri)
+    yield g, ref
+    g.close()
+
+
+@pytest.mark.parametrize("precon", [1, 2])
+@pytest.mark.parametrize("ldfl", [True, False])
+def test_davidson_config1(cfg1, precon, ldfl):
+    """Config 1: 6 roots, tol 1e-8: eigenvalues within 1e-8 Ha of the oracle."""
+    g, ref = cfg1
+    res = g.davdiag_block(6, 1e-8, precon=precon, ldfl=ldfl)
+    st, ev, _, info = ref.davidson(6, 1e-8, precon=precon, deflate=ldfl)
+    assert st == 0 and res.status == 0
+    assert np.abs(res.evals - ev).max() < 1e-8
+    # residuals of the returned vectors in FP64
+    H = ref.dense()
+    r = H @ res.evecs - res.evecs * res.evals
+    assert np.linalg.norm(r, axis=0).max() < 1e-7
+
+
+def test_davidson_subdiag_guess(cfg1):
+    g, ref = cfg1
+    res = g.davdiag_block(6, 1e-8, lsubdiag=True, guessdim=200)
+    st, ev, _, _ = ref.davidson(6, 1e-8, subdiag=True, guessdim=200)
+    assert np.abs(res.evals - ev).max() < 1e-8
+
+
+def test_davidson_nonconvergence_status(cfg1):
+    from adc_ottawa_gb300 import AdcGpuError
+
+    g, ref = cfg1
+    with pytest.raises(AdcGpuError) as ei:
+        g.davdiag_block(6, 1e-8, maxiter=1)
+    assert ei.value.code == 10
+
+
+def test_mixed_precision_davidson(gpu):
+    from adc_ottawa_gb300 import ADCGPU_MIXED
+
+    no, nv, seed = 5, 19, 1234
+    g, e, eri = make(no, nv, seed, precision=ADCGPU_MIXED)
+    ref = oracle.Matrix.build(no, nv, e, eri)
+    w = np.linalg.eigh(ref.dense())[0]
+    res = g.davdiag_block(6, 1e-6, precision=ADCGPU_MIXED)
+    assert res.status == 0
+    assert np.abs(res.evals - w[:6]).max() < 1e-6
+
+
+@pytest.mark.parametrize("orthotype", [0, 1])
+def test_lanczos_config1(cfg1, orthotype):
+    g, ref = cfg1
+    b, ncyc = 4, 12
+    q0 = np.random.RandomState(9).rand(g.ndim, b)
+    T, ev, _ = g.lancdiag_block(q0, ncyc, orthotype=orthotype)
+    Tr, evr = ref.block_lanczos(q0, ncyc, orthotype=orthotype)
+    # T equals the oracle's up to a block-diagonal sign similarity: compare
+    # eigenvalues and first-block moments
+    assert np.abs(ev - evr).max() <= 1e-9 * np.abs(evr).max()
+    Tk, Trk = np.eye(b * ncyc)[:, :b], np.eye(b * ncyc)[:, :b]
+    for k in range(1, 2 * ncyc):
+        Tk, Trk = T @ Tk, Tr @ Trk
+        assert np.abs(Tk[:b] - Trk[:b]).max() <= 1e-10 * np.abs(Trk[:b]).max()
+    assert np.allclose(np.abs(np.diag(T, -b)), np.abs(np.diag(Tr, -b)), rtol=1e-9, atol=1e-12)
+
+
+def test_lanczos_ritz_vectors(cfg1):
+    g, ref = cfg1
+    q0 = np.random.RandomState(4).rand(g.ndim, 2)
+    T, ev, R = g.lancdiag_block(q0, 30, orthotype=1, want_ritz=True)
+    H = ref.dense()
+    assert np.allclose(np.linalg.norm(R, axis=0), 1.0)
+    # lowest Ritz pair is an eigenpair to good accuracy
+    r0 = H @ R[:, 0] - ev[0] * R[:, 0]
+    assert np.linalg.norm(r0) < 1e-6
+
+
+def test_sil_autocorr_config1(cfg1):
+    g, ref = cfg1
+    f = np.random.RandomState(2).rand(g.ndim, 3)
+    a, nm = g.propagate_fvec(f, tout=0.5, tfinal=6.0, kdim=12, autotol=1e-9)
+    for p in range(3):
+        st, ar, nmr = ref.autocorr(f[:, p], 0.5, 6.0, 12, 1e-9)
+        assert st == 0
+        assert np.abs(a[p] - ar).max() <= 1e-7 * np.abs(ar).max()
+
+
+def test_silstep_single(cfg1):
+    g, ref = cfg1
+    H = ref.dense()
+    psi = np.random.RandomState(1).rand(g.ndim).astype(np.complex128)
+    psi /= np.linalg.norm(psi)
+    dtpsi = -1j * (H @ psi)
+    p2, d2, step, order, stt = g.silstep(psi.copy(), dtpsi.copy(), 0.05, 10, 1e-10)
+    w, V = np.linalg.eigh(H)
+    exact = V @ (np.exp(-1j * w * step) * (V.T @ psi))
+    assert np.abs(p2 - exact).max() < 1e-8
+    assert stt.old_order == order
