@@ -157,14 +157,18 @@ struct DavidsonGPU {
     return ADCGPU_OK;
   }
 
-  // Orthonormalise nt columns at Tb against Q1 (n1 cols), Q2 (n2 cols) and
-  // among themselves.  Returns the number of columns replaced by random
-  // vectors (numerically dependent ones).
+  // Orthonormalise nt columns at Tb against Q1 (nq1 cols), Q2 (nq2 cols)
+  // and among themselves: block CGS twice, then Cholesky QR twice on the
+  // column-scaled Gram matrix.  A column whose norm drops below 1e-10 of its
+  // norm before projection (numerically inside the span) is replaced by a
+  // random vector, as Householder QR would complete the basis.
   int orthonormalise(T* Tb, int nt, const T* Q1, int nq1, const T* Q2, int nq2, int* nreplaced) {
     *nreplaced = 0;
     if (nt > 2 * blocksize || nt > maxvec) return set_err(c, ADCGPU_BAD_INPUT, "orthonormalise: block too wide");
-    std::vector<double> G, Rc((size_t)nt * nt), Ri((size_t)nt * nt);
-    for (int attempt = 0; attempt < 4; ++attempt) {
+    std::vector<double> G, Gs((size_t)nt * nt), Rc((size_t)nt * nt), Ri((size_t)nt * nt), n0(nt), sc(nt);
+    ST(tn_to_host(nt, nt, Tb, Tb, G));
+    for (int j = 0; j < nt; ++j) n0[j] = std::sqrt(std::max(G[(size_t)j * nt + j], 0.0));
+    for (int attempt = 0; attempt < nt + 3; ++attempt) {
       for (int pass = 0; pass < 2; ++pass) {
         ST(project_out(Q2, nq2, Tb, nt));
         ST(project_out(Q1, nq1, Tb, nt));
@@ -172,15 +176,28 @@ struct DavidsonGPU {
       bool ok = true;
       for (int pass = 0; pass < 2 && ok; ++pass) {
         ST(tn_to_host(nt, nt, Tb, Tb, G));
-        int bad = host_cholesky_upper(nt, G.data(), Rc.data(), 1e-20);
+        int bad = -1;
+        for (int j = 0; j < nt && bad < 0; ++j) {
+          double nj = std::sqrt(std::max(G[(size_t)j * nt + j], 0.0));
+          if (!(nj > 0.0) || (pass == 0 && nj <= 1e-10 * n0[j])) bad = j;
+          else sc[j] = 1.0 / nj;
+        }
+        if (bad < 0) {
+          for (int j = 0; j < nt; ++j)
+            for (int i = 0; i < nt; ++i) Gs[(size_t)j * nt + i] = G[(size_t)j * nt + i] * sc[i] * sc[j];
+          bad = host_cholesky_upper(nt, Gs.data(), Rc.data(), 1e-12);
+        }
         if (bad >= 0) {
-          // replace the dependent column by a random vector and start over
           fill_random<T>(c, Tb + (size_t)bad * N, N, 0xC0FFEEull + 7919ull * (attempt + 1) + bad);
+          n0[bad] = 1.0;
           ++*nreplaced;
           ok = false;
           break;
         }
+        // R = Rs S^{-1}  =>  R^{-1} = S Rs^{-1}
         host_triu_inverse(nt, Rc.data(), Ri.data());
+        for (int j = 0; j < nt; ++j)
+          for (int i = 0; i < nt; ++i) Ri[(size_t)j * nt + i] *= sc[i];
         ADC_CUDA(c, cudaMemcpyAsync(d_small2, Ri.data(), sizeof(double) * nt * nt, cudaMemcpyHostToDevice, c->stream));
         ST((gemm_nn<T, double>(c, N, nt, nt, T(1), Tb, N, d_small2, nt, T(0), Tmp, N)));
         ADC_CUDA(c, cudaMemcpyAsync(Tb, Tmp, bytes_v * nt, cudaMemcpyDeviceToDevice, c->stream));

@@ -513,6 +513,7 @@ extern "C" int adcgpu_silstep(adcgpu_ctx* h, double* psi, double* dtpsi, int psi
   std::vector<int> mask(1, 1);
   std::vector<double> period(1, intperiod);
   ST(E.silstep(mask, pk, period, tol, relax != 0));
+  ADC_CUDA(c, cudaStreamSynchronize(c->stream));
   if (pk[0].err) return pk[0].err;
   ADC_CUDA(c, cudaMemcpy(blk.data(), E.Psi, sizeof(double) * 2 * N, cudaMemcpyDeviceToHost));
   for (int64_t i = 0; i < N; ++i) { psi[2 * i] = blk[i]; psi[2 * i + 1] = blk[N + i]; }

@@ -1,0 +1,101 @@
+"""Generate the golden fixtures in tests/golden/ from the oracle.
+
+Run on a CPU host:  python tests/golden/make_golden.py [--config2]
+
+The fixtures pin (i) the seeded synthetic generator bit for bit across
+hosts (SHA-256 of the orbital energies and packed ERIs), (ii) the oracle's
+kept structure (count and an order-independent hash), diagonal and values,
+and (iii) the oracle's eigenvalues, Lanczos spectra and SIL autocorrelation
+on small systems.  --config2 adds the nocc=10, nvirt=110 system (about
+137 M kept elements; the oracle Davidson takes tens of minutes there).
+"""
+from __future__ import annotations
+
+import hashlib
+import json
+import os
+import sys
+import time
+
+import numpy as np
+
+HERE = os.path.dirname(os.path.abspath(__file__))
+ROOT = os.path.dirname(os.path.dirname(HERE))
+sys.path.insert(0, ROOT)
+
+import oracle  # noqa: E402
+from adc_ottawa_gb300 import synth_system, synth_uniform_block  # noqa: E402
+
+
+def sha(a: np.ndarray) -> str:
+    return hashlib.sha256(np.ascontiguousarray(a).tobytes()).hexdigest()
+
+
+def matrix_fingerprint(M: oracle.Matrix) -> dict:
+    d, h, oi, oj = M.coo()
+    k = np.lexsort((oj, oi))
+    return {
+        "ndim": int(M.ndim),
+        "nnz": int(M.nnz),
+        "structure_hash": [str(x) for x in oracle.structure_hash(oi, oj)],
+        "diag_sha": sha(d),
+        "values_sorted_sha": sha(h[k]),
+    }
+
+
+def small_case(no, nv, seed, dav=None, lanczos=None, sil=None) -> dict:
+    e, eri = synth_system(no, nv, seed)
+    M = oracle.Matrix.build(no, nv, e, eri)
+    out = {"nocc": no, "nvirt": nv, "seed": seed, "e_sha": sha(e), "eri_sha": sha(eri)}
+    out.update(matrix_fingerprint(M))
+    if dav:
+        st, ev, _, info = M.davidson(dav["nstates"], dav["tol"], precon=dav.get("precon", 1))
+        assert st == 0, st
+        out["davidson"] = {**dav, "evals": ev.tolist(), "iterations": info["iterations"]}
+    if lanczos:
+        q0 = synth_uniform_block(M.ndim, lanczos["b"], lanczos["seed"])
+        T, ev = M.block_lanczos(q0, lanczos["ncycles"], orthotype=lanczos.get("orthotype", 0))
+        b = lanczos["b"]
+        mom, Tk = [], np.eye(T.shape[0])[:, :b]
+        for k in range(1, 2 * lanczos["ncycles"]):
+            Tk = T @ Tk
+            mom.append(np.trace(Tk[:b]))
+        out["lanczos"] = {**lanczos, "evals": ev.tolist(), "trace_moments": mom}
+    if sil:
+        f = synth_uniform_block(M.ndim, 1, sil["seed"])[:, 0]
+        st, a, nm = M.autocorr(f, sil["tout"], sil["tfinal"], sil["kdim"], sil["tol"])
+        assert st == 0
+        out["sil"] = {**sil, "auto_re": a.real.tolist(), "auto_im": a.imag.tolist()}
+    return out
+
+
+def main():
+    cases = [
+        small_case(2, 3, 5),
+        small_case(4, 9, 7, dav={"nstates": 4, "tol": 1e-8}),
+        small_case(5, 19, 1234, dav={"nstates": 6, "tol": 1e-8},
+                   lanczos={"b": 4, "ncycles": 10, "seed": 77},
+                   sil={"seed": 78, "tout": 0.5, "tfinal": 5.0, "kdim": 12, "tol": 1e-9}),
+        small_case(6, 30, 11, dav={"nstates": 5, "tol": 1e-8, "precon": 2}),
+    ]
+    with open(os.path.join(HERE, "small_cases.json"), "w") as f:
+        json.dump(cases, f, indent=1)
+    print("wrote small_cases.json")
+    if "--config2" in sys.argv:
+        t = time.time()
+        no, nv, seed = 10, 110, 2024
+        e, eri = synth_system(no, nv, seed)
+        M = oracle.Matrix.build(no, nv, e, eri)
+        out = {"nocc": no, "nvirt": nv, "seed": seed, "e_sha": sha(e), "eri_sha": sha(eri)}
+        out.update(matrix_fingerprint(M))
+        print("config2 matrix", out["nnz"], time.time() - t, flush=True)
+        st, ev, _, info = M.davidson(10, 1e-8, precon=1)
+        out["davidson"] = {"nstates": 10, "tol": 1e-8, "precon": 1, "status": int(st), "evals": ev.tolist(),
+                           "iterations": info["iterations"], "nmult": info["nmult"], "seconds": time.time() - t}
+        with open(os.path.join(HERE, "config2.json"), "w") as f:
+            json.dump(out, f, indent=1)
+        print("wrote config2.json", time.time() - t)
+
+
+if __name__ == "__main__":
+    main()
