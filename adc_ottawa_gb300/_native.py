@@ -30,6 +30,8 @@ class DavParams(C.Structure):
         ("davtol", C.c_double),
         ("precision", C.c_int),
         ("refine", C.c_int),
+        ("tol_bf16", C.c_double),
+        ("tol_fp32", C.c_double),
     ]
 
 
@@ -41,6 +43,10 @@ class DavInfo(C.Structure):
         ("seconds", C.c_double),
         ("sigma_seconds", C.c_double),
         ("max_residual", C.c_double),
+        ("iters_bf16", C.c_int),
+        ("iters_fp32", C.c_int),
+        ("iters_fp64", C.c_int),
+        ("nmult_reference", C.c_int64),
     ]
 
 
@@ -77,6 +83,7 @@ SIGNATURES = {
                                   C.POINTER(C.c_int), _i64p]),
     "adcgpu_last_sigma_ms": (C.c_double, [_vp]),
     "adcgpu_device_bytes": (C.c_int64, [_vp]),
+    "adcgpu_sigma_stats": (C.c_int, [_vp, _dp, C.c_int]),
 }
 
 _lib = None

@@ -102,6 +102,11 @@ class DavidsonResult:
     nconv: int
     seconds: float
     sigma_seconds: float
+    max_residual: float = 0.0
+    iters_bf16: int = 0
+    iters_fp32: int = 0
+    iters_fp64: int = 0
+    nmult_reference: int = 0
 
 
 class AdcGpu:
@@ -192,24 +197,32 @@ class AdcGpu:
     def last_sigma_ms(self) -> float:
         return float(lib().adcgpu_last_sigma_ms(self._h))
 
+    def sigma_stats(self, reset: bool = False) -> dict:
+        out = np.zeros(4)
+        self._check(lib().adcgpu_sigma_stats(self._h, ptr(out), int(reset)), "sigma_stats")
+        return {"calls": int(out[0]), "ms": float(out[1]), "alg_bytes": float(out[2]), "columns": int(out[3])}
+
     def device_bytes(self) -> int:
         return int(lib().adcgpu_device_bytes(self._h))
 
     # -- solvers --------------------------------------------------------------
     def davdiag_block(self, davstates: int, davtol: float, dmain: int = 0, maxsubdim: int = -1, maxiter: int = 100,
                       precon: int = PRECON_DPR, ldfl: bool = True, lsubdiag: bool = False, guessdim: int = 800,
-                      precision: int = ADCGPU_FP64, refine: int = 3, want_vectors: bool = True,
+                      precision: int = ADCGPU_FP64, refine: int = 0, tol_bf16: float = 0.0,
+                      tol_fp32: float = 0.0, want_vectors: bool = True,
                       raise_on_nonconv: bool = True) -> DavidsonResult:
         p = DavParams(davstates=davstates, dmain=dmain, maxsubdim=maxsubdim, maxiter=maxiter, precon=precon,
                       ldfl=int(ldfl), lsubdiag=int(lsubdiag), guessdim=guessdim, davtol=davtol,
-                      precision=precision, refine=refine)
+                      precision=precision, refine=refine, tol_bf16=tol_bf16, tol_fp32=tol_fp32)
         ev = np.empty(davstates)
         vec = np.empty((self.ndim, davstates), order="F") if want_vectors else None
         info = DavInfo()
         st = lib().adcgpu_davidson(self._h, C.byref(p), ptr(ev), ptr(vec), C.byref(info))
         if st and not (st == 10 and not raise_on_nonconv):
             self._check(st, "davdiag_block")
-        return DavidsonResult(ev, vec, st, info.iterations, info.nmult, info.nconv, info.seconds, info.sigma_seconds)
+        return DavidsonResult(ev, vec, st, info.iterations, info.nmult, info.nconv, info.seconds, info.sigma_seconds,
+                              info.max_residual, info.iters_bf16, info.iters_fp32, info.iters_fp64,
+                              info.nmult_reference)
 
     def lancdiag_block(self, q0: np.ndarray, ncycles: int, orthotype: int = 0, want_tmat: bool = True,
                        want_evals: bool = True, want_ritz: bool = False):

@@ -250,27 +250,31 @@ __device__ inline double coupling(const Eri& E, int a, int k, const Double& r) {
   }
 }
 
-// One warp per double row: evaluates its structural entries, applies the
-// minc threshold (get_matrix.f90:904 etc.) and counts the kept ones.
+// One warp per stored row of B^T: evaluates its structural entries, applies
+// the minc threshold (get_matrix.f90:904 etc.), zeroes the padding and counts
+// the kept entries.
 __global__ void k_coupling(Eri E, GeomDev g, double* __restrict__ Bt, int64_t* __restrict__ rowcount) {
   const int lane = threadIdx.x & 31;
   const int64_t warp = (blockIdx.x * (int64_t)blockDim.x + threadIdx.x) >> 5;
   const int64_t nwarps = ((int64_t)gridDim.x * blockDim.x) >> 5;
-  for (int64_t d = warp; d < g.n2; d += nwarps) {
-    Double r = decode_double(g, d);
+  for (int64_t row_i = warp; row_i < g.n2; row_i += nwarps) {
+    Double r = decode_row(g, row_i);
     const int64_t L = g.len[r.cls];
-    double* row = Bt + g.off[r.cls] + (d - g.start[r.cls]) * L;
+    double* row = Bt + g.off[r.cls] + (row_i - g.start[r.cls]) * L;
     int cnt = 0;
     for (int e = lane; e < L; e += 32) {
       int64_t s = entry_single(g, r, e);
-      int a = (int)(s / g.no), k = (int)(s % g.no);
-      double x = coupling(E, a, k, r);
-      bool keep = fabs(x) > MINC;
+      double x = 0.0;
+      if (s >= 0) {
+        int a = (int)(s / g.no), k = (int)(s % g.no);
+        x = coupling(E, a, k, r);
+      }
+      bool keep = s >= 0 && fabs(x) > MINC;
       row[e] = keep ? x : 0.0;
       cnt += keep;
     }
     for (int o = 16; o; o >>= 1) cnt += __shfl_xor_sync(0xffffffffu, cnt, o);
-    if (lane == 0) rowcount[d] = cnt;
+    if (lane == 0) rowcount[row_i] = cnt;
   }
 }
 
@@ -321,11 +325,12 @@ __global__ void k_export_coupling(GeomDev g, const double* __restrict__ Bt, cons
   const int lane = threadIdx.x & 31;
   const int64_t warp = (blockIdx.x * (int64_t)blockDim.x + threadIdx.x) >> 5;
   const int64_t nwarps = ((int64_t)gridDim.x * blockDim.x) >> 5;
-  for (int64_t d = warp; d < g.n2; d += nwarps) {
-    Double r = decode_double(g, d);
+  for (int64_t row_i = warp; row_i < g.n2; row_i += nwarps) {
+    Double r = decode_row(g, row_i);
+    const int64_t d = row_to_d(g, r, row_i);
     const int64_t L = g.len[r.cls];
-    const double* row = Bt + g.off[r.cls] + (d - g.start[r.cls]) * L;
-    int64_t base = pos[d];
+    const double* row = Bt + g.off[r.cls] + (row_i - g.start[r.cls]) * L;
+    int64_t base = pos[row_i];
     for (int e0 = 0; e0 < L; e0 += 32) {
       int e = e0 + lane;
       double x = e < L ? row[e] : 0.0;

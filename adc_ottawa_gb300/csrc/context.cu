@@ -34,8 +34,6 @@ void dfree(Ctx* c, void* p, size_t bytes) {
   if (bytes) c->dev_bytes -= (int64_t)bytes;
 }
 
-int prepare_desc(Ctx* c);
-
 static void free_matrix(Ctx* c) {
   void** ps[] = {(void**)&c->d_diag, (void**)&c->d_A, (void**)&c->d_Bt, (void**)&c->d_A32, (void**)&c->d_Bt16,
                  (void**)&c->d_Bt32, (void**)&c->d_diag32, (void**)&c->d_rowcount, &c->d_ws};
@@ -44,6 +42,7 @@ static void free_matrix(Ctx* c) {
     *p = nullptr;
   }
   c->ws_bytes = 0;
+  free_sigma_plan(c);
   c->have_matrix = false;
 }
 
@@ -100,6 +99,8 @@ int adcgpu_ctx_destroy(adcgpu_ctx* h) {
   if (c->d_sil) cudaFree(c->d_sil);
   cudaEventDestroy(c->ev0);
   cudaEventDestroy(c->ev1);
+  if (c->st_ev0) cudaEventDestroy(c->st_ev0);
+  if (c->st_ev1) cudaEventDestroy(c->st_ev1);
   cudaStreamDestroy(c->stream);
   delete c;
   return ADCGPU_OK;
@@ -113,8 +114,8 @@ const char* adcgpu_last_error(const adcgpu_ctx* h) {
 int adcgpu_set_orbitals(adcgpu_ctx* h, int nocc, int nvirt, const double* e) {
   Ctx* c = reinterpret_cast<Ctx*>(h);
   CTX_CHECK(c);
-  if (nocc <= 0 || nvirt <= 1 || nocc > 255 || nvirt > 65535 || !e)
-    return set_err(c, ADCGPU_BAD_INPUT, "nocc in [1,255], nvirt in [2,65535] and e required");
+  if (nocc <= 0 || nvirt <= 1 || nocc > 32 || nvirt > 256 || !e)
+    return set_err(c, ADCGPU_BAD_INPUT, "nocc in [1,32], nvirt in [2,256] and e required");
   Geometry g;
   g.init(nocc, nvirt);
   if (g.N > INT32_MAX) return set_err(c, ADCGPU_UNSUPPORTED, "ADC(2) dimension exceeds int32 kpq indexing");

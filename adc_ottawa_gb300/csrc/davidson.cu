@@ -237,8 +237,14 @@ struct DavidsonGPU {
     return ADCGPU_OK;
   }
 
+  int64_t nmult_ref = 0;       // sum of currdim over iterations (reference hxvec columns)
+  double max_res = 0.0;        // largest residual norm among the returned roots
+  std::vector<double> Cnorm;   // residual norms of the deflated roots
+
+  // evecs_dev: capacity ncap >= nstates columns; receives the nstates roots
+  // (ascending) followed by the other current Ritz vectors; *nout = count.
   int run(const std::vector<double>& hdiag, int guess_kind, int guessdim, const T* guess_dev, int nguess,
-          std::vector<double>& evals_out, T* evecs_dev, int* iters_out, int* nconv_out) {
+          std::vector<double>& evals_out, T* evecs_dev, int ncap, int* nout, int* iters_out, int* nconv_out) {
     ST(alloc());
     if (guess_kind == 1) ST(guess_subdiag(hdiag, guessdim));
     else if (guess_kind == 2) ST(guess_vectors(guess_dev, nguess));
@@ -250,6 +256,7 @@ struct DavidsonGPU {
     std::vector<double> S;
     for (int k = 1; k <= niter; ++k) {
       iters = k;
+      nmult_ref += currdim;
       // hxvec: only the columns without a product
       ST(sigma_cols(nW, currdim));
       // calcrmat: new columns of the Rayleigh matrix (upper triangle)
@@ -292,6 +299,7 @@ struct DavidsonGPU {
           // store the converged vector and value
           ADC_CUDA(c, cudaMemcpyAsync(col(Cv, nconv_store), col(X, src), bytes_v, cudaMemcpyDeviceToDevice, c->stream));
           Cval.push_back(lam[src]);
+          Cnorm.push_back(norm[src]);
           ++nconv_store;
           if (indx != src) {
             ADC_CUDA(c, cudaMemcpyAsync(col(X, src), col(X, indx), bytes_v, cudaMemcpyDeviceToDevice, c->stream));
@@ -358,14 +366,23 @@ struct DavidsonGPU {
     if (nstates > 1) host_heapsort_index(nstates, ev.data(), indx);
     else indx.assign(1, 1);
     evals_out.resize(nstates);
+    max_res = 0.0;
+    for (int i = 0; i < nstates_curr; ++i) max_res = std::max(max_res, norm[i]);
+    for (double v : Cnorm) max_res = std::max(max_res, v);
+    int nw = 0;
     for (int i = 0; i < nstates; ++i) {
       int k = (int)indx[i] - 1;
       evals_out[i] = ev[k];
       if (evecs_dev) {
         const T* src = src_col[k] >= 0 ? col(X, src_col[k]) : col(Cv, -src_col[k] - 1);
         ADC_CUDA(c, cudaMemcpyAsync(evecs_dev + (size_t)i * N, src, bytes_v, cudaMemcpyDeviceToDevice, c->stream));
+        ++nw;
       }
     }
+    // the remaining current Ritz vectors (useful as a warm start)
+    for (int i = nstates_curr; evecs_dev && i < bs_curr && nw < ncap; ++i, ++nw)
+      ADC_CUDA(c, cudaMemcpyAsync(evecs_dev + (size_t)nw * N, col(X, i), bytes_v, cudaMemcpyDeviceToDevice, c->stream));
+    if (nout) *nout = nw;
     ADC_CUDA(c, cudaStreamSynchronize(c->stream));
     *iters_out = iters;
     *nconv_out = nconv;
@@ -393,11 +410,11 @@ __global__ void k_gather_sub(GeomDev g, const double* __restrict__ A, const doub
       if (p < g.n1 && q < g.n1) v = A[p * g.n1 + q];
       else if (p < g.n1 || q < g.n1) {
         int64_t s = p < g.n1 ? p : q, dd = (p < g.n1 ? q : p) - g.n1;
-        uint2 qd = desc[dd];
-        int ap = qd.x & 0xFFFF, bp = qd.x >> 16, kp = qd.y & 0xFF, lp = (qd.y >> 8) & 0xFF, cls = qd.y >> 16;
-        Double r{ap, bp, kp, lp, cls};
-        const int64_t L = g.len[cls];
-        const double* row = Bt + g.off[cls] + (dd - g.start[cls]) * L;
+        Double r = decode_double(g, dd);
+        // storage row of the double (class 2 is stored hole-outer)
+        int64_t rw = r.cls == 1 ? g.start[1] + (int64_t)r.kp * g.npair_v + pair_index(r.ap, r.bp, g.nv) : dd;
+        const int64_t L = g.len[r.cls];
+        const double* row = Bt + g.off[r.cls] + (rw - g.start[r.cls]) * L;
         for (int e = 0; e < L; ++e)
           if (entry_single(g, r, e) == s) { v = row[e]; break; }
       }
@@ -422,7 +439,7 @@ int DavidsonGPU<T>::guess_subdiag(const std::vector<double>& hdiag, int subdim) 
   ST(dmalloc(c, (void**)&d_sub, sizeof(int64_t) * subdim));
   ST(dmalloc(c, (void**)&d_H, sizeof(double) * (size_t)subdim * subdim));
   ADC_CUDA(c, cudaMemcpyAsync(d_sub, sub.data(), sizeof(int64_t) * subdim, cudaMemcpyHostToDevice, c->stream));
-  k_gather_sub<<<152 * 4, 256, 0, c->stream>>>(to_dev(c->geom), c->d_A, c->d_Bt, (const uint2*)c->d_ws, d_sub,
+  k_gather_sub<<<152 * 4, 256, 0, c->stream>>>(to_dev(c->geom), c->d_A, c->d_Bt, nullptr, d_sub,
                                                subdim, d_H);
   std::vector<double> H((size_t)subdim * subdim), w(subdim), Vs((size_t)subdim * subdim);
   ADC_CUDA(c, cudaMemcpyAsync(H.data(), d_H, sizeof(double) * H.size(), cudaMemcpyDeviceToHost, c->stream));
@@ -445,7 +462,15 @@ template struct DavidsonGPU<double>;
 template struct DavidsonGPU<float>;
 
 // ---------------------------------------------------------------------------
-// Driver used by the C ABI: FP64 path, or mixed path + FP64 refinement.
+// Driver used by the C ABI.
+//   FP64  : one FP64 Davidson (the plain drop-in path).
+//   MIXED : a precision ladder, each phase warm-started with the previous
+//           phase's block of Ritz vectors:
+//             1. BF16 matrix values, FP32 vectors, to residual tol_bf16
+//             2. FP32 matrix values, FP32 vectors, to residual tol_fp32
+//             3. FP64 refinement to davtol: the FP64 residual norm decides
+//           Rayleigh-Ritz, Gram-Schmidt and residual norms are FP64 in every
+//           phase (davidson.cu DavidsonGPU).
 // ---------------------------------------------------------------------------
 int davidson_solve(Ctx* c, const adcgpu_dav_params* p, double* evals, double* evecs, adcgpu_dav_info* info,
                    const MlpPrecond* mlp) {
@@ -464,58 +489,66 @@ int davidson_solve(Ctx* c, const adcgpu_dav_params* p, double* evals, double* ev
   std::vector<double> hdiag(N);
   ADC_CUDA(c, cudaMemcpy(hdiag.data(), c->d_diag, sizeof(double) * N, cudaMemcpyDeviceToHost));
   const int guess_kind = p->lsubdiag ? 1 : 0;
-  int st;
+  const int precon64 = p->precon == ADCGPU_PRECON_MLP ? ADCGPU_PRECON_DPR : p->precon;
+  int st = ADCGPU_OK;
   adcgpu_dav_info inf{};
   std::vector<double> ev;
+  double* out64 = nullptr;
+  ST(dmalloc(c, (void**)&out64, sizeof(double) * (size_t)N * blocksize));
   if (p->precision == ADCGPU_MIXED) {
-    if (c->precision != ADCGPU_MIXED) return set_err(c, ADCGPU_BAD_INPUT, "matrix was not built for MIXED");
-    // phase 1: FP32 vectors / BF16-FP32 matrix, to a residual the FP32
-    // product can resolve
-    DavidsonGPU<float> D;
-    D.c = c; D.N = N; D.nstates = nstates; D.blocksize = blocksize; D.maxvec = maxvec;
-    D.niter = p->maxiter; D.ipre = p->precon; D.ldeflate = p->ldfl != 0;
-    D.tol = std::max(p->davtol, 1e-4);
-    D.hii = c->d_diag32; D.mlp = mlp;
-    float* ev32 = nullptr;
-    ST(dmalloc(c, (void**)&ev32, sizeof(float) * (size_t)N * blocksize));
-    int it1 = 0, nc1 = 0;
-    st = D.run(hdiag, guess_kind, p->guessdim, nullptr, 0, ev, ev32, &it1, &nc1);
-    inf.iterations += it1; inf.nmult += D.nmult; inf.sigma_seconds += D.sigma_s;
-    D.release();
-    if (st && st != ADCGPU_NOT_CONVERGED) { dfree(c, ev32, 0); return st; }
-    // phase 2: FP64 refinement from the mixed-precision Ritz vectors
+    if (c->precision != ADCGPU_MIXED) { dfree(c, out64, 0); return set_err(c, ADCGPU_BAD_INPUT, "matrix was not built for MIXED"); }
+    const double tol_b = p->tol_bf16 == 0.0 ? 1e-2 : p->tol_bf16;
+    const double tol_f = p->tol_fp32 == 0.0 ? 1e-5 : p->tol_fp32;
+    float* g32 = nullptr;
+    ST(dmalloc(c, (void**)&g32, sizeof(float) * (size_t)N * blocksize));
+    int nguess = 0;
+    for (int phase = 0; phase < 2; ++phase) {
+      if (phase == 0 && tol_b < 0) continue;
+      c->mixed_bf16 = phase == 0 ? 1 : 0;
+      DavidsonGPU<float> D;
+      D.c = c; D.N = N; D.nstates = nstates; D.blocksize = blocksize; D.maxvec = maxvec;
+      D.niter = p->maxiter; D.ipre = p->precon; D.ldeflate = p->ldfl != 0;
+      D.tol = std::max(p->davtol, phase == 0 ? tol_b : tol_f);
+      D.hii = c->d_diag32; D.mlp = mlp;
+      int it = 0, nc = 0;
+      st = D.run(hdiag, nguess ? 2 : guess_kind, p->guessdim, g32, nguess, ev, g32, blocksize, &nguess, &it, &nc);
+      inf.iterations += it; inf.nmult += D.nmult; inf.sigma_seconds += D.sigma_s;
+      inf.nmult_reference += D.nmult_ref;
+      if (phase == 0) inf.iters_bf16 = it; else inf.iters_fp32 = it;
+      D.release();
+      if (st && st != ADCGPU_NOT_CONVERGED) { dfree(c, g32, 0); dfree(c, out64, 0); return st; }
+    }
+    c->mixed_bf16 = 1;
+    // FP64 refinement from the mixed-precision Ritz block
     double* g64 = nullptr;
-    ST(dmalloc(c, (void**)&g64, sizeof(double) * (size_t)N * nstates));
-    ST((convert<float, double>(c, ev32, g64, (int64_t)N * nstates)));
-    dfree(c, ev32, 0);
+    ST(dmalloc(c, (void**)&g64, sizeof(double) * (size_t)N * blocksize));
+    ST((convert<float, double>(c, g32, g64, (int64_t)N * nguess)));
+    dfree(c, g32, 0);
     DavidsonGPU<double> F;
-    F.c = c; F.N = N; F.nstates = nstates; F.blocksize = nstates; F.maxvec = std::max(2, p->refine > 0 ? p->refine : 3) * nstates;
-    F.niter = p->maxiter; F.ipre = p->precon == ADCGPU_PRECON_MLP ? ADCGPU_PRECON_DPR : p->precon;
+    F.c = c; F.N = N; F.nstates = nstates; F.blocksize = blocksize;
+    F.maxvec = (p->refine > 1 ? p->refine : 4) * blocksize;
+    F.niter = p->maxiter; F.ipre = precon64;
     F.ldeflate = p->ldfl != 0; F.tol = p->davtol; F.hii = c->d_diag;
-    double* out64 = nullptr;
-    ST(dmalloc(c, (void**)&out64, sizeof(double) * (size_t)N * nstates));
-    int it2 = 0, nc2 = 0;
-    st = F.run(hdiag, 2, 0, g64, nstates, ev, out64, &it2, &nc2);
-    inf.iterations += it2; inf.nmult += F.nmult; inf.sigma_seconds += F.sigma_s; inf.nconv = nc2;
+    int it2 = 0, nc2 = 0, nout = 0;
+    st = F.run(hdiag, 2, 0, g64, nguess, ev, out64, blocksize, &nout, &it2, &nc2);
+    inf.iterations += it2; inf.iters_fp64 = it2; inf.nmult += F.nmult; inf.sigma_seconds += F.sigma_s;
+    inf.nmult_reference += F.nmult_ref; inf.nconv = nc2; inf.max_residual = F.max_res;
     F.release();
     dfree(c, g64, 0);
-    if (evecs) cudaMemcpy(evecs, out64, sizeof(double) * (size_t)N * nstates, cudaMemcpyDeviceToHost);
-    dfree(c, out64, 0);
   } else {
     DavidsonGPU<double> D;
     D.c = c; D.N = N; D.nstates = nstates; D.blocksize = blocksize; D.maxvec = maxvec;
-    D.niter = p->maxiter; D.ipre = p->precon == ADCGPU_PRECON_MLP ? ADCGPU_PRECON_DPR : p->precon;
+    D.niter = p->maxiter; D.ipre = precon64;
     D.ldeflate = p->ldfl != 0; D.tol = p->davtol; D.hii = c->d_diag;
-    double* out = nullptr;
-    ST(dmalloc(c, (void**)&out, sizeof(double) * (size_t)N * nstates));
-    int it = 0, nc = 0;
-    st = D.run(hdiag, guess_kind, p->guessdim, nullptr, 0, ev, out, &it, &nc);
-    inf.iterations = it; inf.nmult = D.nmult; inf.sigma_seconds = D.sigma_s; inf.nconv = nc;
+    int it = 0, nc = 0, nout = 0;
+    st = D.run(hdiag, guess_kind, p->guessdim, nullptr, 0, ev, out64, blocksize, &nout, &it, &nc);
+    inf.iterations = it; inf.iters_fp64 = it; inf.nmult = D.nmult; inf.sigma_seconds = D.sigma_s; inf.nconv = nc;
+    inf.nmult_reference = D.nmult_ref; inf.max_residual = D.max_res;
     D.release();
-    if (evecs && (st == ADCGPU_OK || st == ADCGPU_NOT_CONVERGED))
-      cudaMemcpy(evecs, out, sizeof(double) * (size_t)N * nstates, cudaMemcpyDeviceToHost);
-    dfree(c, out, 0);
   }
+  if (evecs && (st == ADCGPU_OK || st == ADCGPU_NOT_CONVERGED))
+    cudaMemcpy(evecs, out64, sizeof(double) * (size_t)N * nstates, cudaMemcpyDeviceToHost);
+  dfree(c, out64, 0);
   if (st && st != ADCGPU_NOT_CONVERGED) return st;
   for (int i = 0; i < nstates; ++i) evals[i] = ev[i];
   inf.seconds = now_s() - t_start;

@@ -13,15 +13,21 @@
 // B^T is a closed-form function of d.  Each row holds its structural entries
 // in a fixed segment order and values with |h| <= minc are stored as 0.0, so
 // the matrix equals the reference's thresholded COO exactly while the sigma
-// product streams 8 bytes per entry instead of 16.
+// product streams only values (8, 4 or 2 bytes per entry), no indices.
 //
 //   segment A : singles (a',k), k = 0..no-1           (always)
 //   segment B : singles (b',k), k = 0..no-1           (a' != b')
-//   segment C : singles (a,k'),  a = 0..nv-1, a not in {a',b'}
-//   segment D : singles (a,l'),  a = 0..nv-1, a not in {a',b'}   (k' != l')
+//   segment C : singles (a,k'),  a = 0..nv-1          (padded: 0 at a in {a',b'})
+//   segment D : singles (a,l'),  a = 0..nv-1          (k' != l'; padded likewise)
 //
-// Row lengths: class 1 (a'=b',k'=l') no+nv-1; class 2 (a'<b',k'=l') 2no+nv-2;
-// class 3 (a'=b',k'<l') no+2nv-2; classes 4I/4II 2no+2nv-4.
+// Row lengths: class 1 (a'=b',k'=l') no+nv; class 2 (a'<b',k'=l') 2no+nv;
+// class 3 (a'=b',k'<l') no+2nv; classes 4I/4II 2no+2nv.  Segments C and D are
+// padded to the full virtual range so that lane a of a warp always owns
+// single (a,k'): the sigma product then accumulates B V2 in registers.
+//
+// Storage order of rows ("slabs" of fixed (k',l')): classes 1, 3, 4I, 4II in
+// the kpq order (hole indices outer); class 2 hole-outer (k' outer, pair
+// (a'<b') inner), the transpose of its kpq order (pair outer, hole inner).
 //
 // All indices below are 0-based: occupied i in [0,no), virtual a in [0,nv)
 // (orbital no+a), single s = a*no + k (select_atom_is order), doubles in the
@@ -66,15 +72,16 @@ struct Geometry {
     N = n1 + n2;
     start[0] = 0; start[1] = c1; start[2] = c1 + c2; start[3] = c1 + c2 + c3;
     start[4] = start[3] + c4; start[5] = n2;
-    len[0] = no + nv - 1;
-    len[1] = 2 * no + nv - 2;
-    len[2] = no + 2 * nv - 2;
-    len[3] = 2 * no + 2 * nv - 4;
+    len[0] = no + nv;
+    len[1] = 2 * no + nv;
+    len[2] = no + 2 * nv;
+    len[3] = 2 * no + 2 * nv;
     len[4] = len[3];
     off[0] = 0;
     for (int c = 0; c < 5; ++c) off[c + 1] = off[c] + (start[c + 1] - start[c]) * len[c];
   }
-  int64_t structural_nnz() const { return n1 * (n1 - 1) / 2 + off[5]; }
+  // rows of one slab (fixed k',l') per class
+  int64_t slab_len(int c) const { return (c == 0 || c == 2) ? nv : npair_v; }
 };
 
 // Decoded double: virtuals a' <= b', occupied k' <= l', class 0..4.
@@ -136,7 +143,27 @@ __host__ __device__ inline Double decode_double(const GeomDev& g, int64_t d) {
   return r;
 }
 
-// Single index of entry e of the B^T row of double r (segment order above).
+// Storage row -> configuration (storage order described above).
+__host__ __device__ inline Double decode_row(const GeomDev& g, int64_t row) {
+  if (row >= g.start[1] && row < g.start[2]) {
+    int64_t t = row - g.start[1];
+    Double r;
+    r.cls = 1;
+    r.kp = r.lp = (int)(t / g.npair_v);
+    pair_decode(t % g.npair_v, g.nv, r.ap, r.bp);
+    return r;
+  }
+  return decode_double(g, row);
+}
+
+// Storage row of a configuration -> its doubles-local (kpq) index.
+__host__ __device__ inline int64_t row_to_d(const GeomDev& g, const Double& r, int64_t row) {
+  if (r.cls == 1) return g.start[1] + pair_index(r.ap, r.bp, g.nv) * g.no + r.kp;
+  return row;
+}
+
+// Single index of entry e of the B^T row of double r, or -1 for a padding
+// position of segments C/D.
 __host__ __device__ inline int64_t entry_single(const GeomDev& g, const Double& r, int e) {
   const int no = g.no;
   if (e < no) return (int64_t)r.ap * no + e;                   // segment A
@@ -146,15 +173,10 @@ __host__ __device__ inline int64_t entry_single(const GeomDev& g, const Double& 
     if (e < no) return (int64_t)r.bp * no + e;                 // segment B
     e -= no;
   }
-  const int nseg = g.nv - (twoa ? 2 : 1);
-  int seg = e / nseg;                                           // 0: C (k'), 1: D (l')
-  int t = e - seg * nseg;
-  // t-th virtual not in {a',b'}
-  int a = t;
-  if (a >= r.ap) ++a;
-  if (twoa && a >= r.bp) ++a;
-  int occ = seg == 0 ? r.kp : r.lp;
-  return (int64_t)a * no + occ;
+  const int seg = e / g.nv;                                     // 0: C (k'), 1: D (l')
+  const int a = e - seg * g.nv;
+  if (a == r.ap || a == r.bp) return -1;
+  return (int64_t)a * no + (seg == 0 ? r.kp : r.lp);
 }
 
 // ---------------------------------------------------------------------------
@@ -193,10 +215,18 @@ struct Ctx {
   int64_t nnz_kept = 0;           // reference noffd
   int64_t nnz_ph = 0;             // kept ph-ph entries
   int64_t* d_rowcount = nullptr;  // kept entries per double row (for COO export)
-  // sigma workspace
+  // sigma work lists (SigmaPlan, sigma.cu)
+  void* sigma_plan = nullptr;
   void* d_ws = nullptr;
   size_t ws_bytes = 0;
   double last_sigma_ms = 0.0;
+  // sigma statistics (adcgpu_sigma_stats)
+  int64_t st_calls = 0, st_cols = 0;
+  double st_ms = 0.0, st_bytes = 0.0;
+  cudaEvent_t st_ev0 = nullptr, st_ev1 = nullptr;
+  bool st_pending = false;
+  double st_pending_bytes = 0.0;
+  int st_pending_cols = 0;
   int64_t dev_bytes = 0;
   // SIL persistent state for adcgpu_silstep (device Krylov vectors)
   double* d_sil = nullptr;
@@ -227,6 +257,13 @@ int build_matrix(Ctx* c);
 int export_coo_device(Ctx* c, double* d_h, int32_t* d_oi, int32_t* d_oj);
 
 // sigma.cu : W = H V for m columns (column-major, leading dim ld), FP64 or FP32.
+struct SigmaPlan {
+  int2* d_chunks = nullptr;   // pass 1: [row_begin, row_end) inside one slab
+  int2* d_items = nullptr;    // pass 2: (first row of slab, b')
+  int nchunks = 0, nitems = 0;
+};
+int prepare_desc(Ctx* c);
+void free_sigma_plan(Ctx* c);
 int sigma_fp64(Ctx* c, int m, const double* dV, int64_t ldv, double* dW, int64_t ldw);
 int sigma_fp32(Ctx* c, int m, const float* dV, int64_t ldv, float* dW, int64_t ldw);
 int prepare_mixed(Ctx* c);

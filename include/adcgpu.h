@@ -130,8 +130,10 @@ int adcgpu_build_adc2s(adcgpu_ctx* ctx, int ndim, const int32_t* kpq,
 int adcgpu_get_diag(adcgpu_ctx* ctx, double* hii);
 
 /* The kept off-diagonal elements as COO (h, oi<oj, 1-based), the content of
-   SCRATCH/hmlt.off<flag>.  Order: row oi ascending, then oj ascending.
-   cap must be >= noffd. */
+   SCRATCH/hmlt.off<flag>.  As in the reference, whose file order depends on
+   the OpenMP schedule (get_matrix.f90:1059-1125), only the set is defined:
+   the ph-ph block comes first (row-major), then the coupling block in the
+   device's storage order.  cap must be >= noffd. */
 int adcgpu_export_coo(adcgpu_ctx* ctx, int64_t cap, double* h, int32_t* oi,
                       int32_t* oj);
 
@@ -166,16 +168,24 @@ typedef struct {
   int guessdim;      /* subspace dimension for initvec_subdiag      */
   double davtol;     /* residual-norm tolerance                     */
   int precision;     /* adcgpu_precision for the iterations         */
-  int refine;        /* MIXED only: FP64 refinement sweeps at the end */
+  int refine;        /* MIXED: maxvec of the FP64 refinement, in blocks (0: 4) */
+  double tol_bf16;   /* MIXED: residual at which the BF16-valued phase hands
+                        over to the FP32-valued phase (0: 1e-2; <0: skip)    */
+  double tol_fp32;   /* MIXED: residual at which the FP32 phase hands over to
+                        the FP64 refinement (0: 1e-5)                        */
 } adcgpu_dav_params;
 
 typedef struct {
-  int iterations;    /* Davidson iterations performed             */
+  int iterations;    /* Davidson iterations performed (all phases) */
   int64_t nmult;     /* sigma-vector columns computed             */
   int nconv;         /* converged roots                           */
   double seconds;    /* wall time inside the solver               */
   double sigma_seconds;  /* time in the sigma-vector kernels      */
   double max_residual;   /* FP64 residual norm of the worst root  */
+  int iters_bf16, iters_fp32, iters_fp64;   /* iterations per phase    */
+  int64_t nmult_reference;  /* sigma columns the reference algorithm would
+                               compute (it re-multiplies all currdim
+                               columns every iteration)                 */
 } adcgpu_dav_info;
 
 /* evals[davstates] ascending; evecs ndim x davstates column-major (may be
@@ -244,6 +254,14 @@ double adcgpu_last_sigma_ms(const adcgpu_ctx* ctx);
 
 /* Device bytes held by the context (matrix, ERI blocks, work spaces). */
 int64_t adcgpu_device_bytes(const adcgpu_ctx* ctx);
+
+/* Sigma-product statistics accumulated since the last reset, measured with
+   CUDA events on the context's stream around every sigma call (including
+   those inside the solvers): out[0] calls, out[1] total device milliseconds,
+   out[2] algorithmic bytes (each stored matrix value read once per call,
+   diagonal, vectors read and written once), out[3] columns multiplied.
+   reset != 0 clears the counters after reading. */
+int adcgpu_sigma_stats(adcgpu_ctx* ctx, double* out4, int reset);
 
 #ifdef __cplusplus
 }
