@@ -1,0 +1,251 @@
+!#######################################################################
+! adcgpu_iface: ISO_C_BINDING interface to libadcgpu.so (include/adcgpu.h)
+! and drop-in wrappers for the ADC(2)-s hot path of ADC_ottawa.
+!
+! The wrappers keep the reference's argument lists and read the same
+! module globals (parameters.f90), so the drivers change only the name
+! they call:
+!
+!   write_fspace_adc2_1  -> write_fspace_adc2_1_gpu   (fspacetrial.f90:533)
+!   davdiag_block        -> davdiag_block_gpu         (block_davidson.f90:33)
+!   lancdiag_block       -> lancdiag_block_gpu        (block_lanczos.f90:28)
+!   propagate_fvec       -> propagate_fvec_gpu        (fvecprop.f90:27)
+!
+! A non-zero status from the library is turned into errmsg +
+! error_control, as the reference does for its own failures.
+!#######################################################################
+module adcgpu_iface
+
+  use iso_c_binding
+  implicit none
+
+  type, bind(C) :: adcgpu_dav_params
+     integer(c_int) :: davstates, dmain, maxsubdim, maxiter, precon, ldfl, &
+                       lsubdiag, guessdim
+     real(c_double) :: davtol
+     integer(c_int) :: precision, refine
+     real(c_double) :: tol_bf16, tol_fp32
+  end type adcgpu_dav_params
+
+  type, bind(C) :: adcgpu_dav_info
+     integer(c_int)     :: iterations
+     integer(c_int64_t) :: nmult
+     integer(c_int)     :: nconv
+     real(c_double)     :: seconds, sigma_seconds, max_residual
+     integer(c_int)     :: iters_bf16, iters_fp32, iters_fp64
+     integer(c_int64_t) :: nmult_reference
+  end type adcgpu_dav_info
+
+  interface
+     integer(c_int) function adcgpu_ctx_create(device, ctx) bind(C, name="adcgpu_ctx_create")
+       import :: c_int, c_ptr
+       integer(c_int), value :: device
+       type(c_ptr)           :: ctx
+     end function adcgpu_ctx_create
+
+     integer(c_int) function adcgpu_ctx_destroy(ctx) bind(C, name="adcgpu_ctx_destroy")
+       import :: c_int, c_ptr
+       type(c_ptr), value :: ctx
+     end function adcgpu_ctx_destroy
+
+     integer(c_int) function adcgpu_set_orbitals(ctx, nocc, nvirt, e) bind(C, name="adcgpu_set_orbitals")
+       import :: c_int, c_ptr, c_double
+       type(c_ptr), value    :: ctx
+       integer(c_int), value :: nocc, nvirt
+       real(c_double)        :: e(*)
+     end function adcgpu_set_orbitals
+
+     integer(c_int) function adcgpu_set_eri_mo_complex(ctx, buf) bind(C, name="adcgpu_set_eri_mo_complex")
+       import :: c_int, c_ptr
+       type(c_ptr), value :: ctx
+       type(c_ptr), value :: buf      ! c_loc(moIntegrals%buffer_real)
+     end function adcgpu_set_eri_mo_complex
+
+     integer(c_int) function adcgpu_build_adc2s(ctx, ndim, kpq, noffd, flag, precision) &
+          bind(C, name="adcgpu_build_adc2s")
+       import :: c_int, c_ptr, c_int32_t, c_int64_t, c_char
+       type(c_ptr), value          :: ctx
+       integer(c_int), value       :: ndim, precision
+       integer(c_int32_t)          :: kpq(*)
+       integer(c_int64_t)          :: noffd
+       character(kind=c_char), value :: flag
+     end function adcgpu_build_adc2s
+
+     integer(c_int) function adcgpu_write_hmlt_files(ctx, dir, flag) bind(C, name="adcgpu_write_hmlt_files")
+       import :: c_int, c_ptr, c_char
+       type(c_ptr), value            :: ctx
+       character(kind=c_char)        :: dir(*)
+       character(kind=c_char), value :: flag
+     end function adcgpu_write_hmlt_files
+
+     integer(c_int) function adcgpu_davidson(ctx, p, evals, evecs, info) bind(C, name="adcgpu_davidson")
+       import :: c_int, c_ptr, c_double, adcgpu_dav_params, adcgpu_dav_info
+       type(c_ptr), value      :: ctx
+       type(adcgpu_dav_params) :: p
+       real(c_double)          :: evals(*), evecs(*)
+       type(adcgpu_dav_info)   :: info
+     end function adcgpu_davidson
+
+     integer(c_int) function adcgpu_write_davidson_file(path, ndim, nstates, evals, evecs) &
+          bind(C, name="adcgpu_write_davidson_file")
+       import :: c_int, c_double, c_char
+       character(kind=c_char)   :: path(*)
+       integer(c_int), value    :: ndim, nstates
+       real(c_double)           :: evals(*), evecs(*)
+     end function adcgpu_write_davidson_file
+
+     integer(c_int) function adcgpu_block_lanczos(ctx, lmain, ncycles, orthotype, q0, tmat, evals, ritz) &
+          bind(C, name="adcgpu_block_lanczos")
+       import :: c_int, c_ptr, c_double
+       type(c_ptr), value    :: ctx
+       integer(c_int), value :: lmain, ncycles, orthotype
+       real(c_double)        :: q0(*)
+       type(c_ptr), value    :: tmat, evals, ritz
+     end function adcgpu_block_lanczos
+
+     integer(c_int) function adcgpu_autocorr(ctx, nwp, f, tout, tfinal, kdim, tol, auto, ntimes, nmult) &
+          bind(C, name="adcgpu_autocorr")
+       import :: c_int, c_ptr, c_double, c_int64_t
+       type(c_ptr), value    :: ctx
+       integer(c_int), value :: nwp, kdim
+       real(c_double)        :: f(*)
+       real(c_double), value :: tout, tfinal, tol
+       complex(c_double)     :: auto(*)
+       integer(c_int)        :: ntimes
+       integer(c_int64_t)    :: nmult
+     end function adcgpu_autocorr
+
+     type(c_ptr) function adcgpu_last_error(ctx) bind(C, name="adcgpu_last_error")
+       import :: c_ptr
+       type(c_ptr), value :: ctx
+     end function adcgpu_last_error
+  end interface
+
+  type(c_ptr), save :: gpu_ctx = c_null_ptr
+
+contains
+
+!#######################################################################
+
+  subroutine adcgpu_check(st, where)
+    use iomod, only: error_control, errmsg
+    integer(c_int), intent(in)   :: st
+    character(len=*), intent(in) :: where
+    if (st.ne.0) then
+       write(errmsg,'(a,a,i3)') trim(where),': libadcgpu status ',st
+       call error_control
+    endif
+  end subroutine adcgpu_check
+
+!#######################################################################
+! Creates the context and uploads the orbital energies and the MO ERIs
+! (moIntegrals%buffer_real, read through vpqrs in the reference).
+
+  subroutine adcgpu_init
+    use parameters, only: e, nocc, nvirt, moIntegrals
+    integer(c_int) :: st
+    if (c_associated(gpu_ctx)) return
+    st = adcgpu_ctx_create(0_c_int, gpu_ctx)
+    call adcgpu_check(st, 'adcgpu_ctx_create')
+    st = adcgpu_set_orbitals(gpu_ctx, int(nocc,c_int), int(nvirt,c_int), e)
+    call adcgpu_check(st, 'adcgpu_set_orbitals')
+    st = adcgpu_set_eri_mo_complex(gpu_ctx, c_loc(moIntegrals%buffer_real))
+    call adcgpu_check(st, 'adcgpu_set_eri_mo_complex')
+  end subroutine adcgpu_init
+
+!#######################################################################
+! write_fspace_adc2_1 (fspacetrial.f90:533-564): the matrix stays on the
+! device; the SCRATCH files are also written so that unmodified consumers
+! of hmlt.dia/hmlt.off keep working.
+
+  subroutine write_fspace_adc2_1_gpu(ndim, kpq, noffdel, chr)
+    use parameters, only: nbas, nocc
+    integer, intent(in)                                 :: ndim
+    integer, dimension(7,0:nBas**2*nOcc**2), intent(in) :: kpq
+    integer*8, intent(out)                              :: noffdel
+    character(1), intent(in)                            :: chr
+    integer(c_int)     :: st
+    integer(c_int64_t) :: n
+    call adcgpu_init
+    st = adcgpu_build_adc2s(gpu_ctx, int(ndim,c_int), kpq, n, chr, 0_c_int)
+    call adcgpu_check(st, 'write_fspace_adc2_1')
+    noffdel = n
+    st = adcgpu_write_hmlt_files(gpu_ctx, 'SCRATCH'//c_null_char, chr)
+    call adcgpu_check(st, 'write_hmlt_files')
+  end subroutine write_fspace_adc2_1_gpu
+
+!#######################################################################
+! davdiag_block (block_davidson.f90:33-145), initial space ('i') or final
+! space ('f') parameters as selected by hamflag.
+
+  subroutine davdiag_block_gpu(matdim, noffd)
+    use parameters
+    integer, intent(in)   :: matdim
+    integer*8, intent(in) :: noffd
+    type(adcgpu_dav_params) :: p
+    type(adcgpu_dav_info)   :: info
+    real(dp), allocatable   :: ev(:), vec(:,:)
+    integer(c_int)          :: st
+    if (hamflag.eq.'i') then
+       p%davstates=davstates; p%dmain=dmain; p%maxsubdim=maxsubdim; p%maxiter=maxiter
+       p%precon=precon; p%ldfl=merge(1,0,ldfl); p%lsubdiag=merge(1,0,lsubdiag)
+       p%guessdim=guessdim; p%davtol=davtol
+    else
+       p%davstates=davstates_f; p%dmain=dmain_f; p%maxsubdim=maxsubdim_f; p%maxiter=maxiter_f
+       p%precon=precon_f; p%ldfl=merge(1,0,ldfl_f); p%lsubdiag=merge(1,0,lsubdiag_f)
+       p%guessdim=guessdim_f; p%davtol=davtol_f
+    endif
+    p%precision=0; p%refine=0; p%tol_bf16=0.0_dp; p%tol_fp32=0.0_dp
+    allocate(ev(p%davstates), vec(matdim,p%davstates))
+    st = adcgpu_davidson(gpu_ctx, p, ev, vec, info)
+    call adcgpu_check(st, 'davdiag_block')
+    if (hamflag.eq.'i') then
+       st = adcgpu_write_davidson_file(trim(davname)//c_null_char, int(matdim,c_int), p%davstates, ev, vec)
+    else
+       st = adcgpu_write_davidson_file(trim(davname_f)//c_null_char, int(matdim,c_int), p%davstates, ev, vec)
+    endif
+    call adcgpu_check(st, 'wreigenpairs')
+    deallocate(ev, vec)
+  end subroutine davdiag_block_gpu
+
+!#######################################################################
+! lancdiag_block (block_lanczos.f90:28-81) from a random start block
+! (init_vecs_random, lancguess = 7).  The pseudospectrum is returned in
+! lanc_evals (lancstates = lmain*ncycles, :1234).
+
+  subroutine lancdiag_block_gpu(dimf, noff, flag, lanc_evals)
+    use parameters
+    integer, intent(in)     :: dimf
+    integer*8, intent(in)   :: noff
+    character(1),intent(in) :: flag
+    real(dp), dimension(:), allocatable, intent(out) :: lanc_evals
+    real(dp), allocatable, target :: q0(:,:), ev(:)
+    integer(c_int) :: st
+    allocate(q0(dimf,lmain), ev(lmain*ncycles))
+    call random_number(q0)
+    st = adcgpu_block_lanczos(gpu_ctx, int(lmain,c_int), int(ncycles,c_int), int(orthotype,c_int), q0, &
+         c_null_ptr, c_loc(ev), c_null_ptr)
+    call adcgpu_check(st, 'lancdiag_block')
+    lancstates = lmain*ncycles
+    call move_alloc(ev, lanc_evals)
+    deallocate(q0)
+  end subroutine lancdiag_block_gpu
+
+!#######################################################################
+! propagate_fvec (fvecprop.f90:27-105) for autoord = 0: the zeroth-order
+! autocorrelation a(t) for t = 0, tout, ..., written by the caller.
+
+  subroutine propagate_fvec_gpu(fvec, ndimf, auto, ntimes)
+    use parameters
+    integer, intent(in)                       :: ndimf
+    real(dp), dimension(ndimf), intent(in)    :: fvec
+    complex(dp), dimension(:), intent(out)    :: auto
+    integer, intent(out)                      :: ntimes
+    integer(c_int)     :: st, nt
+    integer(c_int64_t) :: nm
+    st = adcgpu_autocorr(gpu_ctx, 1_c_int, fvec, tout, tfinal, int(kdim,c_int), autotol, auto, nt, nm)
+    call adcgpu_check(st, 'propagate_fvec')
+    ntimes = nt
+  end subroutine propagate_fvec_gpu
+
+end module adcgpu_iface

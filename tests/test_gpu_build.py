@@ -154,3 +154,26 @@ def test_hmlt_files_roundtrip(gpu, tmp_path):
     a, b = sorted_coo(h, oi, oj), sorted_coo(*g.export_coo())
     for x, y in zip(a, b):
         assert np.array_equal(x, y)
+
+
+@pytest.mark.slow
+def test_config2_full_size_golden(gpu):
+    """nocc=10, nvirt=110 (N=606,650): kept structure, diagonal and values
+    bit-identical to the oracle's committed fingerprint."""
+    import hashlib
+    import json
+    import os
+
+    from tests.conftest import ROOT
+
+    gold = json.load(open(os.path.join(ROOT, "tests", "golden", "config2.json")))
+    g, e, eri = make(gold["nocc"], gold["nvirt"], gold["seed"])
+    sha = lambda a: hashlib.sha256(np.ascontiguousarray(a).tobytes()).hexdigest()
+    assert sha(e) == gold["e_sha"] and sha(eri) == gold["eri_sha"]
+    assert g.noffd == gold["nnz"]
+    assert sha(g.get_diag()) == gold["diag_sha"]
+    h, oi, oj = g.export_coo()
+    assert [str(x) for x in oracle.structure_hash(oi, oj)] == gold["structure_hash"]
+    k = np.lexsort((oj, oi))
+    assert sha(h[k]) == gold["values_sorted_sha"]
+    g.close()

@@ -113,3 +113,21 @@ def test_silstep_single(cfg1):
     exact = V @ (np.exp(-1j * w * step) * (V.T @ psi))
     assert np.abs(p2 - exact).max() < 1e-8
     assert stt.old_order == order
+
+
+@pytest.mark.slow
+def test_davidson_config2_golden(gpu):
+    """nocc=10, nvirt=110, 10 roots, tol 1e-8, DPR: eigenvalues within 1e-8 Ha
+    of the oracle's reference-algorithm run (tests/golden/config2.json)."""
+    import json
+    import os
+
+    from tests.conftest import ROOT
+
+    gold = json.load(open(os.path.join(ROOT, "tests", "golden", "config2.json")))
+    g, e, eri = make(gold["nocc"], gold["nvirt"], gold["seed"])
+    dv = gold["davidson"]
+    res = g.davdiag_block(dv["nstates"], dv["tol"], precon=dv["precon"], want_vectors=False)
+    assert res.status == 0
+    assert np.abs(res.evals - np.array(dv["evals"])).max() < 1e-8
+    g.close()
