@@ -142,7 +142,7 @@ struct DavidsonGPU {
 
   // S(p x q) = A^T B into d_small; copied to host h (p x q col-major).
   int tn_to_host(int p, int q, const T* A, const T* B, std::vector<double>& h) {
-    ST((gemm_tn<T, T, double>(c, ws, N, p, q, A, N, B, N, d_small, p, 1.0, 0.0)));
+    ST((gemm_tn<T, double, double>(c, ws, N, p, q, A, N, B, N, d_small, p, 1.0, 0.0)));
     h.resize((size_t)p * q);
     ADC_CUDA(c, cudaMemcpyAsync(h.data(), d_small, sizeof(double) * p * q, cudaMemcpyDeviceToHost, c->stream));
     ADC_CUDA(c, cudaStreamSynchronize(c->stream));
@@ -152,7 +152,7 @@ struct DavidsonGPU {
   // Tcols -= Q (Q^T Tcols), Q = ncq columns at Qb, nt columns at Tb.
   int project_out(const T* Qb, int ncq, T* Tb, int nt) {
     if (ncq <= 0 || nt <= 0) return ADCGPU_OK;
-    ST((gemm_tn<T, T, double>(c, ws, N, ncq, nt, Qb, N, Tb, N, d_small, ncq, 1.0, 0.0)));
+    ST((gemm_tn<T, double, double>(c, ws, N, ncq, nt, Qb, N, Tb, N, d_small, ncq, 1.0, 0.0)));
     ST((gemm_nn<T, double>(c, N, ncq, nt, T(-1), Qb, N, d_small, ncq, T(1), Tb, N)));
     return ADCGPU_OK;
   }

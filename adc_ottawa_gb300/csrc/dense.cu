@@ -33,6 +33,9 @@ __global__ void __launch_bounds__(256) k_gemm_tn_part(int64_t N, int p, int q, c
   const int tid = threadIdx.x;
   // thread -> 8 outputs: rows i = (tid % 16) + 16*u (u<4), cols j = (tid / 16) + 16*v (v<2)
   const int ti = tid & 15, tj = tid >> 4;
+  // Products are accumulated in T over one 32-row step and the step sums in
+  // TA (FP64 for FP32 inputs: one FP64 add per 32 FP32 FMAs keeps the
+  // Rayleigh and Gram matrices accurate to ~1e-7 over millions of rows).
   TA acc[4][2];
 #pragma unroll
   for (int u = 0; u < 4; ++u) { acc[u][0] = TA(0); acc[u][1] = TA(0); }
@@ -51,16 +54,21 @@ __global__ void __launch_bounds__(256) k_gemm_tn_part(int64_t N, int p, int q, c
       sB[rr][c] = (r < r_end && q0 + c < q) ? B[(int64_t)(q0 + c) * ldb + r] : T(0);
     }
     __syncthreads();
+    T st[4][2];
+#pragma unroll
+    for (int u = 0; u < 4; ++u) { st[u][0] = T(0); st[u][1] = T(0); }
 #pragma unroll 4
     for (int rr = 0; rr < TN_ROWS; ++rr) {
-      TA b0 = (TA)sB[rr][tj], b1 = (TA)sB[rr][tj + 16];
+      T b0 = sB[rr][tj], b1 = sB[rr][tj + 16];
 #pragma unroll
       for (int u = 0; u < 4; ++u) {
-        TA a = (TA)sA[rr][ti + 16 * u];
-        acc[u][0] += a * b0;
-        acc[u][1] += a * b1;
+        T a = sA[rr][ti + 16 * u];
+        st[u][0] += a * b0;
+        st[u][1] += a * b1;
       }
     }
+#pragma unroll
+    for (int u = 0; u < 4; ++u) { acc[u][0] += (TA)st[u][0]; acc[u][1] += (TA)st[u][1]; }
   }
   TA* out = part + ((int64_t)blockIdx.x * gridDim.y + tile) * (TN_P * TN_Q);
 #pragma unroll
