@@ -84,6 +84,8 @@ SIGNATURES = {
     "adcgpu_last_sigma_ms": (C.c_double, [_vp]),
     "adcgpu_device_bytes": (C.c_int64, [_vp]),
     "adcgpu_sigma_stats": (C.c_int, [_vp, _dp, C.c_int]),
+    "adcgpu_sigma_autotune": (C.c_int, [_vp, C.c_int, C.POINTER(C.c_int), C.POINTER(C.c_int), _dp]),
+    "adcgpu_sigma_set_shape": (C.c_int, [_vp, C.c_int, C.c_int, C.c_int]),
 }
 
 _lib = None

@@ -261,8 +261,11 @@ struct SigmaPlan {
   int2* d_chunks = nullptr;   // pass 1: [row_begin, row_end) inside one slab
   int2* d_items = nullptr;    // pass 2: (first row of slab, b')
   int nchunks = 0, nitems = 0;
+  int chunk = 64;             // rows per pass-1 work item (autotuned)
+  int mc_cap[2] = {2, 4};     // columns per pass for FP64 / FP32 vectors (autotuned)
 };
 int prepare_desc(Ctx* c);
+int build_chunks(Ctx* c, int chunk);
 void free_sigma_plan(Ctx* c);
 int sigma_fp64(Ctx* c, int m, const double* dV, int64_t ldv, double* dW, int64_t ldw);
 int sigma_fp32(Ctx* c, int m, const float* dV, int64_t ldv, float* dW, int64_t ldw);

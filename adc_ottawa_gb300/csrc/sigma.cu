@@ -81,43 +81,71 @@ __global__ void __launch_bounds__(256) k_sigma_p1(GeomDev g, const int2* __restr
     for (int c = 0; c < MC; ++c) { xa[c] = T(0); ya[c] = T(0); }
     const TV* rowp = Bt + g.off[cls] + (int64_t)(ch.x - g.start[cls]) * L;
     int ap = r.ap, bp = r.bp;
-    for (int row = ch.x; row < ch.y; ++row, rowp += L) {
-      if (ap != cur_ap) {
+    // software pipeline: the next row's values and V2 entries are loaded
+    // while the current row is reduced
+    T cA, cC[NTMAX], cD[NTMAX], cx2[MC];
+    int64_t cd;
+    {
+      Double rr{ap, bp, kp, lp, cls};
+      cd = row_to_d(g, rr, ch.x);
+      cA = lane < no ? (T)Acc<T, TV>::v(rowp[lane]) : T(0);
+#pragma unroll
+      for (int t = 0; t < NTMAX; ++t) {
+        const int a = lane + 32 * t;
+        cC[t] = a < nv ? (T)Acc<T, TV>::v(rowp[offC + a]) : T(0);
+        cD[t] = (a < nv && hasD) ? (T)Acc<T, TV>::v(rowp[offC + nv + a]) : T(0);
+      }
+#pragma unroll
+      for (int c = 0; c < MC; ++c) cx2[c] = V[(int64_t)c * ldv + n1 + cd];
+    }
+    for (int row = ch.x; row < ch.y; ++row) {
+      const int cur_bp_ap = ap;
+      int nap = ap, nbp = bp;
+      next_pair(nap, nbp, twoa, nv);
+      T nA = T(0), nC[NTMAX], nD[NTMAX], nx2[MC];
+      int64_t nd = 0;
+      if (row + 1 < ch.y) {
+        const TV* np = rowp + L;
+        Double rr{nap, nbp, kp, lp, cls};
+        nd = row_to_d(g, rr, row + 1);
+        nA = lane < no ? (T)Acc<T, TV>::v(np[lane]) : T(0);
+#pragma unroll
+        for (int t = 0; t < NTMAX; ++t) {
+          const int a = lane + 32 * t;
+          nC[t] = a < nv ? (T)Acc<T, TV>::v(np[offC + a]) : T(0);
+          nD[t] = (a < nv && hasD) ? (T)Acc<T, TV>::v(np[offC + nv + a]) : T(0);
+        }
+#pragma unroll
+        for (int c = 0; c < MC; ++c) nx2[c] = V[(int64_t)c * ldv + n1 + nd];
+      } else {
+#pragma unroll
+        for (int t = 0; t < NTMAX; ++t) { nC[t] = T(0); nD[t] = T(0); }
+#pragma unroll
+        for (int c = 0; c < MC; ++c) nx2[c] = T(0);
+      }
+      if (cur_bp_ap != cur_ap) {
         if (cur_ap >= 0 && lane < no) {
 #pragma unroll
           for (int c = 0; c < MC; ++c) atomicAdd(&W[(int64_t)c * ldw + (int64_t)cur_ap * no + lane], ya[c]);
         }
-        cur_ap = ap;
+        cur_ap = cur_bp_ap;
 #pragma unroll
         for (int c = 0; c < MC; ++c) {
-          xa[c] = lane < no ? V[(int64_t)c * ldv + (int64_t)ap * no + lane] : T(0);
+          xa[c] = lane < no ? V[(int64_t)c * ldv + (int64_t)cur_ap * no + lane] : T(0);
           ya[c] = T(0);
         }
       }
-      Double rr{ap, bp, kp, lp, cls};
-      const int64_t d = row_to_d(g, rr, row);
-      T x2[MC], z[MC];
-#pragma unroll
-      for (int c = 0; c < MC; ++c) { x2[c] = V[(int64_t)c * ldv + n1 + d]; z[c] = T(0); }
-      // issue the row's loads first
-      T vA = lane < no ? (T)Acc<T, TV>::v(rowp[lane]) : T(0);
-      T vC[NTMAX], vD[NTMAX];
-#pragma unroll
-      for (int t = 0; t < NTMAX; ++t) {
-        const int a = lane + 32 * t;
-        vC[t] = a < nv ? (T)Acc<T, TV>::v(rowp[offC + a]) : T(0);
-        vD[t] = (a < nv && hasD) ? (T)Acc<T, TV>::v(rowp[offC + nv + a]) : T(0);
-      }
+      T z[MC];
 #pragma unroll
       for (int c = 0; c < MC; ++c) {
-        ya[c] += vA * x2[c];
-        z[c] += vA * xa[c];
+        ya[c] += cA * cx2[c];
+        z[c] = cA * xa[c];
 #pragma unroll
         for (int t = 0; t < NTMAX; ++t) {
-          yk[t][c] += vC[t] * x2[c];
-          z[c] += vC[t] * xk[t][c];
-          yl[t][c] += vD[t] * x2[c];
-          z[c] += vD[t] * xl[t][c];
+          yk[t][c] += cC[t] * cx2[c];
+          z[c] += cC[t] * xk[t][c];
+          yl[t][c] += cD[t] * cx2[c];
+          z[c] += cD[t] * xl[t][c];
         }
       }
 #pragma unroll
@@ -125,9 +153,13 @@ __global__ void __launch_bounds__(256) k_sigma_p1(GeomDev g, const int2* __restr
         T v = z[c];
 #pragma unroll
         for (int o = 16; o; o >>= 1) v += __shfl_xor_sync(0xffffffffu, v, o);
-        if (lane == 0) W[(int64_t)c * ldw + n1 + d] = diag[n1 + d] * x2[c] + v;
+        if (lane == 0) W[(int64_t)c * ldw + n1 + cd] = diag[n1 + cd] * cx2[c] + v;
       }
-      next_pair(ap, bp, twoa, nv);
+      ap = nap; bp = nbp; rowp += L; cd = nd; cA = nA;
+#pragma unroll
+      for (int t = 0; t < NTMAX; ++t) { cC[t] = nC[t]; cD[t] = nD[t]; }
+#pragma unroll
+      for (int c = 0; c < MC; ++c) cx2[c] = nx2[c];
     }
     if (lane < no) {
 #pragma unroll
@@ -171,20 +203,38 @@ __global__ void __launch_bounds__(256) k_sigma_p2(GeomDev g, const int2* __restr
       xb[c] = lane < no ? V[(int64_t)c * ldv + (int64_t)bp * no + lane] : T(0);
       yb[c] = T(0);
     }
-    for (int ap = 0; ap < bp; ++ap) {
-      const int64_t row = slab0 + pair_index(ap, bp, nv);
-      Double rr{ap, bp, r.kp, r.lp, cls};
-      const int64_t d = row_to_d(g, rr, row);
-      const TV* rowp = Bt + g.off[cls] + (row - g.start[cls]) * L;
-      T v = lane < no ? (T)Acc<T, TV>::v(rowp[no + lane]) : T(0);
+    constexpr int U = 4;   // rows in flight per warp
+    for (int ap0 = 0; ap0 < bp; ap0 += U) {
+      T v[U], x2[U][MC], w2[U][MC];
+      int64_t d[U];
 #pragma unroll
-      for (int c = 0; c < MC; ++c) {
-        const T x2 = V[(int64_t)c * ldv + n1 + d];
-        yb[c] += v * x2;
-        T z = v * xb[c];
+      for (int u = 0; u < U; ++u) {
+        const int ap = ap0 + u;
+        d[u] = -1;
+        v[u] = T(0);
+        if (ap < bp) {
+          const int64_t row = slab0 + pair_index(ap, bp, nv);
+          Double rr{ap, bp, r.kp, r.lp, cls};
+          d[u] = row_to_d(g, rr, row);
+          const TV* rowp = Bt + g.off[cls] + (row - g.start[cls]) * L;
+          v[u] = lane < no ? (T)Acc<T, TV>::v(rowp[no + lane]) : T(0);
+        }
 #pragma unroll
-        for (int o = 16; o; o >>= 1) z += __shfl_xor_sync(0xffffffffu, z, o);
-        if (lane == 0) W[(int64_t)c * ldw + n1 + d] += z;
+        for (int c = 0; c < MC; ++c) {
+          x2[u][c] = d[u] >= 0 ? V[(int64_t)c * ldv + n1 + d[u]] : T(0);
+          w2[u][c] = (d[u] >= 0 && lane == 0) ? W[(int64_t)c * ldw + n1 + d[u]] : T(0);
+        }
+      }
+#pragma unroll
+      for (int u = 0; u < U; ++u) {
+#pragma unroll
+        for (int c = 0; c < MC; ++c) {
+          yb[c] += v[u] * x2[u][c];
+          T z = v[u] * xb[c];
+#pragma unroll
+          for (int o = 16; o; o >>= 1) z += __shfl_xor_sync(0xffffffffu, z, o);
+          if (lane == 0 && d[u] >= 0) W[(int64_t)c * ldw + n1 + d[u]] = w2[u][c] + z;
+        }
       }
     }
     if (lane < no) {
@@ -262,7 +312,9 @@ int sigma_impl(Ctx* c, int m, const T* dV, int64_t ldv, T* dW, int64_t ldw, cons
     const int left = m - c0;
     const T* V = dV + (int64_t)c0 * ldv;
     T* W = dW + (int64_t)c0 * ldw;
-    const int mc = (sizeof(T) == 8 || G.nv > 192) ? (left >= 2 ? 2 : 1) : (left >= 4 ? 4 : (left >= 2 ? 2 : 1));
+    int cap = plan->mc_cap[sizeof(T) == 8 ? 0 : 1];
+    if (sizeof(T) == 8 || G.nv > 192) cap = std::min(cap, 2);
+    const int mc = (left >= 4 && cap >= 4) ? 4 : ((left >= 2 && cap >= 2) ? 2 : 1);
     const int g1 = std::min(plan->nchunks, 152 * 8 * 8) / 8 + 1;
     const int g2 = std::min(plan->nitems, 152 * 8 * 8) / 8 + 1;
 #define LAUNCH(MC, NT)                                                                                  \
@@ -299,16 +351,17 @@ __global__ void k_to_bf16(const double* __restrict__ x, __nv_bfloat16* __restric
 
 }  // namespace
 
-// Work lists of the sigma kernels: pass-1 chunks (row ranges inside one
-// slab) and pass-2 items (slab, b') of the classes with a' < b'.
-int prepare_desc(Ctx* c) {
+// Work lists of the sigma kernels: pass-1 chunks (row ranges of at most
+// 'chunk' rows inside one slab) and pass-2 items (slab, b') of the classes
+// with a' < b'.
+int build_chunks(Ctx* c, int chunk) {
   const Geometry& G = c->geom;
   std::vector<int2> chunks, items;
-  const int64_t CH = 64;
   for (int cls = 0; cls < 5; ++cls) {
     const int64_t r0 = G.start[cls], r1 = G.start[cls + 1], sl = G.slab_len(cls);
     for (int64_t s0 = r0; s0 < r1; s0 += sl) {
-      for (int64_t a = s0; a < s0 + sl; a += CH) chunks.push_back(make_int2((int)a, (int)std::min(a + CH, s0 + sl)));
+      for (int64_t a = s0; a < s0 + sl; a += chunk)
+        chunks.push_back(make_int2((int)a, (int)std::min<int64_t>(a + chunk, s0 + sl)));
       if (cls == 1 || cls >= 3)
         for (int bp = 1; bp < G.nv; ++bp) items.push_back(make_int2((int)s0, bp));
     }
@@ -326,7 +379,13 @@ int prepare_desc(Ctx* c) {
     ADC_CUDA(c, cudaMemcpy(plan->d_items, items.data(), sizeof(int2) * items.size(), cudaMemcpyHostToDevice));
   plan->nchunks = (int)chunks.size();
   plan->nitems = (int)items.size();
+  plan->chunk = chunk;
   return ADCGPU_OK;
+}
+
+int prepare_desc(Ctx* c) {
+  SigmaPlan* plan = reinterpret_cast<SigmaPlan*>(c->sigma_plan);
+  return build_chunks(c, plan ? plan->chunk : 64);
 }
 
 void free_sigma_plan(Ctx* c) {
@@ -361,6 +420,70 @@ extern "C" int adcgpu_sigma_stats(adcgpu_ctx* h, double* out, int reset) {
   out[0] = (double)c->st_calls; out[1] = c->st_ms; out[2] = c->st_bytes; out[3] = (double)c->st_cols;
   if (reset) { c->st_calls = 0; c->st_cols = 0; c->st_ms = 0.0; c->st_bytes = 0.0; }
   return ADCGPU_OK;
+}
+
+// Autotuner: times the sigma product for m columns over the launch shapes
+// (pass-1 chunk rows x columns per pass) with CUDA events on the context's
+// stream and keeps the fastest.  Results are cached by the caller.
+extern "C" int adcgpu_sigma_autotune(adcgpu_ctx* h, int m, int* best_chunk, int* best_mc, double* best_ms) {
+  Ctx* c = reinterpret_cast<Ctx*>(h);
+  if (!c || m <= 0) return ADCGPU_BAD_INPUT;
+  cudaSetDevice(c->device);
+  if (!c->have_matrix) return set_err(c, ADCGPU_NO_MATRIX, "build the matrix first");
+  SigmaPlan* plan = reinterpret_cast<SigmaPlan*>(c->sigma_plan);
+  const int64_t N = c->geom.N;
+  const bool mixed = c->precision == ADCGPU_MIXED;
+  const size_t esz = mixed ? sizeof(float) : sizeof(double);
+  void *dv = nullptr, *dw = nullptr;
+  int st;
+  if ((st = dmalloc(c, &dv, esz * N * m))) return st;
+  if ((st = dmalloc(c, &dw, esz * N * m))) { dfree(c, dv, 0); return st; }
+  ADC_CUDA(c, cudaMemsetAsync(dv, 0, esz * N * m, c->stream));
+  const int chunks[] = {16, 32, 64, 128, 256};
+  const int mcs[] = {1, 2, 4};
+  double best = 1e30;
+  int bc = plan->chunk, bm = plan->mc_cap[mixed ? 1 : 0];
+  for (int ch : chunks) {
+    if ((st = build_chunks(c, ch))) break;
+    for (int mc : mcs) {
+      if (!mixed && mc > 2) continue;
+      plan->mc_cap[mixed ? 1 : 0] = mc;
+      double t = 1e30;
+      for (int rep = 0; rep < 3; ++rep) {
+        cudaEventRecord(c->ev0, c->stream);
+        st = mixed ? sigma_fp32(c, m, (const float*)dv, N, (float*)dw, N)
+                   : sigma_fp64(c, m, (const double*)dv, N, (double*)dw, N);
+        cudaEventRecord(c->ev1, c->stream);
+        cudaEventSynchronize(c->ev1);
+        float ms = 0.f;
+        cudaEventElapsedTime(&ms, c->ev0, c->ev1);
+        if (rep > 0) t = std::min(t, (double)ms);
+      }
+      if (t < best) { best = t; bc = ch; bm = mc; }
+    }
+  }
+  sigma_stats_flush(c);
+  c->st_calls = 0; c->st_cols = 0; c->st_ms = 0.0; c->st_bytes = 0.0;
+  plan->mc_cap[mixed ? 1 : 0] = bm;
+  if (!st) st = build_chunks(c, bc);
+  dfree(c, dv, 0);
+  dfree(c, dw, 0);
+  if (best_chunk) *best_chunk = bc;
+  if (best_mc) *best_mc = bm;
+  if (best_ms) *best_ms = best;
+  return st;
+}
+
+// Applies a cached tuning result.
+extern "C" int adcgpu_sigma_set_shape(adcgpu_ctx* h, int chunk, int mc_fp64, int mc_fp32) {
+  Ctx* c = reinterpret_cast<Ctx*>(h);
+  if (!c || chunk < 1 || mc_fp64 < 1 || mc_fp32 < 1) return ADCGPU_BAD_INPUT;
+  cudaSetDevice(c->device);
+  if (!c->have_matrix) return set_err(c, ADCGPU_NO_MATRIX, "build the matrix first");
+  SigmaPlan* plan = reinterpret_cast<SigmaPlan*>(c->sigma_plan);
+  plan->mc_cap[0] = std::min(mc_fp64, 2);
+  plan->mc_cap[1] = std::min(mc_fp32, 4);
+  return build_chunks(c, chunk);
 }
 
 int sigma_fp64(Ctx* c, int m, const double* dV, int64_t ldv, double* dW, int64_t ldw) {

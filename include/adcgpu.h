@@ -263,6 +263,15 @@ int64_t adcgpu_device_bytes(const adcgpu_ctx* ctx);
    reset != 0 clears the counters after reading. */
 int adcgpu_sigma_stats(adcgpu_ctx* ctx, double* out4, int reset);
 
+/* Autotuner of the sigma kernels' launch shape: pass-1 rows per warp work
+   item (16..256) and vector columns per pass (1, 2, 4), timed with CUDA
+   events for m columns on the built matrix; the fastest shape is kept in the
+   context and returned (the Python layer caches it in a JSON file). */
+int adcgpu_sigma_autotune(adcgpu_ctx* ctx, int m, int* best_chunk, int* best_mc, double* best_ms);
+
+/* Applies a launch shape (e.g. from the autotuner's cache). */
+int adcgpu_sigma_set_shape(adcgpu_ctx* ctx, int chunk, int mc_fp64, int mc_fp32);
+
 #ifdef __cplusplus
 }
 #endif

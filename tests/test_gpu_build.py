@@ -177,3 +177,30 @@ def test_config2_full_size_golden(gpu):
     k = np.lexsort((oj, oi))
     assert sha(h[k]) == gold["values_sorted_sha"]
     g.close()
+
+
+@pytest.mark.parametrize("prec", [0, 1])
+def test_sigma_launch_shapes_agree(gpu, prec, tmp_path):
+    """Every launch shape the autotuner may pick gives the same product, and
+    the tuned shape is cached and re-applied."""
+    import ctypes as C
+
+    from adc_ottawa_gb300 import autotune
+    from adc_ottawa_gb300._native import lib
+
+    g, e, eri = make(6, 30, 11, precision=prec)
+    x = np.random.RandomState(3).standard_normal((g.ndim, 5))
+    ref = g.sigma(x)
+    tol = 1e-12 if prec == 0 else 5e-3
+    for chunk in (16, 64, 256):
+        for mc in (1, 2, 4):
+            assert lib().adcgpu_sigma_set_shape(g._h, chunk, mc, mc) == 0
+            y = g.sigma(x)
+            assert np.abs(y - ref).max() <= tol * np.abs(ref).max(), (chunk, mc)
+    cache = str(tmp_path / "tune.json")
+    r1 = autotune.tune(g, 5, prec, cache=cache)
+    r2 = autotune.tune(g, 5, prec, cache=cache)
+    assert not r1["cached"] and r2["cached"] and r1["chunk"] == r2["chunk"]
+    y = g.sigma(x)
+    assert np.abs(y - ref).max() <= tol * np.abs(ref).max()
+    g.close()
