@@ -84,6 +84,14 @@ SIGNATURES = {
     "adcgpu_last_sigma_ms": (C.c_double, [_vp]),
     "adcgpu_device_bytes": (C.c_int64, [_vp]),
     "adcgpu_sigma_stats": (C.c_int, [_vp, _dp, C.c_int]),
+    "adcgpu_mlp_num_params": (C.c_int64, []),
+    "adcgpu_mlp_set_params": (C.c_int, [_vp, C.POINTER(C.c_float), C.c_int64]),
+    "adcgpu_mlp_get_params": (C.c_int, [_vp, C.POINTER(C.c_float), C.c_int64]),
+    "adcgpu_mlp_train_step": (C.c_int, [_vp, C.c_int, C.c_int, C.POINTER(C.c_float), C.POINTER(C.c_float),
+                                        C.POINTER(C.c_float), C.c_float, C.POINTER(C.c_float), C.POINTER(C.c_float)]),
+    "adcgpu_mlp_infer": (C.c_int, [_vp, C.c_int, _dp, _dp, C.POINTER(C.c_float), _dp, C.POINTER(C.c_float)]),
+    "adcgpu_davidson_trace": (C.c_int, [_vp, C.POINTER(DavParams), C.c_int, C.c_int, _dp, _dp, _dp, _dp, _dp,
+                                        C.POINTER(C.c_int)]),
     "adcgpu_sigma_autotune": (C.c_int, [_vp, C.c_int, C.POINTER(C.c_int), C.POINTER(C.c_int), _dp]),
     "adcgpu_sigma_set_shape": (C.c_int, [_vp, C.c_int, C.c_int, C.c_int]),
 }

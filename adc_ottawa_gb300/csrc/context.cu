@@ -95,6 +95,7 @@ int adcgpu_ctx_destroy(adcgpu_ctx* h) {
   cudaStreamSynchronize(c->stream);
   free_matrix(c);
   free_eri(c);
+  free_mlp(c);
   if (c->d_e) cudaFree(c->d_e);
   if (c->d_sil) cudaFree(c->d_sil);
   cudaEventDestroy(c->ev0);

@@ -237,6 +237,10 @@ struct DavidsonGPU {
     return ADCGPU_OK;
   }
 
+  // optional trace of (residual, Ritz vector, Ritz value) of the first
+  // nstates roots every trace_every iterations (training data of the MLP)
+  double *tr_R = nullptr, *tr_X = nullptr, *tr_lam = nullptr;
+  int tr_every = 0, tr_max = 0, tr_n = 0;
   int64_t nmult_ref = 0;       // sum of currdim over iterations (reference hxvec columns)
   double max_res = 0.0;        // largest residual norm among the returned roots
   std::vector<double> Cnorm;   // residual norms of the deflated roots
@@ -282,6 +286,14 @@ struct DavidsonGPU {
       std::vector<double> n2(bs_curr);
       ST(residuals<T>(c, ws, N, bs_curr, X, WY, N, d_lam, R, n2.data()));
       for (int i = 0; i < bs_curr; ++i) norm[i] = std::sqrt(n2[i]);
+      if (tr_every > 0 && (k - 1) % tr_every == 0 && tr_n < tr_max && nstates_curr == nstates) {
+        const size_t blk = sizeof(T) * (size_t)N * nstates;
+        ADC_CUDA(c, cudaMemcpyAsync(tr_R + (size_t)tr_n * N * nstates, R, blk, cudaMemcpyDeviceToHost, c->stream));
+        ADC_CUDA(c, cudaMemcpyAsync(tr_X + (size_t)tr_n * N * nstates, X, blk, cudaMemcpyDeviceToHost, c->stream));
+        for (int i = 0; i < nstates; ++i) tr_lam[(size_t)tr_n * nstates + i] = lam[i];
+        ADC_CUDA(c, cudaStreamSynchronize(c->stream));
+        ++tr_n;
+      }
       if (!ldeflate) nconv = 0;
       for (int i = 0; i < nstates_curr; ++i)
         if (norm[i] < tol) ++nconv;
@@ -329,8 +341,9 @@ struct DavidsonGPU {
       T* Tb = col(V, ilast);
       if (ipre == ADCGPU_PRECON_OLSEN) {
         ST((precond_olsen<T, T>(c, ws, N, bs_curr, X, R, N, d_lam, hii, Tb, N, nullptr)));
-      } else if (ipre == ADCGPU_PRECON_MLP && mlp) {
-        ST(mlp_apply(c, *mlp, N, bs_curr, R, X, d_lam, hii, Tb));
+      } else if (ipre == ADCGPU_PRECON_MLP && c->mlp) {
+        MlpPrecond none;
+        ST(mlp_apply(c, mlp ? *mlp : none, N, bs_curr, R, X, d_lam, hii, Tb));
       } else {
         ST((precond_dpr<T, T>(c, N, bs_curr, R, N, d_lam, hii, Tb, N)));
       }
@@ -489,7 +502,7 @@ int davidson_solve(Ctx* c, const adcgpu_dav_params* p, double* evals, double* ev
   std::vector<double> hdiag(N);
   ADC_CUDA(c, cudaMemcpy(hdiag.data(), c->d_diag, sizeof(double) * N, cudaMemcpyDeviceToHost));
   const int guess_kind = p->lsubdiag ? 1 : 0;
-  const int precon64 = p->precon == ADCGPU_PRECON_MLP ? ADCGPU_PRECON_DPR : p->precon;
+  const int precon64 = p->precon;
   int st = ADCGPU_OK;
   adcgpu_dav_info inf{};
   std::vector<double> ev;
@@ -566,6 +579,41 @@ extern "C" int adcgpu_davidson(adcgpu_ctx* h, const adcgpu_dav_params* p, double
   cudaSetDevice(c->device);
   if (!c->have_matrix) return set_err(c, ADCGPU_NO_MATRIX, "build the matrix first");
   return davidson_solve(c, p, evals, evecs, info, nullptr);
+}
+
+extern "C" int adcgpu_davidson_trace(adcgpu_ctx* h, const adcgpu_dav_params* p, int every, int max_records,
+                                     double* R_out, double* X_out, double* lam_out, double* evals, double* evecs,
+                                     int* nrec) {
+  using namespace adcgpu;
+  Ctx* c = reinterpret_cast<Ctx*>(h);
+  if (!c || !p || every <= 0 || max_records <= 0 || !R_out || !X_out || !lam_out || !evals || !evecs)
+    return ADCGPU_BAD_INPUT;
+  cudaSetDevice(c->device);
+  if (!c->have_matrix) return set_err(c, ADCGPU_NO_MATRIX, "build the matrix first");
+  const int64_t N = c->geom.N;
+  const int nstates = p->davstates;
+  int blocksize = p->dmain > 0 ? p->dmain : std::max(nstates + 5, 2 * nstates);
+  int maxvec = p->maxsubdim >= 0 ? p->maxsubdim : 4 * blocksize;
+  maxvec = (maxvec / blocksize) * blocksize;
+  std::vector<double> hdiag(N), ev;
+  ADC_CUDA(c, cudaMemcpy(hdiag.data(), c->d_diag, sizeof(double) * N, cudaMemcpyDeviceToHost));
+  DavidsonGPU<double> D;
+  D.c = c; D.N = N; D.nstates = nstates; D.blocksize = blocksize; D.maxvec = maxvec;
+  D.niter = p->maxiter; D.ipre = p->precon; D.ldeflate = false; D.tol = p->davtol; D.hii = c->d_diag;
+  D.tr_R = R_out; D.tr_X = X_out; D.tr_lam = lam_out; D.tr_every = every; D.tr_max = max_records;
+  double* out = nullptr;
+  int st = dmalloc(c, (void**)&out, sizeof(double) * (size_t)N * blocksize);
+  if (st) return st;
+  int it = 0, nc = 0, nout = 0;
+  st = D.run(hdiag, p->lsubdiag ? 1 : 0, p->guessdim, nullptr, 0, ev, out, blocksize, &nout, &it, &nc);
+  if (st == ADCGPU_OK || st == ADCGPU_NOT_CONVERGED) {
+    cudaMemcpy(evecs, out, sizeof(double) * (size_t)N * nstates, cudaMemcpyDeviceToHost);
+    for (int i = 0; i < nstates; ++i) evals[i] = ev[i];
+  }
+  if (nrec) *nrec = D.tr_n;
+  D.release();
+  dfree(c, out, 0);
+  return st;
 }
 
 extern "C" int adcgpu_write_davidson_file(const char* path, int ndim, int nstates, const double* evals,

@@ -95,11 +95,16 @@ __host__ __device__ inline int64_t pair_index(int x, int y, int n) {
 }
 
 __host__ __device__ inline void pair_decode(int64_t p, int n, int& x, int& y) {
-  // invert pair_index by walking rows; n is small (<= a few hundred)
-  int xx = 0;
-  int64_t rowlen = n - 1;
-  while (p >= rowlen) { p -= rowlen; ++xx; --rowlen; }
-  x = xx; y = xx + 1 + (int)p;
+  // invert pair_index: estimate the row from the quadratic, then correct
+  const double b = 2.0 * n - 1.0;
+  double disc = b * b - 8.0 * (double)p;
+  int xx = (int)((b - sqrt(disc > 0.0 ? disc : 0.0)) * 0.5);
+  if (xx < 0) xx = 0;
+  if (xx > n - 2) xx = n - 2;
+  while (xx > 0 && pair_index(xx, xx + 1, n) > p) --xx;
+  while (xx < n - 2 && pair_index(xx + 1, xx + 2, n) <= p) ++xx;
+  x = xx;
+  y = (int)(p - pair_index(xx, xx + 1, n)) + xx + 1;
 }
 
 struct GeomDev {
@@ -228,6 +233,8 @@ struct Ctx {
   double st_pending_bytes = 0.0;
   int st_pending_cols = 0;
   int64_t dev_bytes = 0;
+  // learned preconditioner (MlpState, mlp.cu); DPR is used when absent
+  void* mlp = nullptr;
   // SIL persistent state for adcgpu_silstep (device Krylov vectors)
   double* d_sil = nullptr;
   int64_t sil_cap = 0;
@@ -270,6 +277,7 @@ void free_sigma_plan(Ctx* c);
 int sigma_fp64(Ctx* c, int m, const double* dV, int64_t ldv, double* dW, int64_t ldw);
 int sigma_fp32(Ctx* c, int m, const float* dV, int64_t ldv, float* dW, int64_t ldw);
 int prepare_mixed(Ctx* c);
+void free_mlp(Ctx* c);
 
 // hostla.cpp : dense host linear algebra (FP64)
 // Symmetric eigen-decomposition (Householder tridiagonalisation + implicit QL).

@@ -178,6 +178,10 @@ def run_gb300(args):
     nnz = g.write_fspace_adc2_1(None, precision=ADCGPU_MIXED)
     build_s = time.perf_counter() - t0
     prec = ADCGPU_MIXED
+    from adc_ottawa_gb300 import autotune
+
+    blocksize = max(NROOTS + 5, 2 * NROOTS)
+    tuned = autotune.tune(g, blocksize, prec)
     kw = dict(precon=PRECON_DPR, precision=prec, want_vectors=True, raise_on_nonconv=False)
     for _ in range(args.warmup):
         r = g.davdiag_block(NROOTS, TOL, **kw)
@@ -227,7 +231,7 @@ def run_gb300(args):
     cpu = None
     if rank == 0 and world == 1 and not args.no_cpu:
         nthr = os.cpu_count() or 1
-        nmult_ref = getattr(r, "nmult_reference", 0) or r.nmult * 4
+        nmult_ref = r.nmult_reference
         cpu = cpu_sample(no, nv, SEED, e, eri, nmult_ref, g.ndim, nnz, nthr)
     line = {
         "metric": "time-to-converge 20 roots at 1e-6 (mixed precision + FP64 refinement)",
@@ -244,6 +248,8 @@ def run_gb300(args):
         "data": "synthetic (seeded orbital energies and 8-fold symmetric ERIs)",
         "config": {"workload": f"ADC(2)-s nocc={no} nvirt={nv} N={g.ndim} davidson {NROOTS} roots tol {TOL}",
                    "nnz_kept": nnz, "build_s": build_s, "iterations": r.iterations, "nmult": r.nmult,
+                   "phase_iterations_bf16_fp32_fp64": [r.iters_bf16, r.iters_fp32, r.iters_fp64],
+                   "max_residual_fp64": r.max_residual, "sigma_shape": tuned,
                    "status": r.status, "evals_lowest": r.evals[:5].tolist(),
                    "l2": "inputs larger than L2 (stored matrix > 3 GB)", "parallelism": f"replicas x{world}",
                    "fp64_gpu": fp64,

@@ -247,6 +247,39 @@ int adcgpu_autocorr(adcgpu_ctx* ctx, int nwp, const double* f, double tout,
                     int* ntimes_out, int64_t* nmult_out);
 
 /* ---------------------------------------------------------------------------
+ * Learned preconditioner (ADCGPU_PRECON_MLP).  No counterpart routine in the
+ * reference: it replaces the diagonal preconditioner of dpr
+ * (block_davidson.f90:1288-1342) by t = m * r / (lambda - h), m = MLP(features),
+ * and falls back to dpr when no network is loaded.  The parameter vector is
+ * W1[256][16], b1[256], W2[256][256], b2[256], w3[256], b3 (FP32).
+ * ------------------------------------------------------------------------- */
+int64_t adcgpu_mlp_num_params(void);
+int adcgpu_mlp_set_params(adcgpu_ctx* ctx, const float* params, int64_t n);
+int adcgpu_mlp_get_params(adcgpu_ctx* ctx, float* params, int64_t n);
+
+/* One Adam step (lr > 0) or a gradient evaluation only (lr == 0) on G groups
+   of S rows: features (G*S x 16), t0 = r / (lambda - h) and the target
+   correction, from host arrays.  Loss = mean over groups of
+   1 - cos^2(m * t0, target).  grad_out (may be NULL): the summed gradient. */
+int adcgpu_mlp_train_step(adcgpu_ctx* ctx, int G, int S, const float* feats, const float* t0,
+                          const float* target, float lr, float* loss_out, float* grad_out);
+
+/* Fused inference on the built matrix for nb roots: m_out and t_out
+   (N*nb, row q = i*N + j) for residuals R (N x nb, may be NULL) and Ritz
+   values lam; feats_out (N*nb x 16, may be NULL) the features used. */
+int adcgpu_mlp_infer(adcgpu_ctx* ctx, int nb, const double* lam, const double* R, float* m_out,
+                     double* t_out, float* feats_out);
+
+/* Davidson trace for training data: runs the FP64 Davidson of p and stores,
+   every 'every' iterations, the residuals and Ritz vectors of the first
+   davstates roots (N x davstates each) and their Ritz values, up to
+   max_records iterations; converged eigenvectors go to evecs.
+   *nrec receives the number of stored iterations. */
+int adcgpu_davidson_trace(adcgpu_ctx* ctx, const adcgpu_dav_params* p, int every, int max_records,
+                          double* R_out, double* X_out, double* lam_out, double* evals, double* evecs,
+                          int* nrec);
+
+/* ---------------------------------------------------------------------------
  * Timing helpers for benchmarks: device milliseconds of the last sigma
  * call as measured by CUDA events on the context's stream.
  * ------------------------------------------------------------------------- */

@@ -1,0 +1,99 @@
+"""Learned preconditioner: hand-written BF16 kernels checked against the CPU
+oracle (oracle/mlp_ref.py), and the trained network against the diagonal
+preconditioner it replaces."""
+import numpy as np
+import pytest
+
+from oracle import mlp_ref
+from tests.conftest import system
+from tests.test_gpu_build import make
+
+pytestmark = pytest.mark.gpu
+
+
+def random_params(seed):
+    from adc_ottawa_gb300 import mlp_train
+
+    p = mlp_train.init_params(seed).astype(np.float64)
+    rs = np.random.RandomState(seed + 1)
+    W1, b1, W2, b2, w3, b3 = mlp_train.unpack(p)
+    w3[:] = rs.standard_normal(256) * 0.05
+    b1[:] = rs.standard_normal(256) * 0.1
+    b2[:] = rs.standard_normal(256) * 0.1
+    return p.astype(np.float32)
+
+
+def test_features_and_identity_init(gpu):
+    """Device features equal the numpy features; the initial network (w3 = 0,
+    b3 = 1) reproduces the diagonal preconditioner exactly."""
+    from adc_ottawa_gb300 import mlp_train
+    from adc_ottawa_gb300._native import lib
+    import ctypes as C
+
+    no, nv = 4, 9
+    g, e, eri = make(no, nv, 7)
+    mlp_train.load_into(g, mlp_train.init_params(0))
+    h = g.get_diag()
+    lam = np.array([0.7, -0.2])
+    R = np.random.RandomState(2).standard_normal((g.ndim, 2))
+    m = np.empty(g.ndim * 2, np.float32)
+    t = np.empty(g.ndim * 2)
+    F = np.empty((g.ndim * 2, 16), np.float32)
+    st = lib().adcgpu_mlp_infer(g._h, 2, lam.ctypes.data_as(C.POINTER(C.c_double)),
+                                np.asfortranarray(R).ctypes.data_as(C.POINTER(C.c_double)),
+                                m.ctypes.data_as(C.POINTER(C.c_float)), t.ctypes.data_as(C.POINTER(C.c_double)),
+                                F.ctypes.data_as(C.POINTER(C.c_float)))
+    assert st == 0
+    d0, cls = mlp_train.config_info(no, nv, e)
+    for i in range(2):
+        Fn = mlp_train.features(lam[i], h, d0, cls)
+        assert np.abs(F[i * g.ndim:(i + 1) * g.ndim] - Fn).max() < 1e-5
+        dpr = R[:, i] / (lam[i] - h)
+        assert np.all(m[i * g.ndim:(i + 1) * g.ndim] == 1.0)
+        assert np.abs(t[i * g.ndim:(i + 1) * g.ndim] - dpr).max() <= 1e-6 * np.abs(dpr).max()
+    g.close()
+
+
+def test_fused_inference_matches_oracle(gpu):
+    from adc_ottawa_gb300 import mlp_train
+    from adc_ottawa_gb300._native import lib
+    import ctypes as C
+
+    no, nv = 4, 9
+    g, e, eri = make(no, nv, 7)
+    p = random_params(3)
+    mlp_train.load_into(g, p)
+    lam = np.array([0.4])
+    m = np.empty(g.ndim, np.float32)
+    F = np.empty((g.ndim, 16), np.float32)
+    assert lib().adcgpu_mlp_infer(g._h, 1, lam.ctypes.data_as(C.POINTER(C.c_double)), None,
+                                  m.ctypes.data_as(C.POINTER(C.c_float)), None,
+                                  F.ctypes.data_as(C.POINTER(C.c_float))) == 0
+    ref = mlp_ref.forward_m(p, F)
+    assert np.abs(m - ref).max() <= 2e-2 * max(1.0, np.abs(ref).max())
+    assert np.corrcoef(m, ref)[0, 1] > 0.999
+    g.close()
+
+
+def test_gradient_check_against_oracle(gpu):
+    from adc_ottawa_gb300 import mlp_train
+
+    G, S = 6, 512
+    rs = np.random.RandomState(11)
+    F = np.zeros((G * S, 16), np.float32)
+    F[:, :11] = rs.standard_normal((G * S, 11)).astype(np.float32)
+    t0 = rs.standard_normal(G * S).astype(np.float32)
+    e = (t0 * (1 + 0.3 * rs.standard_normal(G * S))).astype(np.float32)
+    p = random_params(5)
+    grad, loss = mlp_train.gradient(p, F, t0, e, G, S)
+    lref, gref = mlp_ref.loss_and_grad(p, F, t0, e, G, S)
+    assert abs(loss - lref) <= 1e-3 * max(1e-3, abs(lref)) + 1e-5
+    cos = grad @ gref / (np.linalg.norm(grad) * np.linalg.norm(gref))
+    assert cos > 0.999, cos
+    assert np.linalg.norm(grad - gref) <= 3e-2 * np.linalg.norm(gref)
+    # per block: every parameter group has a matching gradient
+    off = 0
+    for n in (256 * 16, 256, 256 * 256, 256, 256, 1):
+        a, b = grad[off:off + n], gref[off:off + n]
+        assert np.linalg.norm(a - b) <= 5e-2 * np.linalg.norm(b) + 1e-7
+        off += n
