@@ -243,9 +243,10 @@ int Workspace::reserve(Ctx* c, size_t need) {
   return ADCGPU_OK;
 }
 
+// Row blocks of the TN reduction: at least 4 blocks per SM on large N.
 static int tn_blocks(int64_t N) {
-  int64_t b = (N + 4095) / 4096;
-  return (int)std::max<int64_t>(1, std::min<int64_t>(b, 152 * 2));
+  int64_t b = (N + 1023) / 1024;
+  return (int)std::max<int64_t>(1, std::min<int64_t>(b, 152 * 4));
 }
 
 template <typename T, typename TA, typename TC>
@@ -254,7 +255,7 @@ int gemm_tn(Ctx* c, Workspace& ws, int64_t N, int p, int q, const T* A, int64_t 
   if (p <= 0 || q <= 0) return ADCGPU_OK;
   const int ntile = ((p + TN_P - 1) / TN_P) * ((q + TN_Q - 1) / TN_Q);
   const int nblk = tn_blocks(N);
-  const int64_t rows = (N + nblk - 1) / nblk;
+  const int64_t rows = ((N + nblk - 1) / nblk + TN_ROWS - 1) / TN_ROWS * TN_ROWS;
   size_t need = sizeof(TA) * (size_t)nblk * ntile * TN_P * TN_Q;
   int st = ws.reserve(c, need);
   if (st) return st;

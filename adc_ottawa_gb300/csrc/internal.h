@@ -17,13 +17,17 @@
 //
 //   segment A : singles (a',k), k = 0..no-1           (always)
 //   segment B : singles (b',k), k = 0..no-1           (a' != b')
-//   segment C : singles (a,k'),  a = 0..nv-1          (padded: 0 at a in {a',b'})
-//   segment D : singles (a,l'),  a = 0..nv-1          (k' != l'; padded likewise)
+//   segment C : singles (a,k'),  a = 0..nv-1          (0 at a in {a',b'})
+//   segment D : singles (a,l'),  a = 0..nv-1          (k' != l'; 0 likewise)
 //
-// Row lengths: class 1 (a'=b',k'=l') no+nv; class 2 (a'<b',k'=l') 2no+nv;
-// class 3 (a'=b',k'<l') no+2nv; classes 4I/4II 2no+2nv.  Segments C and D are
-// padded to the full virtual range so that lane a of a warp always owns
-// single (a,k'): the sigma product then accumulates B V2 in registers.
+// Segments A/B are padded to noP = 8*ceil(no/8) and C/D to nvP = 8*ceil(nv/8)
+// entries (zeros), so every segment starts on a 16-byte boundary for BF16
+// (and on 32/64 bytes for FP32/FP64) and a lane can fetch 8 consecutive
+// values with one vector load.  Row lengths: class 1 (a'=b',k'=l') noP+nvP;
+// class 2 (a'<b',k'=l') 2noP+nvP; class 3 (a'=b',k'<l') noP+2nvP; classes
+// 4I/4II 2noP+2nvP.  Because C and D cover the full virtual range, the lane
+// that owns virtual a always owns single (a,k'): the sigma product
+// accumulates B V2 in registers.
 //
 // Storage order of rows ("slabs" of fixed (k',l')): classes 1, 3, 4I, 4II in
 // the kpq order (hole indices outer); class 2 hole-outer (k' outer, pair
@@ -51,6 +55,7 @@ constexpr int BUF_SIZE = 655360; // parameters.f90:425
 // ---------------------------------------------------------------------------
 struct Geometry {
   int no = 0, nv = 0;
+  int noP = 0, nvP = 0;   // segment lengths padded to multiples of 8
   int64_t n1 = 0;         // singles
   int64_t c1 = 0, c2 = 0, c3 = 0, c4 = 0;   // class sizes (4 = each of 4I, 4II)
   int64_t n2 = 0, N = 0;
@@ -61,6 +66,8 @@ struct Geometry {
 
   void init(int no_, int nv_) {
     no = no_; nv = nv_;
+    noP = (no + 7) / 8 * 8;
+    nvP = (nv + 7) / 8 * 8;
     n1 = (int64_t)no * nv;
     npair_v = (int64_t)nv * (nv - 1) / 2;
     npair_o = (int64_t)no * (no - 1) / 2;
@@ -72,10 +79,10 @@ struct Geometry {
     N = n1 + n2;
     start[0] = 0; start[1] = c1; start[2] = c1 + c2; start[3] = c1 + c2 + c3;
     start[4] = start[3] + c4; start[5] = n2;
-    len[0] = no + nv;
-    len[1] = 2 * no + nv;
-    len[2] = no + 2 * nv;
-    len[3] = 2 * no + 2 * nv;
+    len[0] = noP + nvP;
+    len[1] = 2 * noP + nvP;
+    len[2] = noP + 2 * nvP;
+    len[3] = 2 * noP + 2 * nvP;
     len[4] = len[3];
     off[0] = 0;
     for (int c = 0; c < 5; ++c) off[c + 1] = off[c] + (start[c + 1] - start[c]) * len[c];
@@ -108,7 +115,7 @@ __host__ __device__ inline void pair_decode(int64_t p, int n, int& x, int& y) {
 }
 
 struct GeomDev {
-  int no, nv;
+  int no, nv, noP, nvP;
   int64_t n1, n2, N;
   int64_t start[6];
   int64_t len[5];
@@ -118,7 +125,7 @@ struct GeomDev {
 
 inline GeomDev to_dev(const Geometry& g) {
   GeomDev d;
-  d.no = g.no; d.nv = g.nv; d.n1 = g.n1; d.n2 = g.n2; d.N = g.N;
+  d.no = g.no; d.nv = g.nv; d.noP = g.noP; d.nvP = g.nvP; d.n1 = g.n1; d.n2 = g.n2; d.N = g.N;
   for (int i = 0; i < 6; ++i) { d.start[i] = g.start[i]; d.off[i] = g.off[i]; }
   for (int i = 0; i < 5; ++i) d.len[i] = g.len[i];
   d.npair_v = g.npair_v; d.npair_o = g.npair_o;
@@ -171,16 +178,16 @@ __host__ __device__ inline int64_t row_to_d(const GeomDev& g, const Double& r, i
 // position of segments C/D.
 __host__ __device__ inline int64_t entry_single(const GeomDev& g, const Double& r, int e) {
   const int no = g.no;
-  if (e < no) return (int64_t)r.ap * no + e;                   // segment A
-  e -= no;
+  if (e < g.noP) return e < no ? (int64_t)r.ap * no + e : -1;  // segment A
+  e -= g.noP;
   const bool twoa = r.ap != r.bp;
   if (twoa) {
-    if (e < no) return (int64_t)r.bp * no + e;                 // segment B
-    e -= no;
+    if (e < g.noP) return e < no ? (int64_t)r.bp * no + e : -1;  // segment B
+    e -= g.noP;
   }
-  const int seg = e / g.nv;                                     // 0: C (k'), 1: D (l')
-  const int a = e - seg * g.nv;
-  if (a == r.ap || a == r.bp) return -1;
+  const int seg = e / g.nvP;                                    // 0: C (k'), 1: D (l')
+  const int a = e - seg * g.nvP;
+  if (a >= g.nv || a == r.ap || a == r.bp) return -1;
   return (int64_t)a * no + (seg == 0 ? r.kp : r.lp);
 }
 
@@ -270,6 +277,8 @@ struct SigmaPlan {
   int nchunks = 0, nitems = 0;
   int chunk = 64;             // rows per pass-1 work item (autotuned)
   int mc_cap[2] = {2, 4};     // columns per pass for FP64 / FP32 vectors (autotuned)
+  void* d_acc = nullptr;      // FP64 accumulator of the singles rows (FP32 path)
+  size_t acc_bytes = 0;
 };
 int prepare_desc(Ctx* c);
 int build_chunks(Ctx* c, int chunk);

@@ -16,6 +16,8 @@
 // k_singles: W1 = diag1 . V1 + A V1 as a tiled dense product (n1 <= ~5000).
 #include <cuda_bf16.h>
 
+#include <type_traits>
+
 #include "internal.h"
 
 namespace adcgpu {
@@ -31,8 +33,32 @@ template <> struct Acc<double, double> { __device__ static double v(double x) { 
 template <> struct Acc<float, float> { __device__ static float v(float x) { return x; } };
 template <> struct Acc<float, __nv_bfloat16> { __device__ static float v(__nv_bfloat16 x) { return __bfloat162float(x); } };
 
-// Virtual index a = lane + 32 t, t < NT (template: 4, 6 or 8 for nv <= 128,
-// 192, 256).
+// 8 consecutive stored values -> T (one 16-byte load for BF16, two for FP32,
+// four for FP64; segments start on 16-byte boundaries).
+template <typename T, typename TV> struct Load8;
+template <> struct Load8<float, __nv_bfloat16> {
+  __device__ __forceinline__ static void go(const __nv_bfloat16* p, float (&v)[8]) {
+    uint4 q = __ldg(reinterpret_cast<const uint4*>(p));
+    const __nv_bfloat162* h = reinterpret_cast<const __nv_bfloat162*>(&q);
+#pragma unroll
+    for (int i = 0; i < 4; ++i) { float2 f = __bfloat1622float2(h[i]); v[2 * i] = f.x; v[2 * i + 1] = f.y; }
+  }
+};
+template <> struct Load8<float, float> {
+  __device__ __forceinline__ static void go(const float* p, float (&v)[8]) {
+    float4 a = __ldg(reinterpret_cast<const float4*>(p)), b = __ldg(reinterpret_cast<const float4*>(p) + 1);
+    v[0] = a.x; v[1] = a.y; v[2] = a.z; v[3] = a.w; v[4] = b.x; v[5] = b.y; v[6] = b.z; v[7] = b.w;
+  }
+};
+template <> struct Load8<double, double> {
+  __device__ __forceinline__ static void go(const double* p, double (&v)[8]) {
+#pragma unroll
+    for (int i = 0; i < 4; ++i) {
+      double2 d = __ldg(reinterpret_cast<const double2*>(p) + i);
+      v[2 * i] = d.x; v[2 * i + 1] = d.y;
+    }
+  }
+};
 
 // Advance (a',b') to the next row of a slab in storage order.
 __device__ __forceinline__ void next_pair(int& ap, int& bp, bool twoa, int nv) {
@@ -40,20 +66,24 @@ __device__ __forceinline__ void next_pair(int& ap, int& bp, bool twoa, int nv) {
   if (++bp == nv) { ++ap; bp = ap + 1; }
 }
 
-// Pass 1: one warp per chunk of rows inside one slab (fixed k', l', class).
-// Segment C/D products with V2 accumulate in registers (lane owns virtual a),
-// segment A products accumulate while a' is unchanged; W2 rows are complete
-// except for segment B, which pass 2 adds.
-template <typename T, typename TV, int MC, int NTMAX>
+// Pass 1: one warp per work item (rows of one slab: fixed k', l', class).
+// The row's A, C and D segments are split in 8-value chunks; lane l owns
+// chunks l and l + 32 for the whole item (role A: singles (a', 8q..8q+7);
+// C: (8q..8q+7, k'); D: (8q..8q+7, l')).  Products with V2 accumulate in
+// registers (C/D: fixed targets; A: while a' is unchanged); W2 rows are
+// written complete except for segment B, which pass 2 adds.  The next row's
+// values and V2 entries are loaded before the current row is reduced.
+template <typename T, typename TV, typename TA, int MC>
 __global__ void __launch_bounds__(256) k_sigma_p1(GeomDev g, const int2* __restrict__ chunks, int nchunks,
                                                   const TV* __restrict__ Bt, const T* __restrict__ diag,
                                                   const T* __restrict__ V, int64_t ldv, T* __restrict__ W,
-                                                  int64_t ldw) {
+                                                  int64_t ldw, TA* __restrict__ W1, int64_t ld1) {
   const int lane = threadIdx.x & 31;
   const int warp = (blockIdx.x * blockDim.x + threadIdx.x) >> 5;
   const int nwarps = (gridDim.x * blockDim.x) >> 5;
   const int no = g.no, nv = g.nv;
   const int64_t n1 = g.n1;
+  const int nA = g.noP / 8, nC = g.nvP / 8;
   for (int ci = warp; ci < nchunks; ci += nwarps) {
     const int2 ch = chunks[ci];
     Double r = decode_row(g, ch.x);
@@ -61,93 +91,105 @@ __global__ void __launch_bounds__(256) k_sigma_p1(GeomDev g, const int2* __restr
     const bool twoa = (cls == 1 || cls >= 3);
     const bool hasD = cls >= 2;
     const int64_t L = g.len[cls];
-    const int offC = twoa ? 2 * no : no;
+    const int offC = twoa ? 2 * g.noP : g.noP;
     const int kp = r.kp, lp = r.lp;
-    T xk[NTMAX][MC], xl[NTMAX][MC], yk[NTMAX][MC], yl[NTMAX][MC];
+    const int nCh = nA + nC + (hasD ? nC : 0);
+    // roles of the two owned chunks: 0 A, 1 C, 2 D, -1 none
+    int role[2], base[2], moff[2];
 #pragma unroll
-    for (int t = 0; t < NTMAX; ++t) {
-      const int a = lane + 32 * t;
-#pragma unroll
-      for (int c = 0; c < MC; ++c) {
-        xk[t][c] = (a < nv) ? V[(int64_t)c * ldv + (int64_t)a * no + kp] : T(0);
-        xl[t][c] = (a < nv && hasD) ? V[(int64_t)c * ldv + (int64_t)a * no + lp] : T(0);
-        yk[t][c] = T(0);
-        yl[t][c] = T(0);
-      }
+    for (int k = 0; k < 2; ++k) {
+      const int q = lane + 32 * k;
+      if (q >= nCh) { role[k] = -1; base[k] = 0; moff[k] = 0; }
+      else if (q < nA) { role[k] = 0; base[k] = 8 * q; moff[k] = 8 * q; }
+      else if (q < nA + nC) { role[k] = 1; base[k] = 8 * (q - nA); moff[k] = offC + 8 * (q - nA); }
+      else { role[k] = 2; base[k] = 8 * (q - nA - nC); moff[k] = offC + g.nvP + 8 * (q - nA - nC); }
     }
-    int cur_ap = -1;
-    T xa[MC], ya[MC];
+    T xq[2][8][MC], yq[2][8][MC];
 #pragma unroll
-    for (int c = 0; c < MC; ++c) { xa[c] = T(0); ya[c] = T(0); }
+    for (int k = 0; k < 2; ++k)
+#pragma unroll
+      for (int u = 0; u < 8; ++u)
+#pragma unroll
+        for (int c = 0; c < MC; ++c) {
+          yq[k][u][c] = T(0);
+          const int a = base[k] + u;
+          T x = T(0);
+          if ((role[k] == 1 || role[k] == 2) && a < nv)
+            x = V[(int64_t)c * ldv + (int64_t)a * no + (role[k] == 1 ? kp : lp)];
+          xq[k][u][c] = x;
+        }
+    int cur_ap = -1;
     const TV* rowp = Bt + g.off[cls] + (int64_t)(ch.x - g.start[cls]) * L;
     int ap = r.ap, bp = r.bp;
-    // software pipeline: the next row's values and V2 entries are loaded
-    // while the current row is reduced
-    T cA, cC[NTMAX], cD[NTMAX], cx2[MC];
+    T cv[2][8], cx2[MC];
     int64_t cd;
     {
       Double rr{ap, bp, kp, lp, cls};
       cd = row_to_d(g, rr, ch.x);
-      cA = lane < no ? (T)Acc<T, TV>::v(rowp[lane]) : T(0);
 #pragma unroll
-      for (int t = 0; t < NTMAX; ++t) {
-        const int a = lane + 32 * t;
-        cC[t] = a < nv ? (T)Acc<T, TV>::v(rowp[offC + a]) : T(0);
-        cD[t] = (a < nv && hasD) ? (T)Acc<T, TV>::v(rowp[offC + nv + a]) : T(0);
+      for (int k = 0; k < 2; ++k) {
+        if (role[k] >= 0) Load8<T, TV>::go(rowp + moff[k], cv[k]);
+        else {
+#pragma unroll
+          for (int u = 0; u < 8; ++u) cv[k][u] = T(0);
+        }
       }
 #pragma unroll
       for (int c = 0; c < MC; ++c) cx2[c] = V[(int64_t)c * ldv + n1 + cd];
     }
     for (int row = ch.x; row < ch.y; ++row) {
-      const int cur_bp_ap = ap;
+      // prefetch the next row
       int nap = ap, nbp = bp;
       next_pair(nap, nbp, twoa, nv);
-      T nA = T(0), nC[NTMAX], nD[NTMAX], nx2[MC];
+      T nv_[2][8], nx2[MC];
       int64_t nd = 0;
-      if (row + 1 < ch.y) {
-        const TV* np = rowp + L;
+      const bool more = row + 1 < ch.y;
+      if (more) {
         Double rr{nap, nbp, kp, lp, cls};
         nd = row_to_d(g, rr, row + 1);
-        nA = lane < no ? (T)Acc<T, TV>::v(np[lane]) : T(0);
-#pragma unroll
-        for (int t = 0; t < NTMAX; ++t) {
-          const int a = lane + 32 * t;
-          nC[t] = a < nv ? (T)Acc<T, TV>::v(np[offC + a]) : T(0);
-          nD[t] = (a < nv && hasD) ? (T)Acc<T, TV>::v(np[offC + nv + a]) : T(0);
-        }
-#pragma unroll
-        for (int c = 0; c < MC; ++c) nx2[c] = V[(int64_t)c * ldv + n1 + nd];
-      } else {
-#pragma unroll
-        for (int t = 0; t < NTMAX; ++t) { nC[t] = T(0); nD[t] = T(0); }
-#pragma unroll
-        for (int c = 0; c < MC; ++c) nx2[c] = T(0);
       }
-      if (cur_bp_ap != cur_ap) {
-        if (cur_ap >= 0 && lane < no) {
 #pragma unroll
-          for (int c = 0; c < MC; ++c) atomicAdd(&W[(int64_t)c * ldw + (int64_t)cur_ap * no + lane], ya[c]);
-        }
-        cur_ap = cur_bp_ap;
+      for (int k = 0; k < 2; ++k) {
+        if (more && role[k] >= 0) Load8<T, TV>::go(rowp + L + moff[k], nv_[k]);
+        else {
 #pragma unroll
-        for (int c = 0; c < MC; ++c) {
-          xa[c] = lane < no ? V[(int64_t)c * ldv + (int64_t)cur_ap * no + lane] : T(0);
-          ya[c] = T(0);
+          for (int u = 0; u < 8; ++u) nv_[k][u] = T(0);
         }
+      }
+#pragma unroll
+      for (int c = 0; c < MC; ++c) nx2[c] = more ? V[(int64_t)c * ldv + n1 + nd] : T(0);
+      // segment A targets change with a'
+      if (ap != cur_ap) {
+#pragma unroll
+        for (int k = 0; k < 2; ++k) {
+          if (role[k] == 0) {
+#pragma unroll
+            for (int u = 0; u < 8; ++u) {
+              const int kk = base[k] + u;
+#pragma unroll
+              for (int c = 0; c < MC; ++c) {
+                if (cur_ap >= 0 && kk < no && yq[k][u][c] != T(0))
+                  atomicAdd(&W1[(int64_t)c * ld1 + (int64_t)cur_ap * no + kk], (TA)yq[k][u][c]);
+                yq[k][u][c] = T(0);
+                xq[k][u][c] = kk < no ? V[(int64_t)c * ldv + (int64_t)ap * no + kk] : T(0);
+              }
+            }
+          }
+        }
+        cur_ap = ap;
       }
       T z[MC];
 #pragma unroll
-      for (int c = 0; c < MC; ++c) {
-        ya[c] += cA * cx2[c];
-        z[c] = cA * xa[c];
+      for (int c = 0; c < MC; ++c) z[c] = T(0);
 #pragma unroll
-        for (int t = 0; t < NTMAX; ++t) {
-          yk[t][c] += cC[t] * cx2[c];
-          z[c] += cC[t] * xk[t][c];
-          yl[t][c] += cD[t] * cx2[c];
-          z[c] += cD[t] * xl[t][c];
-        }
-      }
+      for (int k = 0; k < 2; ++k)
+#pragma unroll
+        for (int u = 0; u < 8; ++u)
+#pragma unroll
+          for (int c = 0; c < MC; ++c) {
+            yq[k][u][c] += cv[k][u] * cx2[c];
+            z[c] += cv[k][u] * xq[k][u][c];
+          }
 #pragma unroll
       for (int c = 0; c < MC; ++c) {
         T v = z[c];
@@ -155,91 +197,118 @@ __global__ void __launch_bounds__(256) k_sigma_p1(GeomDev g, const int2* __restr
         for (int o = 16; o; o >>= 1) v += __shfl_xor_sync(0xffffffffu, v, o);
         if (lane == 0) W[(int64_t)c * ldw + n1 + cd] = diag[n1 + cd] * cx2[c] + v;
       }
-      ap = nap; bp = nbp; rowp += L; cd = nd; cA = nA;
+      ap = nap; bp = nbp; rowp += L; cd = nd;
 #pragma unroll
-      for (int t = 0; t < NTMAX; ++t) { cC[t] = nC[t]; cD[t] = nD[t]; }
+      for (int k = 0; k < 2; ++k)
+#pragma unroll
+        for (int u = 0; u < 8; ++u) cv[k][u] = nv_[k][u];
 #pragma unroll
       for (int c = 0; c < MC; ++c) cx2[c] = nx2[c];
     }
-    if (lane < no) {
+    // flush the register accumulators
 #pragma unroll
-      for (int c = 0; c < MC; ++c) atomicAdd(&W[(int64_t)c * ldw + (int64_t)cur_ap * no + lane], ya[c]);
-    }
+    for (int k = 0; k < 2; ++k) {
+      if (role[k] < 0) continue;
 #pragma unroll
-    for (int t = 0; t < NTMAX; ++t) {
-      const int a = lane + 32 * t;
-      if (a < nv) {
+      for (int u = 0; u < 8; ++u) {
+        const int idx = base[k] + u;
+        int64_t tgt = -1;
+        if (role[k] == 0) { if (idx < no) tgt = (int64_t)cur_ap * no + idx; }
+        else if (idx < nv) tgt = (int64_t)idx * no + (role[k] == 1 ? kp : lp);
+        if (tgt < 0) continue;
 #pragma unroll
-        for (int c = 0; c < MC; ++c) {
-          atomicAdd(&W[(int64_t)c * ldw + (int64_t)a * no + kp], yk[t][c]);
-          if (hasD) atomicAdd(&W[(int64_t)c * ldw + (int64_t)a * no + lp], yl[t][c]);
-        }
+        for (int c = 0; c < MC; ++c)
+          if (yq[k][u][c] != T(0)) atomicAdd(&W1[(int64_t)c * ld1 + tgt], (TA)yq[k][u][c]);
       }
     }
   }
 }
 
 // Pass 2: segment B (classes 2, 4I, 4II).  One warp per (slab, b'): rows
-// (a',b') for a' < b' share the target singles (b', k), accumulated in
-// registers; W2 rows receive the segment-B part of their sums.
-template <typename T, typename TV, int MC>
+// (a', b') for a' < b' share the target singles (b', k).  Lanes form groups
+// of GS (>= noP/8 chunks of segment B): group slot = row, lane in group =
+// 8-value chunk.  32/GS rows are in flight per step; partial W1 sums reduce
+// across groups at the end, W2 sums within a group.
+template <typename T, typename TV, typename TA, int MC, int GS>
 __global__ void __launch_bounds__(256) k_sigma_p2(GeomDev g, const int2* __restrict__ items, int nitems,
                                                   const TV* __restrict__ Bt, const T* __restrict__ V, int64_t ldv,
-                                                  T* __restrict__ W, int64_t ldw) {
+                                                  T* __restrict__ W, int64_t ldw, TA* __restrict__ W1, int64_t ld1) {
   const int lane = threadIdx.x & 31;
   const int warp = (blockIdx.x * blockDim.x + threadIdx.x) >> 5;
   const int nwarps = (gridDim.x * blockDim.x) >> 5;
   const int no = g.no, nv = g.nv;
   const int64_t n1 = g.n1;
+  const int nB = g.noP / 8;
+  const int slot = lane / GS, h = lane % GS;
+  constexpr int RPS = 32 / GS;   // rows per step
   for (int it = warp; it < nitems; it += nwarps) {
     const int2 item = items[it];
     const int slab0 = item.x, bp = item.y;
     Double r = decode_row(g, slab0);
     const int cls = r.cls;
     const int64_t L = g.len[cls];
-    T xb[MC], yb[MC];
+    const bool act = h < nB;
+    T xb[8][MC], yb[8][MC];
 #pragma unroll
-    for (int c = 0; c < MC; ++c) {
-      xb[c] = lane < no ? V[(int64_t)c * ldv + (int64_t)bp * no + lane] : T(0);
-      yb[c] = T(0);
-    }
-    constexpr int U = 4;   // rows in flight per warp
-    for (int ap0 = 0; ap0 < bp; ap0 += U) {
-      T v[U], x2[U][MC], w2[U][MC];
-      int64_t d[U];
+    for (int u = 0; u < 8; ++u)
 #pragma unroll
-      for (int u = 0; u < U; ++u) {
-        const int ap = ap0 + u;
-        d[u] = -1;
-        v[u] = T(0);
-        if (ap < bp) {
-          const int64_t row = slab0 + pair_index(ap, bp, nv);
-          Double rr{ap, bp, r.kp, r.lp, cls};
-          d[u] = row_to_d(g, rr, row);
-          const TV* rowp = Bt + g.off[cls] + (row - g.start[cls]) * L;
-          v[u] = lane < no ? (T)Acc<T, TV>::v(rowp[no + lane]) : T(0);
-        }
+      for (int c = 0; c < MC; ++c) {
+        const int kk = 8 * h + u;
+        xb[u][c] = (act && kk < no) ? V[(int64_t)c * ldv + (int64_t)bp * no + kk] : T(0);
+        yb[u][c] = T(0);
+      }
+    for (int a0 = 0; a0 < bp; a0 += RPS) {
+      const int ap = a0 + slot;
+      const bool rv = ap < bp;
+      T v[8], x2[MC], w2[MC];
+      int64_t d = 0;
+      if (rv) {
+        const int64_t row = slab0 + pair_index(ap, bp, nv);
+        Double rr{ap, bp, r.kp, r.lp, cls};
+        d = row_to_d(g, rr, row);
+        if (act) Load8<T, TV>::go(Bt + g.off[cls] + (row - g.start[cls]) * L + g.noP + 8 * h, v);
+      }
+      if (!(rv && act)) {
 #pragma unroll
-        for (int c = 0; c < MC; ++c) {
-          x2[u][c] = d[u] >= 0 ? V[(int64_t)c * ldv + n1 + d[u]] : T(0);
-          w2[u][c] = (d[u] >= 0 && lane == 0) ? W[(int64_t)c * ldw + n1 + d[u]] : T(0);
-        }
+        for (int u = 0; u < 8; ++u) v[u] = T(0);
       }
 #pragma unroll
-      for (int u = 0; u < U; ++u) {
+      for (int c = 0; c < MC; ++c) {
+        x2[c] = rv ? V[(int64_t)c * ldv + n1 + d] : T(0);
+        w2[c] = (rv && h == 0) ? W[(int64_t)c * ldw + n1 + d] : T(0);
+      }
 #pragma unroll
-        for (int c = 0; c < MC; ++c) {
-          yb[c] += v[u] * x2[u][c];
-          T z = v[u] * xb[c];
+      for (int c = 0; c < MC; ++c) {
+        T z = T(0);
 #pragma unroll
-          for (int o = 16; o; o >>= 1) z += __shfl_xor_sync(0xffffffffu, z, o);
-          if (lane == 0 && d[u] >= 0) W[(int64_t)c * ldw + n1 + d[u]] = w2[u][c] + z;
+        for (int u = 0; u < 8; ++u) {
+          yb[u][c] += v[u] * x2[c];
+          z += v[u] * xb[u][c];
         }
+#pragma unroll
+        for (int o = 1; o < GS; o <<= 1) z += __shfl_xor_sync(0xffffffffu, z, o);
+        if (rv && h == 0) W[(int64_t)c * ldw + n1 + d] = w2[c] + z;
       }
     }
-    if (lane < no) {
+    // sum yb over the row slots (lanes with equal h), then flush
 #pragma unroll
-      for (int c = 0; c < MC; ++c) atomicAdd(&W[(int64_t)c * ldw + (int64_t)bp * no + lane], yb[c]);
+    for (int u = 0; u < 8; ++u)
+#pragma unroll
+      for (int c = 0; c < MC; ++c) {
+        T y = yb[u][c];
+#pragma unroll
+        for (int o = GS; o < 32; o <<= 1) y += __shfl_xor_sync(0xffffffffu, y, o);
+        yb[u][c] = y;
+      }
+    if (slot == 0 && act) {
+#pragma unroll
+      for (int u = 0; u < 8; ++u) {
+        const int kk = 8 * h + u;
+        if (kk >= no) continue;
+#pragma unroll
+        for (int c = 0; c < MC; ++c)
+          if (yb[u][c] != T(0)) atomicAdd(&W1[(int64_t)c * ld1 + (int64_t)bp * no + kk], (TA)yb[u][c]);
+      }
     }
   }
 }
@@ -286,6 +355,14 @@ void sigma_stats_flush(Ctx* c) {
   c->st_pending = false;
 }
 
+// W1 += accumulated coupling part (FP64 accumulator of the FP32 path)
+__global__ void k_w1_finalize(int n1, int m, const double* __restrict__ acc, float* __restrict__ W, int64_t ldw) {
+  for (int i = blockIdx.x * blockDim.x + threadIdx.x; i < n1 * m; i += gridDim.x * blockDim.x) {
+    const int c = i / n1, s = i - c * n1;
+    W[(int64_t)c * ldw + s] += (float)acc[i];
+  }
+}
+
 template <typename T, typename TV>
 int sigma_impl(Ctx* c, int m, const T* dV, int64_t ldv, T* dW, int64_t ldw, const T* A, const T* diag,
                const TV* Bt) {
@@ -303,33 +380,56 @@ int sigma_impl(Ctx* c, int m, const T* dV, int64_t ldv, T* dW, int64_t ldw, cons
   dim3 gs((n1 + 63) / 64, (m + 3) / 4);
   k_singles<T><<<gs, 256, 0, s>>>(n1, A, diag, dV, ldv, dW, ldw, m);
   ADC_CUDA(c, cudaGetLastError());
-  const SigmaPlan* plan = reinterpret_cast<const SigmaPlan*>(c->sigma_plan);
+  SigmaPlan* plan = reinterpret_cast<SigmaPlan*>(c->sigma_plan);
   if (!plan) return set_err(c, ADCGPU_NO_MATRIX, "sigma plan missing");
   const int2* chunks = plan->d_chunks;
   const int2* items = plan->d_items;
+  // FP64 path: coupling contributions to W1 go straight into W.  FP32 path:
+  // into an FP64 n1 x m accumulator, added to W1 at the end (a singles row
+  // sums ~ n2 n1 / N products; FP32 atomics there would floor the residual).
+  typedef typename std::conditional<sizeof(T) == 8, T, double>::type TAcc;
+  TAcc* W1base = nullptr;
+  if (sizeof(T) == 4) {
+    const size_t need = sizeof(double) * (size_t)n1 * m;
+    if (plan->acc_bytes < need) {
+      if (plan->d_acc) cudaFree(plan->d_acc);
+      plan->d_acc = nullptr; plan->acc_bytes = 0;
+      int st2 = dmalloc(c, (void**)&plan->d_acc, need);
+      if (st2) return st2;
+      plan->acc_bytes = need;
+    }
+    ADC_CUDA(c, cudaMemsetAsync(plan->d_acc, 0, need, s));
+    W1base = reinterpret_cast<TAcc*>(plan->d_acc);
+  }
   int c0 = 0;
   while (c0 < m) {
     const int left = m - c0;
     const T* V = dV + (int64_t)c0 * ldv;
     T* W = dW + (int64_t)c0 * ldw;
+    TAcc* W1 = sizeof(T) == 8 ? reinterpret_cast<TAcc*>(W) : W1base + (int64_t)c0 * n1;
+    const int64_t ld1 = sizeof(T) == 8 ? ldw : (int64_t)n1;
     int cap = plan->mc_cap[sizeof(T) == 8 ? 0 : 1];
-    if (sizeof(T) == 8 || G.nv > 192) cap = std::min(cap, 2);
+    if (sizeof(T) == 8) cap = std::min(cap, 2);
     const int mc = (left >= 4 && cap >= 4) ? 4 : ((left >= 2 && cap >= 2) ? 2 : 1);
     const int g1 = std::min(plan->nchunks, 152 * 8 * 8) / 8 + 1;
     const int g2 = std::min(plan->nitems, 152 * 8 * 8) / 8 + 1;
-#define LAUNCH(MC, NT)                                                                                  \
-  k_sigma_p1<T, TV, MC, NT><<<g1, 256, 0, s>>>(g, chunks, plan->nchunks, Bt, diag, V, ldv, W, ldw);    \
-  if (plan->nitems) k_sigma_p2<T, TV, MC><<<g2, 256, 0, s>>>(g, items, plan->nitems, Bt, V, ldv, W, ldw);
-#define LAUNCH_NT(MC)                                     \
-  if (G.nv <= 128) { LAUNCH(MC, 4) }                      \
-  else if (G.nv <= 192) { LAUNCH(MC, 6) }                 \
-  else { LAUNCH(MC, 8) }
-    if (mc == 4) { LAUNCH_NT(4) } else if (mc == 2) { LAUNCH_NT(2) } else { LAUNCH_NT(1) }
-#undef LAUNCH_NT
+#define LAUNCH_P2(MC, GS) \
+  k_sigma_p2<T, TV, TAcc, MC, GS><<<g2, 256, 0, s>>>(g, items, plan->nitems, Bt, V, ldv, W, ldw, W1, ld1);
+#define LAUNCH(MC)                                                                                              \
+  k_sigma_p1<T, TV, TAcc, MC><<<g1, 256, 0, s>>>(g, chunks, plan->nchunks, Bt, diag, V, ldv, W, ldw, W1, ld1); \
+  if (plan->nitems) {                                                                                           \
+    if (G.noP <= 8) { LAUNCH_P2(MC, 1) } else if (G.noP <= 16) { LAUNCH_P2(MC, 2) } else { LAUNCH_P2(MC, 4) }   \
+  }
+    if (mc == 4) { LAUNCH(4) } else if (mc == 2) { LAUNCH(2) } else { LAUNCH(1) }
+#undef LAUNCH
+#undef LAUNCH_P2_NT
 #undef LAUNCH
     ADC_CUDA(c, cudaGetLastError());
     c0 += mc;
   }
+  if (sizeof(T) == 4)
+    k_w1_finalize<<<(n1 * m + 255) / 256, 256, 0, s>>>(n1, m, reinterpret_cast<const double*>(W1base),
+                                                       reinterpret_cast<float*>(dW), ldw);
   ADC_CUDA(c, cudaEventRecord(c->st_ev1, s));
   c->st_pending = true;
   c->st_pending_cols = m;
@@ -393,6 +493,7 @@ void free_sigma_plan(Ctx* c) {
   if (!plan) return;
   if (plan->d_chunks) cudaFree(plan->d_chunks);
   if (plan->d_items) cudaFree(plan->d_items);
+  if (plan->d_acc) cudaFree(plan->d_acc);
   delete plan;
   c->sigma_plan = nullptr;
 }
