@@ -199,3 +199,66 @@ def load(path: str) -> np.ndarray:
 
 
 DEFAULT_WEIGHTS = os.path.join(os.path.dirname(os.path.abspath(__file__)), "mlp_weights.npy")
+
+
+def evaluate(params, systems, nstates=6, tol=1e-6, maxiter=300):
+    """Davidson iterations and time with the diagonal and the learned
+    preconditioner on the given (nocc, nvirt, seed) systems (FP64 path)."""
+    import time
+
+    rows = []
+    for no, nv, seed in systems:
+        e, eri = api.synth_system(no, nv, seed)
+        g = api.AdcGpu(0)
+        g.set_orbitals(no, nv, e)
+        g.set_eri_packed(eri)
+        g.write_fspace_adc2_1(None)
+        t = time.perf_counter()
+        r0 = g.davdiag_block(nstates, tol, precon=api.PRECON_DPR, maxiter=maxiter, want_vectors=False,
+                             raise_on_nonconv=False)
+        t0 = time.perf_counter() - t
+        load_into(g, params)
+        t = time.perf_counter()
+        r1 = g.davdiag_block(nstates, tol, precon=api.PRECON_MLP, maxiter=maxiter, want_vectors=False,
+                             raise_on_nonconv=False)
+        t1 = time.perf_counter() - t
+        g.close()
+        rows.append({"nocc": no, "nvirt": nv, "seed": seed, "iters_dpr": r0.iterations, "iters_mlp": r1.iterations,
+                     "s_dpr": t0, "s_mlp": t1, "status": [r0.status, r1.status],
+                     "max_dE": float(np.abs(r0.evals - r1.evals).max())})
+    return rows
+
+
+def main(argv=None):
+    import argparse
+    import json
+    import time
+
+    ap = argparse.ArgumentParser(description="train the learned Davidson preconditioner on the GPU")
+    ap.add_argument("--systems", type=int, default=200)
+    ap.add_argument("--steps", type=int, default=600)
+    ap.add_argument("--lr", type=float, default=1e-3)
+    ap.add_argument("--out", default=DEFAULT_WEIGHTS)
+    ap.add_argument("--eval", type=int, default=6)
+    a = ap.parse_args(argv)
+    t = time.time()
+    samples = []
+    for no, nv, seed in random_systems(a.systems):
+        samples += make_samples(no, nv, seed)
+    print(f"{len(samples)} samples from {a.systems} systems in {time.time() - t:.1f} s", flush=True)
+    t = time.time()
+    params, losses = train(samples, steps=a.steps, lr=a.lr, log=print)
+    print(f"trained in {time.time() - t:.1f} s: loss {losses[:20].mean():.4f} -> {losses[-20:].mean():.4f}",
+          flush=True)
+    save(a.out, params)
+    held = random_systems(a.eval, seed=99991)
+    rows = evaluate(params, held)
+    for r in rows:
+        print(json.dumps(r), flush=True)
+    it0 = sum(r["iters_dpr"] for r in rows)
+    it1 = sum(r["iters_mlp"] for r in rows)
+    print(json.dumps({"held_out_iters_dpr": it0, "held_out_iters_mlp": it1, "ratio": it1 / max(it0, 1)}), flush=True)
+
+
+if __name__ == "__main__":
+    main()
