@@ -277,6 +277,7 @@ struct SigmaPlan {
   int nchunks = 0, nitems = 0;
   int chunk = 64;             // rows per pass-1 work item (autotuned)
   int mc_cap[2] = {2, 4};     // columns per pass for FP64 / FP32 vectors (autotuned)
+  int staged = 1;             // pass 1 through a cp.async shared-memory ring (autotuned)
   void* d_acc = nullptr;      // FP64 accumulator of the singles rows (FP32 path)
   size_t acc_bytes = 0;
 };

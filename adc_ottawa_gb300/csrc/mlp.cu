@@ -592,7 +592,7 @@ extern "C" int adcgpu_mlp_train_step(adcgpu_ctx* h, int G, int S, const float* f
   if (!st && grad_out) {
     ADC_CUDA(c, cudaMemcpyAsync(grad_out, s->grad, sizeof(float) * NPARAM, cudaMemcpyDeviceToHost, c->stream));
   }
-  if (!st && lr > 0.f) {
+  if (!st && lr > 0.f && std::isfinite(loss)) {
     s->step += 1;
     const float b1 = 0.9f, b2 = 0.999f;
     const float c1 = 1.f - powf(b1, (float)s->step), c2 = 1.f - powf(b2, (float)s->step);

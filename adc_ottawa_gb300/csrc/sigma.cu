@@ -74,7 +74,7 @@ __device__ __forceinline__ void next_pair(int& ap, int& bp, bool twoa, int nv) {
 // written complete except for segment B, which pass 2 adds.  The next row's
 // values and V2 entries are loaded before the current row is reduced.
 template <typename T, typename TV, typename TA, int MC>
-__global__ void __launch_bounds__(256) k_sigma_p1(GeomDev g, const int2* __restrict__ chunks, int nchunks,
+__global__ void __launch_bounds__(128) k_sigma_p1(GeomDev g, const int2* __restrict__ chunks, int nchunks,
                                                   const TV* __restrict__ Bt, const T* __restrict__ diag,
                                                   const T* __restrict__ V, int64_t ldv, T* __restrict__ W,
                                                   int64_t ldw, TA* __restrict__ W1, int64_t ld1) {
@@ -206,6 +206,200 @@ __global__ void __launch_bounds__(256) k_sigma_p1(GeomDev g, const int2* __restr
       for (int c = 0; c < MC; ++c) cx2[c] = nx2[c];
     }
     // flush the register accumulators
+#pragma unroll
+    for (int k = 0; k < 2; ++k) {
+      if (role[k] < 0) continue;
+#pragma unroll
+      for (int u = 0; u < 8; ++u) {
+        const int idx = base[k] + u;
+        int64_t tgt = -1;
+        if (role[k] == 0) { if (idx < no) tgt = (int64_t)cur_ap * no + idx; }
+        else if (idx < nv) tgt = (int64_t)idx * no + (role[k] == 1 ? kp : lp);
+        if (tgt < 0) continue;
+#pragma unroll
+        for (int c = 0; c < MC; ++c)
+          if (yq[k][u][c] != T(0)) atomicAdd(&W1[(int64_t)c * ld1 + tgt], (TA)yq[k][u][c]);
+      }
+    }
+  }
+}
+
+// Pass 1, staged variant: the same computation, but each lane copies the
+// 16-byte pieces of its two chunks of the next NS-1 rows (and lanes < MC the
+// row's V2 entries) into a per-warp shared-memory ring with cp.async, so NS
+// rows per warp are in flight without holding them in registers.
+__device__ __forceinline__ void cp_async16(void* smem, const void* gmem) {
+  unsigned s = (unsigned)__cvta_generic_to_shared(smem);
+  asm volatile("cp.async.cg.shared.global [%0], [%1], 16;\n" ::"r"(s), "l"(gmem));
+}
+template <int BYTES>
+__device__ __forceinline__ void cp_async_small(void* smem, const void* gmem) {
+  unsigned s = (unsigned)__cvta_generic_to_shared(smem);
+  asm volatile("cp.async.ca.shared.global [%0], [%1], %2;\n" ::"r"(s), "l"(gmem), "n"(BYTES));
+}
+__device__ __forceinline__ void cp_async_commit() { asm volatile("cp.async.commit_group;\n" ::); }
+template <int N>
+__device__ __forceinline__ void cp_async_wait() { asm volatile("cp.async.wait_group %0;\n" ::"n"(N)); }
+
+template <typename T, typename TV> struct FromSmem8;
+template <> struct FromSmem8<float, __nv_bfloat16> {
+  __device__ __forceinline__ static void go(const void* p, float (&v)[8]) {
+    uint4 q = *reinterpret_cast<const uint4*>(p);
+    const __nv_bfloat162* h = reinterpret_cast<const __nv_bfloat162*>(&q);
+#pragma unroll
+    for (int i = 0; i < 4; ++i) { float2 f = __bfloat1622float2(h[i]); v[2 * i] = f.x; v[2 * i + 1] = f.y; }
+  }
+};
+template <> struct FromSmem8<float, float> {
+  __device__ __forceinline__ static void go(const void* p, float (&v)[8]) {
+    const float4* q = reinterpret_cast<const float4*>(p);
+    float4 a = q[0], b = q[1];
+    v[0] = a.x; v[1] = a.y; v[2] = a.z; v[3] = a.w; v[4] = b.x; v[5] = b.y; v[6] = b.z; v[7] = b.w;
+  }
+};
+template <> struct FromSmem8<double, double> {
+  __device__ __forceinline__ static void go(const void* p, double (&v)[8]) {
+    const double2* q = reinterpret_cast<const double2*>(p);
+#pragma unroll
+    for (int i = 0; i < 4; ++i) { double2 d = q[i]; v[2 * i] = d.x; v[2 * i + 1] = d.y; }
+  }
+};
+
+template <typename T, typename TV, typename TA, int MC, int NS>
+__global__ void __launch_bounds__(128) k_sigma_p1s(GeomDev g, const int2* __restrict__ chunks, int nchunks,
+                                                   const TV* __restrict__ Bt, const T* __restrict__ diag,
+                                                   const T* __restrict__ V, int64_t ldv, T* __restrict__ W,
+                                                   int64_t ldw, TA* __restrict__ W1, int64_t ld1) {
+  constexpr int CB = 8 * sizeof(TV);              // bytes of one 8-value chunk
+  constexpr int LANE_B = 2 * CB;                  // per lane per stage
+  constexpr int STAGE_B = 32 * LANE_B + 16 * MC;  // + V2 entries (padded)
+  extern __shared__ __align__(16) unsigned char smem_raw[];
+  const int lane = threadIdx.x & 31;
+  unsigned char* ring = smem_raw + (size_t)(threadIdx.x >> 5) * NS * STAGE_B;
+  const int warp = (blockIdx.x * blockDim.x + threadIdx.x) >> 5;
+  const int nwarps = (gridDim.x * blockDim.x) >> 5;
+  const int no = g.no, nv = g.nv;
+  const int64_t n1 = g.n1;
+  const int nA = g.noP / 8, nC = g.nvP / 8;
+  for (int ci = warp; ci < nchunks; ci += nwarps) {
+    const int2 ch = chunks[ci];
+    Double r = decode_row(g, ch.x);
+    const int cls = r.cls;
+    const bool twoa = (cls == 1 || cls >= 3);
+    const bool hasD = cls >= 2;
+    const int64_t L = g.len[cls];
+    const int offC = twoa ? 2 * g.noP : g.noP;
+    const int kp = r.kp, lp = r.lp;
+    const int nCh = nA + nC + (hasD ? nC : 0);
+    int role[2], base[2], moff[2];
+#pragma unroll
+    for (int k = 0; k < 2; ++k) {
+      const int q = lane + 32 * k;
+      if (q >= nCh) { role[k] = -1; base[k] = 0; moff[k] = 0; }
+      else if (q < nA) { role[k] = 0; base[k] = 8 * q; moff[k] = 8 * q; }
+      else if (q < nA + nC) { role[k] = 1; base[k] = 8 * (q - nA); moff[k] = offC + 8 * (q - nA); }
+      else { role[k] = 2; base[k] = 8 * (q - nA - nC); moff[k] = offC + g.nvP + 8 * (q - nA - nC); }
+    }
+    T xq[2][8][MC], yq[2][8][MC];
+#pragma unroll
+    for (int k = 0; k < 2; ++k)
+#pragma unroll
+      for (int u = 0; u < 8; ++u)
+#pragma unroll
+        for (int c = 0; c < MC; ++c) {
+          yq[k][u][c] = T(0);
+          const int a = base[k] + u;
+          T x = T(0);
+          if ((role[k] == 1 || role[k] == 2) && a < nv)
+            x = V[(int64_t)c * ldv + (int64_t)a * no + (role[k] == 1 ? kp : lp)];
+          xq[k][u][c] = x;
+        }
+    const TV* row0p = Bt + g.off[cls] + (int64_t)(ch.x - g.start[cls]) * L;
+    // issue iterator
+    int iap = r.ap, ibp = r.bp;
+    int irow = ch.x;
+    auto issue = [&](int slot) {
+      if (irow < ch.y) {
+        unsigned char* st = ring + slot * STAGE_B;
+        const TV* rp = row0p + (int64_t)(irow - ch.x) * L;
+#pragma unroll
+        for (int k = 0; k < 2; ++k)
+          if (role[k] >= 0) {
+#pragma unroll
+            for (int b = 0; b < CB; b += 16) cp_async16(st + lane * LANE_B + k * CB + b, (const char*)(rp + moff[k]) + b);
+          }
+        if (lane < MC) {
+          Double rr{iap, ibp, kp, lp, cls};
+          const int64_t d = row_to_d(g, rr, irow);
+          cp_async_small<sizeof(T)>(st + 32 * LANE_B + lane * 16, &V[(int64_t)lane * ldv + n1 + d]);
+        }
+        next_pair(iap, ibp, twoa, nv);
+        ++irow;
+      }
+      cp_async_commit();
+    };
+#pragma unroll
+    for (int s0 = 0; s0 < NS - 1; ++s0) issue(s0);
+    int cur_ap = -1;
+    int ap = r.ap, bp = r.bp;
+    int i = 0;
+    for (int row = ch.x; row < ch.y; ++row, ++i) {
+      issue((i + NS - 1) % NS);
+      cp_async_wait<NS - 1>();
+      __syncwarp();
+      const unsigned char* st = ring + (i % NS) * STAGE_B;
+      Double rr{ap, bp, kp, lp, cls};
+      const int64_t cd = row_to_d(g, rr, row);
+      T cx2[MC];
+#pragma unroll
+      for (int c = 0; c < MC; ++c) cx2[c] = *reinterpret_cast<const T*>(st + 32 * LANE_B + c * 16);
+      if (ap != cur_ap) {
+#pragma unroll
+        for (int k = 0; k < 2; ++k) {
+          if (role[k] == 0) {
+#pragma unroll
+            for (int u = 0; u < 8; ++u) {
+              const int kk = base[k] + u;
+#pragma unroll
+              for (int c = 0; c < MC; ++c) {
+                if (cur_ap >= 0 && kk < no && yq[k][u][c] != T(0))
+                  atomicAdd(&W1[(int64_t)c * ld1 + (int64_t)cur_ap * no + kk], (TA)yq[k][u][c]);
+                yq[k][u][c] = T(0);
+                xq[k][u][c] = kk < no ? V[(int64_t)c * ldv + (int64_t)ap * no + kk] : T(0);
+              }
+            }
+          }
+        }
+        cur_ap = ap;
+      }
+      T z[MC];
+#pragma unroll
+      for (int c = 0; c < MC; ++c) z[c] = T(0);
+#pragma unroll
+      for (int k = 0; k < 2; ++k) {
+        if (role[k] < 0) continue;
+        T v[8];
+        FromSmem8<T, TV>::go(st + lane * LANE_B + k * CB, v);
+#pragma unroll
+        for (int u = 0; u < 8; ++u)
+#pragma unroll
+          for (int c = 0; c < MC; ++c) {
+            yq[k][u][c] += v[u] * cx2[c];
+            z[c] += v[u] * xq[k][u][c];
+          }
+      }
+#pragma unroll
+      for (int c = 0; c < MC; ++c) {
+        T v = z[c];
+#pragma unroll
+        for (int o = 16; o; o >>= 1) v += __shfl_xor_sync(0xffffffffu, v, o);
+        if (lane == 0) W[(int64_t)c * ldw + n1 + cd] = diag[n1 + cd] * cx2[c] + v;
+      }
+      __syncwarp();
+      next_pair(ap, bp, twoa, nv);
+    }
+    cp_async_wait<0>();
+    __syncwarp();
 #pragma unroll
     for (int k = 0; k < 2; ++k) {
       if (role[k] < 0) continue;
@@ -411,12 +605,20 @@ int sigma_impl(Ctx* c, int m, const T* dV, int64_t ldv, T* dW, int64_t ldw, cons
     int cap = plan->mc_cap[sizeof(T) == 8 ? 0 : 1];
     if (sizeof(T) == 8) cap = std::min(cap, 2);
     const int mc = (left >= 4 && cap >= 4) ? 4 : ((left >= 2 && cap >= 2) ? 2 : 1);
-    const int g1 = std::min(plan->nchunks, 152 * 8 * 8) / 8 + 1;
+    const int g1 = std::min(plan->nchunks, 152 * 4 * 16) / 4 + 1;   // 4 warps per block
     const int g2 = std::min(plan->nitems, 152 * 8 * 8) / 8 + 1;
 #define LAUNCH_P2(MC, GS) \
   k_sigma_p2<T, TV, TAcc, MC, GS><<<g2, 256, 0, s>>>(g, items, plan->nitems, Bt, V, ldv, W, ldw, W1, ld1);
 #define LAUNCH(MC)                                                                                              \
-  k_sigma_p1<T, TV, TAcc, MC><<<g1, 256, 0, s>>>(g, chunks, plan->nchunks, Bt, diag, V, ldv, W, ldw, W1, ld1); \
+  if (plan->staged) {                                                                                           \
+    constexpr int NS = sizeof(TV) == 2 ? 8 : 4;                                                                 \
+    const size_t smem = (size_t)4 * NS * (32 * 16 * sizeof(TV) + 16 * MC);                                    \
+    auto kern = k_sigma_p1s<T, TV, TAcc, MC, NS>;                                                               \
+    ADC_CUDA(c, cudaFuncSetAttribute(kern, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem));            \
+    kern<<<g1, 128, smem, s>>>(g, chunks, plan->nchunks, Bt, diag, V, ldv, W, ldw, W1, ld1);                   \
+  } else {                                                                                                      \
+    k_sigma_p1<T, TV, TAcc, MC><<<g1, 128, 0, s>>>(g, chunks, plan->nchunks, Bt, diag, V, ldv, W, ldw, W1, ld1); \
+  }                                                                                                             \
   if (plan->nitems) {                                                                                           \
     if (G.noP <= 8) { LAUNCH_P2(MC, 1) } else if (G.noP <= 16) { LAUNCH_P2(MC, 2) } else { LAUNCH_P2(MC, 4) }   \
   }
@@ -540,15 +742,17 @@ extern "C" int adcgpu_sigma_autotune(adcgpu_ctx* h, int m, int* best_chunk, int*
   if ((st = dmalloc(c, &dv, esz * N * m))) return st;
   if ((st = dmalloc(c, &dw, esz * N * m))) { dfree(c, dv, 0); return st; }
   ADC_CUDA(c, cudaMemsetAsync(dv, 0, esz * N * m, c->stream));
-  const int chunks[] = {16, 32, 64, 128, 256};
+  const int chunks[] = {16, 64, 256};
   const int mcs[] = {1, 2, 4};
   double best = 1e30;
-  int bc = plan->chunk, bm = plan->mc_cap[mixed ? 1 : 0];
+  int bc = plan->chunk, bm = plan->mc_cap[mixed ? 1 : 0], bs = plan->staged;
   for (int ch : chunks) {
     if ((st = build_chunks(c, ch))) break;
+    for (int stg = 0; stg < 2; ++stg)
     for (int mc : mcs) {
       if (!mixed && mc > 2) continue;
       plan->mc_cap[mixed ? 1 : 0] = mc;
+      plan->staged = stg;
       double t = 1e30;
       for (int rep = 0; rep < 3; ++rep) {
         cudaEventRecord(c->ev0, c->stream);
@@ -560,17 +764,18 @@ extern "C" int adcgpu_sigma_autotune(adcgpu_ctx* h, int m, int* best_chunk, int*
         cudaEventElapsedTime(&ms, c->ev0, c->ev1);
         if (rep > 0) t = std::min(t, (double)ms);
       }
-      if (t < best) { best = t; bc = ch; bm = mc; }
+      if (t < best) { best = t; bc = ch; bm = mc; bs = stg; }
     }
   }
   sigma_stats_flush(c);
   c->st_calls = 0; c->st_cols = 0; c->st_ms = 0.0; c->st_bytes = 0.0;
   plan->mc_cap[mixed ? 1 : 0] = bm;
+  plan->staged = bs;
   if (!st) st = build_chunks(c, bc);
   dfree(c, dv, 0);
   dfree(c, dw, 0);
   if (best_chunk) *best_chunk = bc;
-  if (best_mc) *best_mc = bm;
+  if (best_mc) *best_mc = bm + 8 * bs;   // bit 3: staged pass-1 variant
   if (best_ms) *best_ms = best;
   return st;
 }
@@ -582,8 +787,9 @@ extern "C" int adcgpu_sigma_set_shape(adcgpu_ctx* h, int chunk, int mc_fp64, int
   cudaSetDevice(c->device);
   if (!c->have_matrix) return set_err(c, ADCGPU_NO_MATRIX, "build the matrix first");
   SigmaPlan* plan = reinterpret_cast<SigmaPlan*>(c->sigma_plan);
-  plan->mc_cap[0] = std::min(mc_fp64, 2);
-  plan->mc_cap[1] = std::min(mc_fp32, 4);
+  plan->staged = ((mc_fp64 | mc_fp32) & 8) ? 1 : 0;
+  plan->mc_cap[0] = std::min(mc_fp64 & 7, 2);
+  plan->mc_cap[1] = std::min(mc_fp32 & 7, 4);
   return build_chunks(c, chunk);
 }
 

@@ -133,7 +133,12 @@ def make_samples(nocc, nvirt, seed, nstates=6, tol=1e-6, S=2048, rs=None):
             if len(idx) < S:
                 idx = np.concatenate([idx, rs.choice(N, size=S - len(idx), replace=True)])
             F = features(lam[k, i], h[idx], d0[idx], cls[idx])
-            out.append((F, t0[idx].astype(np.float32), tgt[idx].astype(np.float32)))
+            ts, es = t0[idx], tgt[idx]
+            nt, ne = np.linalg.norm(ts), np.linalg.norm(es)
+            if not (np.isfinite(nt) and nt > 0 and ne > 0):
+                continue
+            # the loss is scale invariant: normalise so FP32 sums cannot overflow
+            out.append((F, (ts / nt).astype(np.float32), (es / ne).astype(np.float32)))
     return out
 
 

@@ -194,9 +194,10 @@ def test_sigma_launch_shapes_agree(gpu, prec, tmp_path):
     tol = 1e-12 if prec == 0 else 5e-3
     for chunk in (16, 64, 256):
         for mc in (1, 2, 4):
-            assert lib().adcgpu_sigma_set_shape(g._h, chunk, mc, mc) == 0
-            y = g.sigma(x)
-            assert np.abs(y - ref).max() <= tol * np.abs(ref).max(), (chunk, mc)
+            for staged in (0, 8):
+                assert lib().adcgpu_sigma_set_shape(g._h, chunk, mc | staged, mc | staged) == 0
+                y = g.sigma(x)
+                assert np.abs(y - ref).max() <= tol * np.abs(ref).max(), (chunk, mc, staged)
     cache = str(tmp_path / "tune.json")
     r1 = autotune.tune(g, 5, prec, cache=cache)
     r2 = autotune.tune(g, 5, prec, cache=cache)
