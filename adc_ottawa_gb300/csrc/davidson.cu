@@ -511,7 +511,7 @@ int davidson_solve(Ctx* c, const adcgpu_dav_params* p, double* evals, double* ev
   if (p->precision == ADCGPU_MIXED) {
     if (c->precision != ADCGPU_MIXED) { dfree(c, out64, 0); return set_err(c, ADCGPU_BAD_INPUT, "matrix was not built for MIXED"); }
     const double tol_b = p->tol_bf16 == 0.0 ? 1e-2 : p->tol_bf16;
-    const double tol_f = p->tol_fp32 == 0.0 ? 3e-6 : p->tol_fp32;
+    const double tol_f = p->tol_fp32 == 0.0 ? 1e-5 : p->tol_fp32;
     float* g32 = nullptr;
     ST(dmalloc(c, (void**)&g32, sizeof(float) * (size_t)N * blocksize));
     int nguess = 0;
@@ -537,11 +537,9 @@ int davidson_solve(Ctx* c, const adcgpu_dav_params* p, double* evals, double* ev
     ST(dmalloc(c, (void**)&g64, sizeof(double) * (size_t)N * blocksize));
     ST((convert<float, double>(c, g32, g64, (int64_t)N * nguess)));
     dfree(c, g32, 0);
-    // refinement block: the roots themselves (the warm start already spans
-    // them to ~tol_fp32), so every FP64 sigma column is a root correction
     DavidsonGPU<double> F;
-    F.c = c; F.N = N; F.nstates = nstates; F.blocksize = nstates;
-    F.maxvec = (p->refine > 1 ? p->refine : 4) * nstates;
+    F.c = c; F.N = N; F.nstates = nstates; F.blocksize = blocksize;
+    F.maxvec = (p->refine > 1 ? p->refine : 4) * blocksize;
     F.niter = p->maxiter; F.ipre = precon64;
     F.ldeflate = p->ldfl != 0; F.tol = p->davtol; F.hii = c->d_diag;
     int it2 = 0, nc2 = 0, nout = 0;

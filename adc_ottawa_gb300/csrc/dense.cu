@@ -20,6 +20,11 @@ constexpr int TN_ROWS = 32;     // rows staged per step
 constexpr int TN_P = 64, TN_Q = 32;   // output tile
 
 // Partial C tiles: part[(blk * ntile + tile) * TN_P * TN_Q + ...]
+// Block: a range of rows; output tile TN_P x TN_Q (64 x 32); thread -> 8
+// outputs (p = ti + 16 u, q = tj + 16 v), conflict-free shared-memory reads.
+// Products over one 32-row step are summed in T and added to TA accumulators
+// (FP64 for FP32 inputs: one FP64 add per 32 FP32 FMAs keeps the Rayleigh and
+// Gram matrices accurate to ~1e-7 over millions of rows).
 template <typename T, typename TA>
 __global__ void __launch_bounds__(256) k_gemm_tn_part(int64_t N, int p, int q, const T* __restrict__ A,
                                                       int64_t lda, const T* __restrict__ B, int64_t ldb,
@@ -31,11 +36,7 @@ __global__ void __launch_bounds__(256) k_gemm_tn_part(int64_t N, int p, int q, c
   const int tp = tile / ntq, tq = tile % ntq;
   const int p0 = tp * TN_P, q0 = tq * TN_Q;
   const int tid = threadIdx.x;
-  // thread -> 8 outputs: rows i = (tid % 16) + 16*u (u<4), cols j = (tid / 16) + 16*v (v<2)
   const int ti = tid & 15, tj = tid >> 4;
-  // Products are accumulated in T over one 32-row step and the step sums in
-  // TA (FP64 for FP32 inputs: one FP64 add per 32 FP32 FMAs keeps the
-  // Rayleigh and Gram matrices accurate to ~1e-7 over millions of rows).
   TA acc[4][2];
 #pragma unroll
   for (int u = 0; u < 4; ++u) { acc[u][0] = TA(0); acc[u][1] = TA(0); }
@@ -57,7 +58,7 @@ __global__ void __launch_bounds__(256) k_gemm_tn_part(int64_t N, int p, int q, c
     T st[4][2];
 #pragma unroll
     for (int u = 0; u < 4; ++u) { st[u][0] = T(0); st[u][1] = T(0); }
-#pragma unroll 4
+#pragma unroll 8
     for (int rr = 0; rr < TN_ROWS; ++rr) {
       T b0 = sB[rr][tj], b1 = sB[rr][tj + 16];
 #pragma unroll
@@ -93,37 +94,59 @@ __global__ void k_gemm_tn_reduce(int p, int q, int nblk, int ntile, const TA* __
   }
 }
 
-// C(N x q) = beta C + alpha A(N x p) B(p x q); B (p x q, ldb) staged in smem.
+// C(N x q) = beta C + alpha A(N x p) B(p x q).  Block tile 128 rows x 64
+// columns, K staged 16 at a time; thread micro tile 8 rows x 4 columns.
+constexpr int NN_M = 128, NN_N = 64, NN_K = 16;
 template <typename T, typename TB>
 __global__ void __launch_bounds__(256) k_gemm_nn(int64_t N, int p, int q, T alpha, const T* __restrict__ A,
                                                  int64_t lda, const TB* __restrict__ B, int ldb, T beta,
                                                  T* __restrict__ C, int64_t ldc) {
-  extern __shared__ unsigned char smem_raw[];
-  T* sB = reinterpret_cast<T*>(smem_raw);   // [p][q] column-major: sB[j*p + t]
-  for (int l = threadIdx.x; l < p * q; l += blockDim.x) {
-    int t = l % p, j = l / p;
-    sB[l] = (T)B[(int64_t)j * ldb + t];
+  __shared__ __align__(16) T sA[NN_K][NN_M];
+  __shared__ __align__(16) T sB[NN_K][NN_N];
+  const int tid = threadIdx.x;
+  const int tx = tid & 15, ty = tid >> 4;          // columns 4 tx.., rows 8 ty..
+  const int64_t m0 = (int64_t)blockIdx.x * NN_M;
+  const int n0 = blockIdx.y * NN_N;
+  T acc[8][4];
+#pragma unroll
+  for (int i = 0; i < 8; ++i)
+#pragma unroll
+    for (int j = 0; j < 4; ++j) acc[i][j] = T(0);
+  for (int k0 = 0; k0 < p; k0 += NN_K) {
+    __syncthreads();
+    for (int l = tid; l < NN_K * NN_M; l += 256) {
+      const int kk = l / NN_M, rr = l % NN_M;
+      const int64_t r = m0 + rr;
+      sA[kk][rr] = (r < N && k0 + kk < p) ? A[(int64_t)(k0 + kk) * lda + r] : T(0);
+    }
+    for (int l = tid; l < NN_K * NN_N; l += 256) {
+      const int kk = l / NN_N, cc = l % NN_N;
+      sB[kk][cc] = (k0 + kk < p && n0 + cc < q) ? (T)B[(int64_t)(n0 + cc) * ldb + k0 + kk] : T(0);
+    }
+    __syncthreads();
+#pragma unroll
+    for (int kk = 0; kk < NN_K; ++kk) {
+      T a[8], b[4];
+#pragma unroll
+      for (int i = 0; i < 8; ++i) a[i] = sA[kk][8 * ty + i];
+#pragma unroll
+      for (int j = 0; j < 4; ++j) b[j] = sB[kk][4 * tx + j];
+#pragma unroll
+      for (int i = 0; i < 8; ++i)
+#pragma unroll
+        for (int j = 0; j < 4; ++j) acc[i][j] += a[i] * b[j];
+    }
   }
-  __syncthreads();
-  constexpr int JC = 8;
-  for (int64_t r = blockIdx.x * (int64_t)blockDim.x + threadIdx.x; r < N; r += (int64_t)gridDim.x * blockDim.x) {
-    for (int j0 = 0; j0 < q; j0 += JC) {
-      T acc[JC];
 #pragma unroll
-      for (int jj = 0; jj < JC; ++jj) acc[jj] = T(0);
-      for (int t = 0; t < p; ++t) {
-        T a = A[(int64_t)t * lda + r];
+  for (int j = 0; j < 4; ++j) {
+    const int col = n0 + 4 * tx + j;
+    if (col >= q) continue;
 #pragma unroll
-        for (int jj = 0; jj < JC; ++jj)
-          if (j0 + jj < q) acc[jj] += a * sB[(j0 + jj) * p + t];
-      }
-#pragma unroll
-      for (int jj = 0; jj < JC; ++jj) {
-        int j = j0 + jj;
-        if (j < q) {
-          T prev = beta == T(0) ? T(0) : beta * C[(int64_t)j * ldc + r];
-          C[(int64_t)j * ldc + r] = prev + alpha * acc[jj];
-        }
+    for (int i = 0; i < 8; ++i) {
+      const int64_t r = m0 + 8 * ty + i;
+      if (r < N) {
+        T prev = beta == T(0) ? T(0) : beta * C[(int64_t)col * ldc + r];
+        C[(int64_t)col * ldc + r] = prev + alpha * acc[i][j];
       }
     }
   }
@@ -277,13 +300,8 @@ int gemm_nn(Ctx* c, int64_t N, int p, int q, T alpha, const T* A, int64_t lda, c
     }
     return ADCGPU_OK;
   }
-  size_t smem = sizeof(T) * (size_t)p * q;
-  if (smem > 200 * 1024) return set_err(c, ADCGPU_UNSUPPORTED, "gemm_nn: small operand exceeds shared memory");
-  auto kern = k_gemm_nn<T, TB>;
-  ADC_CUDA(c, cudaFuncSetAttribute(kern, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem));
-  int64_t nb = (N + 255) / 256;
-  int grid = (int)std::min<int64_t>(nb, 152 * 8);
-  kern<<<grid, 256, smem, c->stream>>>(N, p, q, alpha, A, lda, B, ldb, beta, C, ldc);
+  dim3 grid((unsigned)((N + NN_M - 1) / NN_M), (unsigned)((q + NN_N - 1) / NN_N));
+  k_gemm_nn<T, TB><<<grid, 256, 0, c->stream>>>(N, p, q, alpha, A, lda, B, ldb, beta, C, ldc);
   ADC_CUDA(c, cudaGetLastError());
   return ADCGPU_OK;
 }

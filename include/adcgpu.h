@@ -172,7 +172,7 @@ typedef struct {
   double tol_bf16;   /* MIXED: residual at which the BF16-valued phase hands
                         over to the FP32-valued phase (0: 1e-2; <0: skip)    */
   double tol_fp32;   /* MIXED: residual at which the FP32 phase hands over to
-                        the FP64 refinement (0: 3e-6)                        */
+                        the FP64 refinement (0: 1e-5)                        */
 } adcgpu_dav_params;
 
 typedef struct {
