@@ -805,3 +805,122 @@ int sigma_fp32(Ctx* c, int m, const float* dV, int64_t ldv, float* dW, int64_t l
 }
 
 }  // namespace adcgpu
+
+// ---------------------------------------------------------------------------
+// Allocation-free sigma product.
+//
+// Some callers must not allocate device memory while they run: a host
+// application that gives the library a device-memory budget up front and
+// needs it not to grow in the middle of a solve (another library, or the
+// host's own caching allocator, already owns the rest of the device), and a
+// host thread that must not stall on the allocator (cudaFree waits for the
+// whole device to go idle).  adcgpu_sigma_device grows a context-owned FP64
+// accumulator on demand, so it may call cudaMalloc.  This variant uses a
+// statically sized device array instead and calls no allocating routine.
+// Its first call on a device does a one-time address lookup (below), so it
+// should come before any stream capture.
+//
+// The array belongs to the library image: every device that loads the
+// library holds it until the process exits, and all calls share it, so the
+// product of one call must not overlap another call on the GPU (calls on
+// one stream, or separated by synchronisation, are safe; concurrent calls
+// race).  Its contents persist between calls; the part a call uses is zeroed
+// at the start of that call.
+// ---------------------------------------------------------------------------
+namespace adcgpu {
+
+constexpr size_t NOALLOC_ACC_DOUBLES = size_t(1) << 20;   // 8 MiB: n1 * m <= 1,048,576
+static __device__ __align__(256) double g_noalloc_acc[NOALLOC_ACC_DOUBLES];
+
+namespace {
+
+// Device address of g_noalloc_acc, looked up once per device with that device
+// current (the host-side symbol is only a stand-in, never a device address).
+double* noalloc_scratch(Ctx* c) {
+  static double* ptrs[64] = {nullptr};
+  if (c->device < 0 || c->device >= 64) return nullptr;
+  if (!ptrs[c->device]) {
+    void* p = nullptr;
+    if (cudaGetSymbolAddress(&p, g_noalloc_acc) != cudaSuccess) {
+      cudaGetLastError();
+      return nullptr;
+    }
+    ptrs[c->device] = reinterpret_cast<double*>(p);
+  }
+  return ptrs[c->device];
+}
+
+template <typename TV>
+int sigma_fp32_with_acc(Ctx* c, int m, const float* dV, int64_t ldv, float* dW, int64_t ldw, const TV* Bt,
+                        double* acc) {
+  typedef float T;
+  typedef double TAcc;
+  const Geometry& G = c->geom;
+  const int n1 = (int)G.n1;
+  cudaStream_t s = c->stream;
+  GeomDev g = to_dev(G);
+  const float* A = c->d_A32;
+  const float* diag = c->d_diag32;
+  dim3 gs((n1 + 63) / 64, (m + 3) / 4);
+  k_singles<T><<<gs, 256, 0, s>>>(n1, A, diag, dV, ldv, dW, ldw, m);
+  ADC_CUDA(c, cudaGetLastError());
+  SigmaPlan* plan = reinterpret_cast<SigmaPlan*>(c->sigma_plan);
+  if (!plan) return set_err(c, ADCGPU_NO_MATRIX, "sigma plan missing");
+  const int2* chunks = plan->d_chunks;
+  const int2* items = plan->d_items;
+  ADC_CUDA(c, cudaMemsetAsync(acc, 0, sizeof(double) * (size_t)n1 * m, s));
+  int c0 = 0;
+  while (c0 < m) {
+    const int left = m - c0;
+    const T* V = dV + (int64_t)c0 * ldv;
+    T* W = dW + (int64_t)c0 * ldw;
+    TAcc* W1 = acc + (int64_t)c0 * n1;
+    const int64_t ld1 = (int64_t)n1;
+    const int cap = plan->mc_cap[1];
+    const int mc = (left >= 4 && cap >= 4) ? 4 : ((left >= 2 && cap >= 2) ? 2 : 1);
+    const int g1 = std::min(plan->nchunks, 152 * 4 * 16) / 4 + 1;
+    const int g2 = std::min(plan->nitems, 152 * 8 * 8) / 8 + 1;
+#define NA_P2(MC, GS) \
+  k_sigma_p2<T, TV, TAcc, MC, GS><<<g2, 256, 0, s>>>(g, items, plan->nitems, Bt, V, ldv, W, ldw, W1, ld1);
+#define NA_LAUNCH(MC)                                                                                           \
+  k_sigma_p1<T, TV, TAcc, MC><<<g1, 128, 0, s>>>(g, chunks, plan->nchunks, Bt, diag, V, ldv, W, ldw, W1, ld1); \
+  if (plan->nitems) {                                                                                           \
+    if (G.noP <= 8) { NA_P2(MC, 1) } else if (G.noP <= 16) { NA_P2(MC, 2) } else { NA_P2(MC, 4) }             \
+  }
+    if (mc == 4) { NA_LAUNCH(4) } else if (mc == 2) { NA_LAUNCH(2) } else { NA_LAUNCH(1) }
+#undef NA_LAUNCH
+#undef NA_P2
+    ADC_CUDA(c, cudaGetLastError());
+    c0 += mc;
+  }
+  k_w1_finalize<<<(n1 * m + 255) / 256, 256, 0, s>>>(n1, m, acc, dW, ldw);
+  ADC_CUDA(c, cudaGetLastError());
+  return ADCGPU_OK;
+}
+
+}  // namespace
+}  // namespace adcgpu
+
+extern "C" int adcgpu_sigma_device_noalloc(adcgpu_ctx* h, int m, const void* dv, void* dw, int64_t ld) {
+  using namespace adcgpu;
+  Ctx* c = reinterpret_cast<Ctx*>(h);
+  if (!c) return ADCGPU_BAD_INPUT;
+  if (cudaSetDevice(c->device) != cudaSuccess) { cudaGetLastError(); return ADCGPU_CUDA_ERROR; }
+  if (!c->have_matrix) return set_err(c, ADCGPU_NO_MATRIX, "no matrix");
+  if (c->precision != ADCGPU_MIXED)
+    return set_err(c, ADCGPU_UNSUPPORTED, "sigma_device_noalloc needs a matrix built with ADCGPU_MIXED");
+  if (m <= 0 || ld < c->geom.N || !dv || !dw) return set_err(c, ADCGPU_BAD_INPUT, "sigma arguments");
+  if ((size_t)c->geom.n1 * (size_t)m > NOALLOC_ACC_DOUBLES)
+    return set_err(c, ADCGPU_BAD_INPUT,
+                   "sigma_device_noalloc: nocc*nvirt*m exceeds the 1,048,576-entry static scratch; "
+                   "use fewer columns per call");
+  double* acc = noalloc_scratch(c);
+  if (!acc) return set_err(c, ADCGPU_CUDA_ERROR, "cudaGetSymbolAddress of the static scratch failed");
+  int st = c->mixed_bf16
+               ? sigma_fp32_with_acc<__nv_bfloat16>(c, m, (const float*)dv, ld, (float*)dw, ld,
+                                                    (const __nv_bfloat16*)c->d_Bt16, acc)
+               : sigma_fp32_with_acc<float>(c, m, (const float*)dv, ld, (float*)dw, ld, c->d_Bt32, acc);
+  if (st) return st;
+  ADC_CUDA(c, cudaStreamSynchronize(c->stream));
+  return ADCGPU_OK;
+}

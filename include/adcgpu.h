@@ -296,6 +296,20 @@ int64_t adcgpu_device_bytes(const adcgpu_ctx* ctx);
    reset != 0 clears the counters after reading. */
 int adcgpu_sigma_stats(adcgpu_ctx* ctx, double* out4, int reset);
 
+/* Allocation-free sigma product on device buffers, for callers that must
+   not allocate device memory while they run: a host application whose
+   device-memory budget is fixed in advance (the rest of the device belongs
+   to another library or allocator), or a host thread that must not stall on
+   cudaFree's device-wide wait.  No counterpart in the reference.  Same arguments and results as adcgpu_sigma_device for a matrix
+   built with ADCGPU_MIXED (float buffers); instead of a context-owned,
+   on-demand-allocated accumulator it uses a static device array of
+   1,048,576 doubles (8 MiB, held by every device that loads the library
+   until the process exits), so nocc*nvirt*m must not exceed 1,048,576
+   (ADCGPU_BAD_INPUT otherwise).  The first call on a device looks up the
+   array's device address; make that first call before any stream capture.
+   All calls share the array: calls that overlap on the GPU race. */
+int adcgpu_sigma_device_noalloc(adcgpu_ctx* ctx, int m, const void* dv, void* dw, int64_t ld);
+
 /* Autotuner of the sigma kernels' launch shape: pass-1 rows per warp work
    item (16..256) and vector columns per pass (1, 2, 4), timed with CUDA
    events for m columns on the built matrix; the fastest shape is kept in the
