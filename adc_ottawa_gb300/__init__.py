@@ -4,6 +4,6 @@ The compute lives in libadcgpu.so (csrc/, C ABI in include/adcgpu.h);
 this package is its host-side mirror (api.py) and build recipe (build.py).
 """
 from .api import (  # noqa: F401
-    ADCGPU_FP64, ADCGPU_MIXED, PRECON_DPR, PRECON_MLP, PRECON_OLSEN, AdcGpu, AdcGpuError, adc2s_dim,
+    ADCGPU_FP64, ADCGPU_MIXED, PRECON_DPR, PRECON_FOLD, PRECON_MLP, PRECON_OLSEN, AdcGpu, AdcGpuError, adc2s_dim,
     eri_packed_size, select_adc2s, synth_eri_packed, synth_orbitals, synth_system, synth_uniform_block,
 )

@@ -75,6 +75,7 @@ SIGNATURES = {
     "adcgpu_sigma": (C.c_int, [_vp, C.c_int, _dp, _dp]),
     "adcgpu_sigma_device": (C.c_int, [_vp, C.c_int, _vp, _vp, C.c_int64]),
     "adcgpu_sigma_device_noalloc": (C.c_int, [_vp, C.c_int, _vp, _vp, C.c_int64]),
+    "adcgpu_kernel_launches": (C.c_uint64, []),
     "adcgpu_davidson": (C.c_int, [_vp, C.POINTER(DavParams), _dp, _dp, C.POINTER(DavInfo)]),
     "adcgpu_write_davidson_file": (C.c_int, [C.c_char_p, C.c_int, C.c_int, _dp, _dp]),
     "adcgpu_block_lanczos": (C.c_int, [_vp, C.c_int, C.c_int, C.c_int, _dp, _dp, _dp, _dp]),

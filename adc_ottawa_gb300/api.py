@@ -23,7 +23,7 @@ from ._native import DavInfo, DavParams, SilState, lib, ptr
 
 ADCGPU_FP64 = 0
 ADCGPU_MIXED = 1
-PRECON_DPR, PRECON_OLSEN, PRECON_MLP = 1, 2, 3
+PRECON_DPR, PRECON_OLSEN, PRECON_MLP, PRECON_FOLD = 1, 2, 3, 4
 
 STATUS = {
     0: "ok", 1: "Illegal integration order", 2: "Stepsize underflow", 3: "Diagonalisation failed",

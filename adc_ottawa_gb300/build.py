@@ -32,6 +32,7 @@ SOURCES = [
     ("build_kernels.cu", ["--fmad=false"]),
     ("sigma.cu", []),
     ("dense.cu", []),
+    ("precond_fold.cu", []),
     ("davidson.cu", []),
     ("lanczos.cu", []),
     ("sil.cu", []),

@@ -9,6 +9,8 @@
 
 namespace adcgpu {
 
+std::atomic<unsigned long long> g_kernel_launches{0};
+
 int set_err(Ctx* c, int code, const std::string& msg) {
   if (c) c->err = msg;
   return code;
@@ -385,5 +387,7 @@ int64_t adcgpu_device_bytes(const adcgpu_ctx* h) {
   const Ctx* c = reinterpret_cast<const Ctx*>(h);
   return c ? c->dev_bytes : 0;
 }
+
+uint64_t adcgpu_kernel_launches(void) { return adcgpu::g_kernel_launches.load(); }
 
 }  // extern "C"

@@ -52,10 +52,10 @@ __global__ void k_fill_random_f(float* x, int64_t n, uint64_t seed) {
 
 template <typename T> void fill_random(Ctx* c, T* x, int64_t n, uint64_t seed);
 template <> void fill_random<double>(Ctx* c, double* x, int64_t n, uint64_t seed) {
-  k_fill_random<<<152 * 4, 256, 0, c->stream>>>(x, n, seed);
+  k_fill_random<<<152 * 4, 256, 0, c->stream>>>(x, n, seed); ADC_COUNT_LAUNCH();
 }
 template <> void fill_random<float>(Ctx* c, float* x, int64_t n, uint64_t seed) {
-  k_fill_random_f<<<152 * 4, 256, 0, c->stream>>>(x, n, seed);
+  k_fill_random_f<<<152 * 4, 256, 0, c->stream>>>(x, n, seed); ADC_COUNT_LAUNCH();
 }
 
 template <typename T> int sigma_t(Ctx* c, int m, const T* V, int64_t ldv, T* W, int64_t ldw);
@@ -72,11 +72,6 @@ double now_s() {
 
 }  // namespace
 
-#define ST(x)                 \
-  do {                        \
-    int _s = (x);             \
-    if (_s) return _s;        \
-  } while (0)
 
 template <typename T>
 struct DavidsonGPU {
@@ -341,6 +336,9 @@ struct DavidsonGPU {
       T* Tb = col(V, ilast);
       if (ipre == ADCGPU_PRECON_OLSEN) {
         ST((precond_olsen<T, T>(c, ws, N, bs_curr, X, R, N, d_lam, hii, Tb, N, nullptr)));
+      } else if (ipre == ADCGPU_PRECON_FOLD) {
+        ST((precond_fold<T>(c, ws, N, bs_curr, R, N, d_lam, hii, Tb, N, Tmp, N)));
+        nmult += bs_curr;   // the folding sigma product
       } else if (ipre == ADCGPU_PRECON_MLP && c->mlp) {
         MlpPrecond none;
         ST(mlp_apply(c, mlp ? *mlp : none, N, bs_curr, R, X, d_lam, hii, Tb));
@@ -453,7 +451,7 @@ int DavidsonGPU<T>::guess_subdiag(const std::vector<double>& hdiag, int subdim) 
   ST(dmalloc(c, (void**)&d_H, sizeof(double) * (size_t)subdim * subdim));
   ADC_CUDA(c, cudaMemcpyAsync(d_sub, sub.data(), sizeof(int64_t) * subdim, cudaMemcpyHostToDevice, c->stream));
   k_gather_sub<<<152 * 4, 256, 0, c->stream>>>(to_dev(c->geom), c->d_A, c->d_Bt, nullptr, d_sub,
-                                               subdim, d_H);
+                                               subdim, d_H); ADC_COUNT_LAUNCH();
   std::vector<double> H((size_t)subdim * subdim), w(subdim), Vs((size_t)subdim * subdim);
   ADC_CUDA(c, cudaMemcpyAsync(H.data(), d_H, sizeof(double) * H.size(), cudaMemcpyDeviceToHost, c->stream));
   ADC_CUDA(c, cudaStreamSynchronize(c->stream));
@@ -511,7 +509,7 @@ int davidson_solve(Ctx* c, const adcgpu_dav_params* p, double* evals, double* ev
   if (p->precision == ADCGPU_MIXED) {
     if (c->precision != ADCGPU_MIXED) { dfree(c, out64, 0); return set_err(c, ADCGPU_BAD_INPUT, "matrix was not built for MIXED"); }
     const double tol_b = p->tol_bf16 == 0.0 ? 1e-2 : p->tol_bf16;
-    const double tol_f = p->tol_fp32 == 0.0 ? 1e-5 : p->tol_fp32;
+    const double tol_f = p->tol_fp32 == 0.0 ? 5e-6 : p->tol_fp32;
     float* g32 = nullptr;
     ST(dmalloc(c, (void**)&g32, sizeof(float) * (size_t)N * blocksize));
     int nguess = 0;

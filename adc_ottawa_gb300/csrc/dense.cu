@@ -282,9 +282,9 @@ int gemm_tn(Ctx* c, Workspace& ws, int64_t N, int p, int q, const T* A, int64_t 
   size_t need = sizeof(TA) * (size_t)nblk * ntile * TN_P * TN_Q;
   int st = ws.reserve(c, need);
   if (st) return st;
-  k_gemm_tn_part<T, TA><<<dim3(nblk, ntile), 256, 0, c->stream>>>(N, p, q, A, lda, B, ldb, (TA*)ws.p, rows);
+  k_gemm_tn_part<T, TA><<<dim3(nblk, ntile), 256, 0, c->stream>>>(N, p, q, A, lda, B, ldb, (TA*)ws.p, rows); ADC_COUNT_LAUNCH();
   k_gemm_tn_reduce<TA, TC><<<(p * q + 255) / 256, 256, 0, c->stream>>>(p, q, nblk, ntile, (TA*)ws.p, C, ldc,
-                                                                       alpha, beta);
+                                                                       alpha, beta); ADC_COUNT_LAUNCH();
   ADC_CUDA(c, cudaGetLastError());
   return ADCGPU_OK;
 }
@@ -301,7 +301,7 @@ int gemm_nn(Ctx* c, int64_t N, int p, int q, T alpha, const T* A, int64_t lda, c
     return ADCGPU_OK;
   }
   dim3 grid((unsigned)((N + NN_M - 1) / NN_M), (unsigned)((q + NN_N - 1) / NN_N));
-  k_gemm_nn<T, TB><<<grid, 256, 0, c->stream>>>(N, p, q, alpha, A, lda, B, ldb, beta, C, ldc);
+  k_gemm_nn<T, TB><<<grid, 256, 0, c->stream>>>(N, p, q, alpha, A, lda, B, ldb, beta, C, ldc); ADC_COUNT_LAUNCH();
   ADC_CUDA(c, cudaGetLastError());
   return ADCGPU_OK;
 }
@@ -309,7 +309,7 @@ int gemm_nn(Ctx* c, int64_t N, int p, int q, T alpha, const T* A, int64_t lda, c
 template <typename T, typename TD>
 int precond_dpr(Ctx* c, int64_t N, int nb, const T* R, int64_t ldr, const double* d_lam, const TD* hii, T* Tout,
                 int64_t ldt) {
-  k_dpr<T, TD><<<152 * 8, 256, 0, c->stream>>>(N, nb, R, ldr, d_lam, hii, Tout, ldt);
+  k_dpr<T, TD><<<152 * 8, 256, 0, c->stream>>>(N, nb, R, ldr, d_lam, hii, Tout, ldt); ADC_COUNT_LAUNCH();
   ADC_CUDA(c, cudaGetLastError());
   return ADCGPU_OK;
 }
@@ -322,15 +322,15 @@ int precond_olsen(Ctx* c, Workspace& ws, int64_t N, int nb, const T* X, const T*
   if (st) return st;
   double* part = (double*)ws.p;
   double* sums = part + (size_t)nblk * nb * 2;
-  k_olsen_dots<T, TD><<<nblk, 256, 0, c->stream>>>(N, nb, X, R, ld, d_lam, hii, part);
-  k_sum_parts<<<(2 * nb + 127) / 128, 128, 0, c->stream>>>(nblk, 2 * nb, 2 * nb, part, sums);
+  k_olsen_dots<T, TD><<<nblk, 256, 0, c->stream>>>(N, nb, X, R, ld, d_lam, hii, part); ADC_COUNT_LAUNCH();
+  k_sum_parts<<<(2 * nb + 127) / 128, 128, 0, c->stream>>>(nblk, 2 * nb, 2 * nb, part, sums); ADC_COUNT_LAUNCH();
   std::vector<double> h(2 * nb), alpha(nb);
   ADC_CUDA(c, cudaMemcpyAsync(h.data(), sums, sizeof(double) * 2 * nb, cudaMemcpyDeviceToHost, c->stream));
   ADC_CUDA(c, cudaStreamSynchronize(c->stream));
   for (int i = 0; i < nb; ++i) alpha[i] = h[2 * i + 1] == 0.0 ? 0.0 : h[2 * i] / h[2 * i + 1];
   double* d_alpha = sums + 2 * nb;
   ADC_CUDA(c, cudaMemcpyAsync(d_alpha, alpha.data(), sizeof(double) * nb, cudaMemcpyHostToDevice, c->stream));
-  k_olsen_apply<T, TD><<<152 * 8, 256, 0, c->stream>>>(N, nb, X, R, ld, d_lam, d_alpha, hii, Tout, ldt);
+  k_olsen_apply<T, TD><<<152 * 8, 256, 0, c->stream>>>(N, nb, X, R, ld, d_lam, d_alpha, hii, Tout, ldt); ADC_COUNT_LAUNCH();
   ADC_CUDA(c, cudaGetLastError());
   if (h_alpha_out) std::copy(alpha.begin(), alpha.end(), h_alpha_out);
   ADC_CUDA(c, cudaStreamSynchronize(c->stream));
@@ -345,8 +345,8 @@ int residuals(Ctx* c, Workspace& ws, int64_t N, int nb, const T* X, const T* WY,
   if (st) return st;
   double* part = (double*)ws.p;
   double* sums = part + (size_t)nblk * nb;
-  k_resid<T><<<nblk, 256, 0, c->stream>>>(N, nb, X, WY, ld, d_lam, Rout, part);
-  k_sum_parts<<<(nb + 127) / 128, 128, 0, c->stream>>>(nblk, nb, nb, part, sums);
+  k_resid<T><<<nblk, 256, 0, c->stream>>>(N, nb, X, WY, ld, d_lam, Rout, part); ADC_COUNT_LAUNCH();
+  k_sum_parts<<<(nb + 127) / 128, 128, 0, c->stream>>>(nblk, nb, nb, part, sums); ADC_COUNT_LAUNCH();
   ADC_CUDA(c, cudaGetLastError());
   ADC_CUDA(c, cudaMemcpyAsync(h_norm2, sums, sizeof(double) * nb, cudaMemcpyDeviceToHost, c->stream));
   ADC_CUDA(c, cudaStreamSynchronize(c->stream));
@@ -355,7 +355,7 @@ int residuals(Ctx* c, Workspace& ws, int64_t N, int nb, const T* X, const T* WY,
 
 template <typename TS, typename TD>
 int convert(Ctx* c, const TS* x, TD* y, int64_t n) {
-  k_convert<TS, TD><<<152 * 8, 256, 0, c->stream>>>(x, y, n);
+  k_convert<TS, TD><<<152 * 8, 256, 0, c->stream>>>(x, y, n); ADC_COUNT_LAUNCH();
   ADC_CUDA(c, cudaGetLastError());
   return ADCGPU_OK;
 }

@@ -33,6 +33,12 @@ template <typename T, typename TD>
 int precond_olsen(Ctx* c, Workspace& ws, int64_t N, int nb, const T* X, const T* R, int64_t ld, const double* d_lam,
                   const TD* hii, T* Tout, int64_t ldt, double* h_alpha_out);
 
+// Folded singles-block preconditioner (precond_fold.cu): Tout = correction of
+// the residual block R; Z (N x nb) is scratch.
+template <typename T>
+int precond_fold(Ctx* c, Workspace& ws, int64_t N, int nb, const T* R, int64_t ldr, const double* d_lam,
+                 const T* hii, T* Tout, int64_t ldt, T* Z, int64_t ldz);
+
 // Rout = lambda X - WY (column-wise); h_norm2 receives ||Rout_i||^2 (FP64 sums).
 template <typename T>
 int residuals(Ctx* c, Workspace& ws, int64_t N, int nb, const T* X, const T* WY, int64_t ld, const double* d_lam,

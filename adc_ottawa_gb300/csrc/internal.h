@@ -40,6 +40,7 @@
 
 #include <cuda_runtime.h>
 #include <stdint.h>
+#include <atomic>
 #include <string>
 #include <vector>
 
@@ -247,8 +248,19 @@ struct Ctx {
   int64_t sil_cap = 0;
 };
 
+// Process-wide count of kernels this library has launched (every launch
+// site is followed by ADC_COUNT_LAUNCH); read with adcgpu_kernel_launches.
+extern std::atomic<unsigned long long> g_kernel_launches;
+#define ADC_COUNT_LAUNCH() ::adcgpu::g_kernel_launches.fetch_add(1, std::memory_order_relaxed)
+
 // error helpers
 int set_err(Ctx* c, int code, const std::string& msg);
+// propagate a non-zero status
+#define ST(x)                 \
+  do {                        \
+    int _s = (x);             \
+    if (_s) return _s;        \
+  } while (0)
 #define ADC_CUDA(ctx, call)                                                     \
   do {                                                                         \
     cudaError_t _e = (call);                                                   \

@@ -51,11 +51,6 @@ __global__ void k_scale_cols(int64_t N, int ncol, double* __restrict__ X, int64_
 
 }  // namespace
 
-#define ST(x)                 \
-  do {                        \
-    int _s = (x);             \
-    if (_s) return _s;        \
-  } while (0)
 
 struct LanczosGPU {
   Ctx* c;
@@ -72,7 +67,7 @@ struct LanczosGPU {
 
   int colnorms(double* X, int ncol, std::vector<double>& out) {
     const int nblk = 152 * 2;
-    k_colnorm2_part<<<nblk, 256, 0, c->stream>>>(N, ncol, X, N, d_part);
+    k_colnorm2_part<<<nblk, 256, 0, c->stream>>>(N, ncol, X, N, d_part); ADC_COUNT_LAUNCH();
     std::vector<double> part((size_t)nblk * ncol);
     ADC_CUDA(c, cudaMemcpyAsync(part.data(), d_part, sizeof(double) * part.size(), cudaMemcpyDeviceToHost, c->stream));
     ADC_CUDA(c, cudaStreamSynchronize(c->stream));
@@ -85,7 +80,7 @@ struct LanczosGPU {
 
   int scale_cols(double* X, int ncol, const std::vector<double>& s) {
     ADC_CUDA(c, cudaMemcpyAsync(d_s2, s.data(), sizeof(double) * ncol, cudaMemcpyHostToDevice, c->stream));
-    k_scale_cols<<<152 * 4, 256, 0, c->stream>>>(N, ncol, X, N, d_s2);
+    k_scale_cols<<<152 * 4, 256, 0, c->stream>>>(N, ncol, X, N, d_s2); ADC_COUNT_LAUNCH();
     ADC_CUDA(c, cudaGetLastError());
     return ADCGPU_OK;
   }
@@ -296,7 +291,7 @@ struct LanczosGPU {
         double* d_sc = nullptr;
         ST(dmalloc(c, (void**)&d_sc, sizeof(double) * nvec));
         ADC_CUDA(c, cudaMemcpyAsync(d_sc, nr.data(), sizeof(double) * nvec, cudaMemcpyHostToDevice, c->stream));
-        k_scale_cols<<<152 * 4, 256, 0, c->stream>>>(N, nvec, d_R, N, d_sc);
+        k_scale_cols<<<152 * 4, 256, 0, c->stream>>>(N, nvec, d_R, N, d_sc); ADC_COUNT_LAUNCH();
         ADC_CUDA(c, cudaMemcpyAsync(ritz_out, d_R, sizeof(double) * (size_t)N * nvec, cudaMemcpyDeviceToHost, c->stream));
         ADC_CUDA(c, cudaStreamSynchronize(c->stream));
         dfree(c, d_E, 0);

@@ -572,7 +572,7 @@ int sigma_impl(Ctx* c, int m, const T* dV, int64_t ldv, T* dW, int64_t ldw, cons
   GeomDev g = to_dev(G);
   // singles block first (plain stores), then the coupling adds atomically
   dim3 gs((n1 + 63) / 64, (m + 3) / 4);
-  k_singles<T><<<gs, 256, 0, s>>>(n1, A, diag, dV, ldv, dW, ldw, m);
+  k_singles<T><<<gs, 256, 0, s>>>(n1, A, diag, dV, ldv, dW, ldw, m); ADC_COUNT_LAUNCH();
   ADC_CUDA(c, cudaGetLastError());
   SigmaPlan* plan = reinterpret_cast<SigmaPlan*>(c->sigma_plan);
   if (!plan) return set_err(c, ADCGPU_NO_MATRIX, "sigma plan missing");
@@ -608,30 +608,30 @@ int sigma_impl(Ctx* c, int m, const T* dV, int64_t ldv, T* dW, int64_t ldw, cons
     const int g1 = std::min(plan->nchunks, 152 * 4 * 16) / 4 + 1;   // 4 warps per block
     const int g2 = std::min(plan->nitems, 152 * 8 * 8) / 8 + 1;
 #define LAUNCH_P2(MC, GS) \
-  k_sigma_p2<T, TV, TAcc, MC, GS><<<g2, 256, 0, s>>>(g, items, plan->nitems, Bt, V, ldv, W, ldw, W1, ld1);
+  k_sigma_p2<T, TV, TAcc, MC, GS><<<g2, 256, 0, s>>>(g, items, plan->nitems, Bt, V, ldv, W, ldw, W1, ld1); ADC_COUNT_LAUNCH();
 #define LAUNCH(MC)                                                                                              \
   if (plan->staged) {                                                                                           \
     constexpr int NS = sizeof(TV) == 2 ? 8 : 4;                                                                 \
     const size_t smem = (size_t)4 * NS * (32 * 16 * sizeof(TV) + 16 * MC);                                    \
     auto kern = k_sigma_p1s<T, TV, TAcc, MC, NS>;                                                               \
     ADC_CUDA(c, cudaFuncSetAttribute(kern, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem));            \
-    kern<<<g1, 128, smem, s>>>(g, chunks, plan->nchunks, Bt, diag, V, ldv, W, ldw, W1, ld1);                   \
+    kern<<<g1, 128, smem, s>>>(g, chunks, plan->nchunks, Bt, diag, V, ldv, W, ldw, W1, ld1); ADC_COUNT_LAUNCH();                   \
   } else {                                                                                                      \
-    k_sigma_p1<T, TV, TAcc, MC><<<g1, 128, 0, s>>>(g, chunks, plan->nchunks, Bt, diag, V, ldv, W, ldw, W1, ld1); \
+    k_sigma_p1<T, TV, TAcc, MC><<<g1, 128, 0, s>>>(g, chunks, plan->nchunks, Bt, diag, V, ldv, W, ldw, W1, ld1); ADC_COUNT_LAUNCH(); \
   }                                                                                                             \
   if (plan->nitems) {                                                                                           \
     if (G.noP <= 8) { LAUNCH_P2(MC, 1) } else if (G.noP <= 16) { LAUNCH_P2(MC, 2) } else { LAUNCH_P2(MC, 4) }   \
   }
     if (mc == 4) { LAUNCH(4) } else if (mc == 2) { LAUNCH(2) } else { LAUNCH(1) }
 #undef LAUNCH
-#undef LAUNCH_P2_NT
-#undef LAUNCH
+#undef LAUNCH_P2
     ADC_CUDA(c, cudaGetLastError());
     c0 += mc;
   }
-  if (sizeof(T) == 4)
+  if (sizeof(T) == 4) {
     k_w1_finalize<<<(n1 * m + 255) / 256, 256, 0, s>>>(n1, m, reinterpret_cast<const double*>(W1base),
-                                                       reinterpret_cast<float*>(dW), ldw);
+                                                       reinterpret_cast<float*>(dW), ldw); ADC_COUNT_LAUNCH();
+  }
   ADC_CUDA(c, cudaEventRecord(c->st_ev1, s));
   c->st_pending = true;
   c->st_pending_cols = m;
@@ -707,10 +707,10 @@ int prepare_mixed(Ctx* c) {
   if (!c->d_diag32 && (st = dmalloc(c, (void**)&c->d_diag32, sizeof(float) * G.N))) return st;
   if (!c->d_Bt16 && (st = dmalloc(c, (void**)&c->d_Bt16, sizeof(uint16_t) * G.off[5]))) return st;
   if (!c->d_Bt32 && (st = dmalloc(c, (void**)&c->d_Bt32, sizeof(float) * G.off[5]))) return st;
-  k_to_f32<<<152 * 8, 256, 0, c->stream>>>(c->d_A, c->d_A32, G.n1 * G.n1);
-  k_to_f32<<<152 * 8, 256, 0, c->stream>>>(c->d_diag, c->d_diag32, G.N);
-  k_to_bf16<<<152 * 8, 256, 0, c->stream>>>(c->d_Bt, (__nv_bfloat16*)c->d_Bt16, G.off[5]);
-  k_to_f32<<<152 * 8, 256, 0, c->stream>>>(c->d_Bt, c->d_Bt32, G.off[5]);
+  k_to_f32<<<152 * 8, 256, 0, c->stream>>>(c->d_A, c->d_A32, G.n1 * G.n1); ADC_COUNT_LAUNCH();
+  k_to_f32<<<152 * 8, 256, 0, c->stream>>>(c->d_diag, c->d_diag32, G.N); ADC_COUNT_LAUNCH();
+  k_to_bf16<<<152 * 8, 256, 0, c->stream>>>(c->d_Bt, (__nv_bfloat16*)c->d_Bt16, G.off[5]); ADC_COUNT_LAUNCH();
+  k_to_f32<<<152 * 8, 256, 0, c->stream>>>(c->d_Bt, c->d_Bt32, G.off[5]); ADC_COUNT_LAUNCH();
   ADC_CUDA(c, cudaGetLastError());
   return ADCGPU_OK;
 }
@@ -797,6 +797,24 @@ int sigma_fp64(Ctx* c, int m, const double* dV, int64_t ldv, double* dW, int64_t
   return sigma_impl<double, double>(c, m, dV, ldv, dW, ldw, c->d_A, c->d_diag, c->d_Bt);
 }
 
+// W = Hss V for the dense singles block alone (diag1 + A), m columns of n1
+// rows: the inner product of the folded preconditioner's MINRES solve.
+int singles_block_product(Ctx* c, int m, const double* V, int64_t ldv, double* W, int64_t ldw) {
+  const int n1 = (int)c->geom.n1;
+  k_singles<double><<<dim3((n1 + 63) / 64, (m + 3) / 4), 256, 0, c->stream>>>(n1, c->d_A, c->d_diag, V, ldv, W, ldw,
+                                                                              m); ADC_COUNT_LAUNCH();
+  ADC_CUDA(c, cudaGetLastError());
+  return ADCGPU_OK;
+}
+int singles_block_product(Ctx* c, int m, const float* V, int64_t ldv, float* W, int64_t ldw) {
+  const int n1 = (int)c->geom.n1;
+  if (!c->d_A32 || !c->d_diag32) return set_err(c, ADCGPU_NO_MATRIX, "FP32 singles block missing");
+  k_singles<float><<<dim3((n1 + 63) / 64, (m + 3) / 4), 256, 0, c->stream>>>(n1, c->d_A32, c->d_diag32, V, ldv, W,
+                                                                             ldw, m); ADC_COUNT_LAUNCH();
+  ADC_CUDA(c, cudaGetLastError());
+  return ADCGPU_OK;
+}
+
 int sigma_fp32(Ctx* c, int m, const float* dV, int64_t ldv, float* dW, int64_t ldw) {
   if (c->mixed_bf16)
     return sigma_impl<float, __nv_bfloat16>(c, m, dV, ldv, dW, ldw, c->d_A32, c->d_diag32,
@@ -862,7 +880,7 @@ int sigma_fp32_with_acc(Ctx* c, int m, const float* dV, int64_t ldv, float* dW, 
   const float* A = c->d_A32;
   const float* diag = c->d_diag32;
   dim3 gs((n1 + 63) / 64, (m + 3) / 4);
-  k_singles<T><<<gs, 256, 0, s>>>(n1, A, diag, dV, ldv, dW, ldw, m);
+  k_singles<T><<<gs, 256, 0, s>>>(n1, A, diag, dV, ldv, dW, ldw, m); ADC_COUNT_LAUNCH();
   ADC_CUDA(c, cudaGetLastError());
   SigmaPlan* plan = reinterpret_cast<SigmaPlan*>(c->sigma_plan);
   if (!plan) return set_err(c, ADCGPU_NO_MATRIX, "sigma plan missing");
@@ -881,9 +899,9 @@ int sigma_fp32_with_acc(Ctx* c, int m, const float* dV, int64_t ldv, float* dW, 
     const int g1 = std::min(plan->nchunks, 152 * 4 * 16) / 4 + 1;
     const int g2 = std::min(plan->nitems, 152 * 8 * 8) / 8 + 1;
 #define NA_P2(MC, GS) \
-  k_sigma_p2<T, TV, TAcc, MC, GS><<<g2, 256, 0, s>>>(g, items, plan->nitems, Bt, V, ldv, W, ldw, W1, ld1);
+  k_sigma_p2<T, TV, TAcc, MC, GS><<<g2, 256, 0, s>>>(g, items, plan->nitems, Bt, V, ldv, W, ldw, W1, ld1); ADC_COUNT_LAUNCH();
 #define NA_LAUNCH(MC)                                                                                           \
-  k_sigma_p1<T, TV, TAcc, MC><<<g1, 128, 0, s>>>(g, chunks, plan->nchunks, Bt, diag, V, ldv, W, ldw, W1, ld1); \
+  k_sigma_p1<T, TV, TAcc, MC><<<g1, 128, 0, s>>>(g, chunks, plan->nchunks, Bt, diag, V, ldv, W, ldw, W1, ld1); ADC_COUNT_LAUNCH(); \
   if (plan->nitems) {                                                                                           \
     if (G.noP <= 8) { NA_P2(MC, 1) } else if (G.noP <= 16) { NA_P2(MC, 2) } else { NA_P2(MC, 4) }             \
   }
@@ -893,7 +911,7 @@ int sigma_fp32_with_acc(Ctx* c, int m, const float* dV, int64_t ldv, float* dW, 
     ADC_CUDA(c, cudaGetLastError());
     c0 += mc;
   }
-  k_w1_finalize<<<(n1 * m + 255) / 256, 256, 0, s>>>(n1, m, acc, dW, ldw);
+  k_w1_finalize<<<(n1 * m + 255) / 256, 256, 0, s>>>(n1, m, acc, dW, ldw); ADC_COUNT_LAUNCH();
   ADC_CUDA(c, cudaGetLastError());
   return ADCGPU_OK;
 }

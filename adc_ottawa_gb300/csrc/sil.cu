@@ -168,11 +168,6 @@ __global__ void k_csquare(int64_t N, int P, const double* __restrict__ Psi, doub
 
 }  // namespace
 
-#define ST(x)                 \
-  do {                        \
-    int _s = (x);             \
-    if (_s) return _s;        \
-  } while (0)
 
 // Per-packet SILStep state (host side).
 struct SilPacket {
@@ -228,7 +223,7 @@ struct SilEngine {
   int minus_i_H(const double* X, double* Y, const std::vector<int>& mask) {
     ST(sigma_fp64(c, 2 * P, X, N, Y, N));
     ST(set_mask(mask));
-    k_minus_i<<<152 * 4, 256, 0, c->stream>>>(N, P, Y, d_mask);
+    k_minus_i<<<152 * 4, 256, 0, c->stream>>>(N, P, Y, d_mask); ADC_COUNT_LAUNCH();
     ADC_CUDA(c, cudaGetLastError());
     int na = 0;
     for (int v : mask) na += v;
@@ -238,7 +233,7 @@ struct SilEngine {
 
   int cdots(const double* X, const double* Y, const std::vector<int>& mask, std::vector<cplx>& out) {
     ST(set_mask(mask));
-    k_cdot<<<SIL_BLK, 256, 0, c->stream>>>(N, P, X, Y, d_mask, d_part);
+    k_cdot<<<SIL_BLK, 256, 0, c->stream>>>(N, P, X, Y, d_mask, d_part); ADC_COUNT_LAUNCH();
     std::vector<double> h((size_t)SIL_BLK * P * 2);
     ADC_CUDA(c, cudaMemcpyAsync(h.data(), d_part, sizeof(double) * h.size(), cudaMemcpyDeviceToHost, c->stream));
     ADC_CUDA(c, cudaStreamSynchronize(c->stream));
@@ -261,7 +256,7 @@ struct SilEngine {
     }
     ADC_CUDA(c, cudaMemcpyAsync(d_coef, coef.data(), sizeof(double) * coef.size(), cudaMemcpyHostToDevice, c->stream));
     ST(set_mask(mask));
-    k_recur<<<SIL_BLK, 256, 0, c->stream>>>(N, P, Kn, K1, K2, d_coef, d_mask, d_part);
+    k_recur<<<SIL_BLK, 256, 0, c->stream>>>(N, P, Kn, K1, K2, d_coef, d_mask, d_part); ADC_COUNT_LAUNCH();
     std::vector<double> h((size_t)SIL_BLK * P);
     ADC_CUDA(c, cudaMemcpyAsync(h.data(), d_part, sizeof(double) * h.size(), cudaMemcpyDeviceToHost, c->stream));
     ADC_CUDA(c, cudaStreamSynchronize(c->stream));
@@ -278,7 +273,7 @@ struct SilEngine {
     for (int p = 0; p < P; ++p) { coef[2 * p] = s[p].real(); coef[2 * p + 1] = s[p].imag(); }
     ADC_CUDA(c, cudaMemcpyAsync(d_coef, coef.data(), sizeof(double) * coef.size(), cudaMemcpyHostToDevice, c->stream));
     ST(set_mask(mask));
-    k_cscale<<<152 * 4, 256, 0, c->stream>>>(N, P, Kn, d_coef, d_mask);
+    k_cscale<<<152 * 4, 256, 0, c->stream>>>(N, P, Kn, d_coef, d_mask); ADC_COUNT_LAUNCH();
     ADC_CUDA(c, cudaGetLastError());
     return ADCGPU_OK;
   }
@@ -393,14 +388,14 @@ struct SilEngine {
     ADC_CUDA(c, cudaMemcpyAsync(d_coef, coef.data(), sizeof(double) * coef.size(), cudaMemcpyHostToDevice, c->stream));
     ADC_CUDA(c, cudaMemcpyAsync(d_order, ordv.data(), sizeof(int) * P, cudaMemcpyHostToDevice, c->stream));
     ST(set_mask(pmask));
-    k_combine<<<152 * 4, 256, 0, c->stream>>>(N, P, Psi, d_kptr, d_coef, d_order, kdim, d_mask);
+    k_combine<<<152 * 4, 256, 0, c->stream>>>(N, P, Psi, d_kptr, d_coef, d_order, kdim, d_mask); ADC_COUNT_LAUNCH();
     ADC_CUDA(c, cudaGetLastError());
     (void)maxord;
     return ADCGPU_OK;
   }
 
   int csquare(std::vector<cplx>& out) {
-    k_csquare<<<SIL_BLK, 256, 0, c->stream>>>(N, P, Psi, d_part);
+    k_csquare<<<SIL_BLK, 256, 0, c->stream>>>(N, P, Psi, d_part); ADC_COUNT_LAUNCH();
     std::vector<double> h((size_t)SIL_BLK * P * 2);
     ADC_CUDA(c, cudaMemcpyAsync(h.data(), d_part, sizeof(double) * h.size(), cudaMemcpyDeviceToHost, c->stream));
     ADC_CUDA(c, cudaStreamSynchronize(c->stream));

@@ -187,6 +187,9 @@ def run_gb300(args):
         r = g.davdiag_block(NROOTS, TOL, **kw)
     barrier(world)
     g.sigma_stats(reset=True)
+    from adc_ottawa_gb300._native import lib
+
+    launches0 = int(lib().adcgpu_kernel_launches())
     clk = ClockSampler(local)
     clk.start()
     times, results = [], []
@@ -198,6 +201,7 @@ def run_gb300(args):
         results.append(r)
     barrier(world)
     clocks = clk.stop()
+    launches = int(lib().adcgpu_kernel_launches()) - launches0
     stats = g.sigma_stats(reset=True)
     t_step = allmax(statistics.mean(times), world)
     r = results[-1]
@@ -261,7 +265,7 @@ def run_gb300(args):
         "clocks": clocks,
         "e2e": e2e,
         "cpu_baseline": cpu,
-        "gpu_launches": None,
+        "gpu_launches": launches,
     }
     if rank == 0:
         print(json.dumps(line), flush=True)

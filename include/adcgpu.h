@@ -60,7 +60,12 @@ enum adcgpu_precision {
 enum adcgpu_precon {
   ADCGPU_PRECON_DPR = 1,    /* dpr   block_davidson.f90:1288-1342 */
   ADCGPU_PRECON_OLSEN = 2,  /* olsen block_davidson.f90:1346-1419 */
-  ADCGPU_PRECON_MLP = 3     /* learned correction, DPR as fallback */
+  ADCGPU_PRECON_MLP = 3,    /* learned correction, DPR as fallback */
+  ADCGPU_PRECON_FOLD = 4    /* singles block with the doubles residual folded
+                               in (no reference counterpart): t_d = DPR,
+                               t_s = (lambda - Hss)^-1 (r_s + B^T t_d) by 8
+                               MINRES steps; one extra sigma product of the
+                               block per iteration */
 };
 
 typedef struct adcgpu_ctx adcgpu_ctx;
@@ -172,7 +177,7 @@ typedef struct {
   double tol_bf16;   /* MIXED: residual at which the BF16-valued phase hands
                         over to the FP32-valued phase (0: 1e-2; <0: skip)    */
   double tol_fp32;   /* MIXED: residual at which the FP32 phase hands over to
-                        the FP64 refinement (0: 1e-5)                        */
+                        the FP64 refinement (0: 5e-6)                        */
 } adcgpu_dav_params;
 
 typedef struct {
@@ -287,6 +292,11 @@ double adcgpu_last_sigma_ms(const adcgpu_ctx* ctx);
 
 /* Device bytes held by the context (matrix, ERI blocks, work spaces). */
 int64_t adcgpu_device_bytes(const adcgpu_ctx* ctx);
+
+/* Number of CUDA kernels this library has launched in this process, over
+   all contexts (a monotonic counter; differences give the launches of a
+   region). */
+uint64_t adcgpu_kernel_launches(void);
 
 /* Sigma-product statistics accumulated since the last reset, measured with
    CUDA events on the context's stream around every sigma call (including

@@ -61,6 +61,43 @@ def test_mixed_precision_davidson(gpu):
     assert np.abs(res.evals - w[:6]).max() < 1e-6
 
 
+@pytest.mark.parametrize("ldfl", [True, False])
+def test_fold_preconditioner_fp64(cfg1, ldfl):
+    """The folded singles-block preconditioner converges to the oracle's
+    (DPR) eigenvalues within 1e-8 Ha, in fewer iterations than DPR."""
+    from adc_ottawa_gb300 import PRECON_FOLD
+
+    g, ref = cfg1
+    res = g.davdiag_block(6, 1e-8, precon=PRECON_FOLD, ldfl=ldfl)
+    dpr = g.davdiag_block(6, 1e-8, precon=1, ldfl=ldfl)
+    st, ev, _, _ = ref.davidson(6, 1e-8, precon=1, deflate=ldfl)
+    assert st == 0 and res.status == 0
+    assert np.abs(res.evals - ev).max() < 1e-8
+    H = ref.dense()
+    r = H @ res.evecs - res.evecs * res.evals
+    assert np.linalg.norm(r, axis=0).max() < 1e-7
+    assert res.iterations < dpr.iterations
+
+
+def test_fold_preconditioner_mixed(gpu):
+    """Mixed ladder with the folded preconditioner on a system whose upper
+    roots sit inside the doubles manifold: eigenvalues within 1e-6 Ha of
+    the oracle's FP64 Davidson and fewer iterations than with DPR."""
+    from adc_ottawa_gb300 import ADCGPU_MIXED, PRECON_FOLD
+
+    no, nv, seed = 6, 24, 77
+    g, e, eri = make(no, nv, seed, precision=ADCGPU_MIXED)
+    ref = oracle.Matrix.build(no, nv, e, eri)
+    st, w, _, _ = ref.davidson(12, 1e-9, precon=1)
+    assert st == 0
+    fold = g.davdiag_block(12, 1e-6, precision=ADCGPU_MIXED, precon=PRECON_FOLD)
+    dpr = g.davdiag_block(12, 1e-6, precision=ADCGPU_MIXED, precon=1)
+    assert fold.status == 0 and dpr.status == 0
+    assert np.abs(fold.evals - w[:12]).max() < 1e-6
+    assert fold.iterations < dpr.iterations
+    g.close()
+
+
 @pytest.mark.parametrize("orthotype", [0, 1])
 def test_lanczos_config1(cfg1, orthotype):
     g, ref = cfg1
