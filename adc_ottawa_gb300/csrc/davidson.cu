@@ -509,7 +509,9 @@ int davidson_solve(Ctx* c, const adcgpu_dav_params* p, double* evals, double* ev
   if (p->precision == ADCGPU_MIXED) {
     if (c->precision != ADCGPU_MIXED) { dfree(c, out64, 0); return set_err(c, ADCGPU_BAD_INPUT, "matrix was not built for MIXED"); }
     const double tol_b = p->tol_bf16 == 0.0 ? 1e-2 : p->tol_bf16;
-    const double tol_f = p->tol_fp32 == 0.0 ? 5e-6 : p->tol_fp32;
+    // the folded preconditioner makes FP64 iterations cheap and few, so it
+    // hands over earlier
+    const double tol_f = p->tol_fp32 != 0.0 ? p->tol_fp32 : (p->precon == ADCGPU_PRECON_FOLD ? 1e-5 : 5e-6);
     float* g32 = nullptr;
     ST(dmalloc(c, (void**)&g32, sizeof(float) * (size_t)N * blocksize));
     int nguess = 0;

@@ -34,7 +34,7 @@ int precond_olsen(Ctx* c, Workspace& ws, int64_t N, int nb, const T* X, const T*
                   const TD* hii, T* Tout, int64_t ldt, double* h_alpha_out);
 
 // Folded singles-block preconditioner (precond_fold.cu): Tout = correction of
-// the residual block R; Z (N x nb) is scratch.
+// the residual block R; Z (N x 2nb, leading dimension N) is scratch.
 template <typename T>
 int precond_fold(Ctx* c, Workspace& ws, int64_t N, int nb, const T* R, int64_t ldr, const double* d_lam,
                  const T* hii, T* Tout, int64_t ldt, T* Z, int64_t ldz);

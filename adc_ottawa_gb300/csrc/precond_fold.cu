@@ -161,11 +161,11 @@ int sigma_any(Ctx* c, int m, const float* V, int64_t ldv, float* W, int64_t ldw)
 
 }  // namespace
 
-// Tout (N x nb) = folded-singles-block correction of the residual block R.
-// Z (N x nb) is scratch; ws holds the MINRES vectors.
+namespace {
+
 template <typename T>
-int precond_fold(Ctx* c, Workspace& ws, int64_t N, int nb, const T* R, int64_t ldr, const double* d_lam,
-                 const T* hii, T* Tout, int64_t ldt, T* Z, int64_t ldz) {
+int fold_impl(Ctx* c, Workspace& ws, int64_t N, int nb, const T* R, int64_t ldr, const double* d_lam,
+              const T* hii, T* Tout, int64_t ldt, T* Z, int64_t ldz) {
   typedef T M;
   const int n1 = (int)c->geom.n1;
   if (nb <= 0) return ADCGPU_OK;
@@ -194,9 +194,38 @@ int precond_fold(Ctx* c, Workspace& ws, int64_t N, int nb, const T* R, int64_t l
   return ADCGPU_OK;
 }
 
-template int precond_fold<double>(Ctx*, Workspace&, int64_t, int, const double*, int64_t, const double*,
-                                  const double*, double*, int64_t, double*, int64_t);
-template int precond_fold<float>(Ctx*, Workspace&, int64_t, int, const float*, int64_t, const double*,
-                                 const float*, float*, int64_t, float*, int64_t);
+}  // namespace
+
+// Tout (N x nb) = folded-singles-block correction of the residual block R.
+// Z is scratch of at least 2 nb columns of N values; ws holds the MINRES
+// vectors.  On a matrix built for ADCGPU_MIXED the fold always runs with FP32
+// vectors and the BF16 matrix values, also inside the FP64 refinement: the
+// preconditioner only shapes the search direction, and the FP64 residual
+// still decides convergence.
+template <>
+int precond_fold<float>(Ctx* c, Workspace& ws, int64_t N, int nb, const float* R, int64_t ldr, const double* d_lam,
+                        const float* hii, float* Tout, int64_t ldt, float* Z, int64_t ldz) {
+  const int save = c->mixed_bf16;
+  c->mixed_bf16 = c->d_Bt16 ? 1 : 0;
+  const int st = fold_impl<float>(c, ws, N, nb, R, ldr, d_lam, hii, Tout, ldt, Z, ldz);
+  c->mixed_bf16 = save;
+  return st;
+}
+
+template <>
+int precond_fold<double>(Ctx* c, Workspace& ws, int64_t N, int nb, const double* R, int64_t ldr,
+                         const double* d_lam, const double* hii, double* Tout, int64_t ldt, double* Z, int64_t ldz) {
+  // the FP32 route carves three float blocks (R, T, Z) = 1.5 nb doubles per
+  // row out of Z
+  if (c->precision == ADCGPU_MIXED && c->d_Bt16 && c->d_A32 && c->d_diag32 && ldr == N && ldt == N && ldz == N) {
+    float* Rf = reinterpret_cast<float*>(Z);
+    float* Tf = Rf + (size_t)N * nb;
+    float* Zf = Tf + (size_t)N * nb;
+    ST((convert<double, float>(c, R, Rf, N * nb)));
+    ST(precond_fold<float>(c, ws, N, nb, Rf, N, d_lam, c->d_diag32, Tf, N, Zf, N));
+    return convert<float, double>(c, Tf, Tout, N * nb);
+  }
+  return fold_impl<double>(c, ws, N, nb, R, ldr, d_lam, hii, Tout, ldt, Z, ldz);
+}
 
 }  // namespace adcgpu

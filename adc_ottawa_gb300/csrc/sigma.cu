@@ -635,10 +635,13 @@ int sigma_impl(Ctx* c, int m, const T* dV, int64_t ldv, T* dW, int64_t ldw, cons
   ADC_CUDA(c, cudaEventRecord(c->st_ev1, s));
   c->st_pending = true;
   c->st_pending_cols = m;
-  // algorithmic bytes: every stored value once, A once, diagonal once,
-  // V read and W written once
-  c->st_pending_bytes = (double)G.off[5] * sizeof(TV) + (double)G.n1 * G.n1 * sizeof(T) +
-                        (double)G.N * sizeof(T) + 2.0 * (double)m * G.N * sizeof(T);
+  // algorithmic bytes of one sparse product of m columns, counted as for a
+  // CSR matrix: every kept coupling value once with a 4-byte column index,
+  // the dense singles block as n1^2 values, n1+1 row pointers, the FP64
+  // diagonal, V read and W written once.  The index-free layout here reads
+  // no indices (and the zero padding of its segments instead).
+  c->st_pending_bytes = (double)(c->nnz_kept - c->nnz_ph) * (sizeof(TV) + 4) + (double)G.n1 * G.n1 * sizeof(TV) +
+                        4.0 * (double)(G.n1 + 1) + 8.0 * (double)G.N + 2.0 * (double)m * G.N * sizeof(T);
   return ADCGPU_OK;
 }
 

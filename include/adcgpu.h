@@ -177,7 +177,8 @@ typedef struct {
   double tol_bf16;   /* MIXED: residual at which the BF16-valued phase hands
                         over to the FP32-valued phase (0: 1e-2; <0: skip)    */
   double tol_fp32;   /* MIXED: residual at which the FP32 phase hands over to
-                        the FP64 refinement (0: 5e-6)                        */
+                        the FP64 refinement (0: 1e-5 with ADCGPU_PRECON_FOLD,
+                        5e-6 otherwise)                                      */
 } adcgpu_dav_params;
 
 typedef struct {
@@ -301,8 +302,10 @@ uint64_t adcgpu_kernel_launches(void);
 /* Sigma-product statistics accumulated since the last reset, measured with
    CUDA events on the context's stream around every sigma call (including
    those inside the solvers): out[0] calls, out[1] total device milliseconds,
-   out[2] algorithmic bytes (each stored matrix value read once per call,
-   diagonal, vectors read and written once), out[3] columns multiplied.
+   out[2] algorithmic bytes (per call: each kept coupling value once with a
+   4-byte column index, the dense singles block as nocc^2 nvirt^2 values,
+   nocc*nvirt+1 row pointers, the FP64 diagonal, the m vectors read and
+   written once), out[3] columns multiplied.
    reset != 0 clears the counters after reading. */
 int adcgpu_sigma_stats(adcgpu_ctx* ctx, double* out4, int reset);
 
