@@ -9,6 +9,9 @@
 //
 // Reductions over N are two-pass (per-block partials, then a fixed-order
 // sum), so results do not depend on scheduling.
+#include <algorithm>
+#include <type_traits>
+
 #include "internal.h"
 #include "dense.h"
 
@@ -79,18 +82,108 @@ __global__ void __launch_bounds__(256) k_gemm_tn_part(int64_t N, int p, int q, c
   }
 }
 
+// Threads walk the partial tiles in their stored order (jj fastest), so the
+// nblk reads of consecutive threads are contiguous.
 template <typename TA, typename TC>
 __global__ void k_gemm_tn_reduce(int p, int q, int nblk, int ntile, const TA* __restrict__ part,
                                  TC* __restrict__ C, int ldc, TC alpha, TC beta) {
   const int ntq = (q + TN_Q - 1) / TN_Q;
-  for (int o = blockIdx.x * blockDim.x + threadIdx.x; o < p * q; o += gridDim.x * blockDim.x) {
-    int i = o % p, j = o / p;
-    int tile = (i / TN_P) * ntq + (j / TN_Q);
-    int ii = i % TN_P, jj = j % TN_Q;
+  const int per_tile = TN_P * TN_Q;
+  for (int o = blockIdx.x * blockDim.x + threadIdx.x; o < ntile * per_tile; o += gridDim.x * blockDim.x) {
+    const int tile = o / per_tile, w = o - tile * per_tile;
+    const int ii = w / TN_Q, jj = w - ii * TN_Q;
+    const int i = (tile / ntq) * TN_P + ii, j = (tile % ntq) * TN_Q + jj;
+    if (i >= p || j >= q) continue;
     TA s = TA(0);
-    for (int b = 0; b < nblk; ++b) s += part[((int64_t)b * ntile + tile) * (TN_P * TN_Q) + ii * TN_Q + jj];
+    for (int b = 0; b < nblk; ++b) s += part[((int64_t)b * ntile + tile) * per_tile + w];
     TC prev = beta == TC(0) ? TC(0) : beta * C[(int64_t)j * ldc + i];
     C[(int64_t)j * ldc + i] = prev + alpha * (TC)s;
+  }
+}
+
+// ---------------------------------------------------------------------------
+// Double-float ("DF") arithmetic for FP64-accurate GEMMs on the FP32 pipe.
+// A double x is held as hi + lo with hi = fl32(x), lo = fl32(x - hi)
+// (48 significant bits).  A product of two such pairs is formed exactly in
+// its leading part with an FMA (Dekker's two-product) plus the two cross
+// terms; sums use Knuth's two-sum, so a step sum of 32 products carries
+// ~2^-44 relative error before it is added to an FP64 accumulator.  On GB300
+// the FP32 pipe issues 64 FMAs for every FP64 FMA, and one DF multiply-add
+// costs about 12 FP32 instructions.
+// ---------------------------------------------------------------------------
+struct df { float hi, lo; };
+
+__device__ __forceinline__ df df_split(double x) {
+  const float h = (float)x;
+  return df{h, (float)(x - (double)h)};
+}
+
+// s += a * b
+__device__ __forceinline__ void df_fma(df& s, df a, df b) {
+  const float p = a.hi * b.hi;
+  float e = fmaf(a.hi, b.hi, -p);
+  e = fmaf(a.hi, b.lo, e);
+  e = fmaf(a.lo, b.hi, e);
+  const float t = s.hi + p;
+  const float v = t - s.hi;
+  const float err = (s.hi - (t - v)) + (p - v);
+  s.lo += err + e;
+  s.hi = t;
+}
+
+__device__ __forceinline__ double df_value(df s) { return (double)s.hi + (double)s.lo; }
+
+// k_gemm_tn_part for FP64 inputs with DF step sums and FP64 accumulators.
+__global__ void __launch_bounds__(256) k_gemm_tn_part_df(int64_t N, int p, int q, const double* __restrict__ A,
+                                                         int64_t lda, const double* __restrict__ B, int64_t ldb,
+                                                         double* __restrict__ part, int64_t rows_per_blk) {
+  __shared__ df sA[TN_ROWS][TN_P + 1];
+  __shared__ df sB[TN_ROWS][TN_Q + 1];
+  const int ntq = (q + TN_Q - 1) / TN_Q;
+  const int tile = blockIdx.y;
+  const int tp = tile / ntq, tq = tile % ntq;
+  const int p0 = tp * TN_P, q0 = tq * TN_Q;
+  const int tid = threadIdx.x;
+  const int ti = tid & 15, tj = tid >> 4;
+  double acc[4][2];
+#pragma unroll
+  for (int u = 0; u < 4; ++u) { acc[u][0] = 0.0; acc[u][1] = 0.0; }
+  const int64_t r_begin = blockIdx.x * rows_per_blk;
+  const int64_t r_end = min(N, r_begin + rows_per_blk);
+  for (int64_t r0 = r_begin; r0 < r_end; r0 += TN_ROWS) {
+    __syncthreads();
+    for (int l = tid; l < TN_ROWS * TN_P; l += 256) {
+      int c = l / TN_ROWS, rr = l % TN_ROWS;
+      int64_t r = r0 + rr;
+      sA[rr][c] = df_split((r < r_end && p0 + c < p) ? A[(int64_t)(p0 + c) * lda + r] : 0.0);
+    }
+    for (int l = tid; l < TN_ROWS * TN_Q; l += 256) {
+      int c = l / TN_ROWS, rr = l % TN_ROWS;
+      int64_t r = r0 + rr;
+      sB[rr][c] = df_split((r < r_end && q0 + c < q) ? B[(int64_t)(q0 + c) * ldb + r] : 0.0);
+    }
+    __syncthreads();
+    df st[4][2];
+#pragma unroll
+    for (int u = 0; u < 4; ++u) { st[u][0] = df{0.f, 0.f}; st[u][1] = df{0.f, 0.f}; }
+#pragma unroll 4
+    for (int rr = 0; rr < TN_ROWS; ++rr) {
+      const df b0 = sB[rr][tj], b1 = sB[rr][tj + 16];
+#pragma unroll
+      for (int u = 0; u < 4; ++u) {
+        const df a = sA[rr][ti + 16 * u];
+        df_fma(st[u][0], a, b0);
+        df_fma(st[u][1], a, b1);
+      }
+    }
+#pragma unroll
+    for (int u = 0; u < 4; ++u) { acc[u][0] += df_value(st[u][0]); acc[u][1] += df_value(st[u][1]); }
+  }
+  double* out = part + ((int64_t)blockIdx.x * gridDim.y + tile) * (TN_P * TN_Q);
+#pragma unroll
+  for (int u = 0; u < 4; ++u) {
+    out[(ti + 16 * u) * TN_Q + tj] = acc[u][0];
+    out[(ti + 16 * u) * TN_Q + tj + 16] = acc[u][1];
   }
 }
 
@@ -146,6 +239,72 @@ __global__ void __launch_bounds__(256) k_gemm_nn(int64_t N, int p, int q, T alph
       const int64_t r = m0 + 8 * ty + i;
       if (r < N) {
         T prev = beta == T(0) ? T(0) : beta * C[(int64_t)col * ldc + r];
+        C[(int64_t)col * ldc + r] = prev + alpha * acc[i][j];
+      }
+    }
+  }
+}
+
+// k_gemm_nn for FP64 operands with DF products; the K sum is flushed to FP64
+// accumulators after every NN_K step.
+__global__ void __launch_bounds__(256) k_gemm_nn_df(int64_t N, int p, int q, double alpha,
+                                                    const double* __restrict__ A, int64_t lda,
+                                                    const double* __restrict__ B, int ldb, double beta,
+                                                    double* __restrict__ C, int64_t ldc) {
+  __shared__ df sA[NN_K][NN_M];
+  __shared__ df sB[NN_K][NN_N];
+  const int tid = threadIdx.x;
+  const int tx = tid & 15, ty = tid >> 4;
+  const int64_t m0 = (int64_t)blockIdx.x * NN_M;
+  const int n0 = blockIdx.y * NN_N;
+  double acc[8][4];
+#pragma unroll
+  for (int i = 0; i < 8; ++i)
+#pragma unroll
+    for (int j = 0; j < 4; ++j) acc[i][j] = 0.0;
+  for (int k0 = 0; k0 < p; k0 += NN_K) {
+    __syncthreads();
+    for (int l = tid; l < NN_K * NN_M; l += 256) {
+      const int kk = l / NN_M, rr = l % NN_M;
+      const int64_t r = m0 + rr;
+      sA[kk][rr] = df_split((r < N && k0 + kk < p) ? A[(int64_t)(k0 + kk) * lda + r] : 0.0);
+    }
+    for (int l = tid; l < NN_K * NN_N; l += 256) {
+      const int kk = l / NN_N, cc = l % NN_N;
+      sB[kk][cc] = df_split((k0 + kk < p && n0 + cc < q) ? B[(int64_t)(n0 + cc) * ldb + k0 + kk] : 0.0);
+    }
+    __syncthreads();
+    df st[8][4];
+#pragma unroll
+    for (int i = 0; i < 8; ++i)
+#pragma unroll
+      for (int j = 0; j < 4; ++j) st[i][j] = df{0.f, 0.f};
+#pragma unroll 2
+    for (int kk = 0; kk < NN_K; ++kk) {
+      df a[8], b[4];
+#pragma unroll
+      for (int i = 0; i < 8; ++i) a[i] = sA[kk][8 * ty + i];
+#pragma unroll
+      for (int j = 0; j < 4; ++j) b[j] = sB[kk][4 * tx + j];
+#pragma unroll
+      for (int i = 0; i < 8; ++i)
+#pragma unroll
+        for (int j = 0; j < 4; ++j) df_fma(st[i][j], a[i], b[j]);
+    }
+#pragma unroll
+    for (int i = 0; i < 8; ++i)
+#pragma unroll
+      for (int j = 0; j < 4; ++j) acc[i][j] += df_value(st[i][j]);
+  }
+#pragma unroll
+  for (int j = 0; j < 4; ++j) {
+    const int col = n0 + 4 * tx + j;
+    if (col >= q) continue;
+#pragma unroll
+    for (int i = 0; i < 8; ++i) {
+      const int64_t r = m0 + 8 * ty + i;
+      if (r < N) {
+        double prev = beta == 0.0 ? 0.0 : beta * C[(int64_t)col * ldc + r];
         C[(int64_t)col * ldc + r] = prev + alpha * acc[i][j];
       }
     }
@@ -282,9 +441,19 @@ int gemm_tn(Ctx* c, Workspace& ws, int64_t N, int p, int q, const T* A, int64_t 
   size_t need = sizeof(TA) * (size_t)nblk * ntile * TN_P * TN_Q;
   int st = ws.reserve(c, need);
   if (st) return st;
-  k_gemm_tn_part<T, TA><<<dim3(nblk, ntile), 256, 0, c->stream>>>(N, p, q, A, lda, B, ldb, (TA*)ws.p, rows); ADC_COUNT_LAUNCH();
-  k_gemm_tn_reduce<TA, TC><<<(p * q + 255) / 256, 256, 0, c->stream>>>(p, q, nblk, ntile, (TA*)ws.p, C, ldc,
-                                                                       alpha, beta); ADC_COUNT_LAUNCH();
+  if constexpr (std::is_same<T, double>::value && std::is_same<TA, double>::value) {
+    if (c->dense_df) {
+      k_gemm_tn_part_df<<<dim3(nblk, ntile), 256, 0, c->stream>>>(N, p, q, A, lda, B, ldb, (TA*)ws.p, rows); ADC_COUNT_LAUNCH();
+    } else {
+      k_gemm_tn_part<T, TA><<<dim3(nblk, ntile), 256, 0, c->stream>>>(N, p, q, A, lda, B, ldb, (TA*)ws.p, rows); ADC_COUNT_LAUNCH();
+    }
+  } else {
+    k_gemm_tn_part<T, TA><<<dim3(nblk, ntile), 256, 0, c->stream>>>(N, p, q, A, lda, B, ldb, (TA*)ws.p, rows); ADC_COUNT_LAUNCH();
+  }
+  const int nout = ntile * TN_P * TN_Q;
+  k_gemm_tn_reduce<TA, TC><<<std::min((nout + 255) / 256, 152 * 8), 256, 0, c->stream>>>(p, q, nblk, ntile,
+                                                                                         (TA*)ws.p, C, ldc, alpha,
+                                                                                         beta); ADC_COUNT_LAUNCH();
   ADC_CUDA(c, cudaGetLastError());
   return ADCGPU_OK;
 }
@@ -301,6 +470,13 @@ int gemm_nn(Ctx* c, int64_t N, int p, int q, T alpha, const T* A, int64_t lda, c
     return ADCGPU_OK;
   }
   dim3 grid((unsigned)((N + NN_M - 1) / NN_M), (unsigned)((q + NN_N - 1) / NN_N));
+  if constexpr (std::is_same<T, double>::value && std::is_same<TB, double>::value) {
+    if (c->dense_df) {
+      k_gemm_nn_df<<<grid, 256, 0, c->stream>>>(N, p, q, alpha, A, lda, B, ldb, beta, C, ldc); ADC_COUNT_LAUNCH();
+      ADC_CUDA(c, cudaGetLastError());
+      return ADCGPU_OK;
+    }
+  }
   k_gemm_nn<T, TB><<<grid, 256, 0, c->stream>>>(N, p, q, alpha, A, lda, B, ldb, beta, C, ldc); ADC_COUNT_LAUNCH();
   ADC_CUDA(c, cudaGetLastError());
   return ADCGPU_OK;

@@ -147,6 +147,63 @@ bool host_syev(int n, const double* A, int lda, double* w, double* V) {
   return true;
 }
 
+// Eigenvalues of a symmetric band matrix (bandwidth kd, the lower band of
+// column-major A is read), as dsbev('N') in diagmat_banded
+// (block_lanczos.f90:2006-2052): the band is reduced to tridiagonal form by
+// Givens rotations, one bandwidth at a time, each fill-in element chased
+// down the band (the band-reduction scheme of Rutishauser and Schwarz), in
+// O(n^2 kd) operations; the implicit QL iteration then gives the
+// eigenvalues in O(n^2).
+bool host_sbev_values(int n, int kd, const double* A, int lda, double* w) {
+  if (n <= 0) return true;
+  kd = std::max(0, std::min(kd, n - 1));
+  // row-major symmetric working copy of the band (+ one bulge diagonal)
+  std::vector<double> z((size_t)n * n, 0.0);
+  auto Z = [&](int i, int j) -> double& { return z[(size_t)i * n + j]; };
+  for (int j = 0; j < n; ++j)
+    for (int i = j; i < std::min(n, j + kd + 1); ++i) {
+      const double x = A[(size_t)j * lda + i];
+      Z(i, j) = x;
+      Z(j, i) = x;
+    }
+  for (int b = kd; b >= 2; --b) {
+    for (int j = 0; j + b < n; ++j) {
+      int p = j + b, col = j;
+      while (p < n) {
+        const double x = Z(p - 1, col), y = Z(p, col);
+        if (y != 0.0) {
+          const double r = std::hypot(x, y), c = x / r, s = y / r;
+          // rows/columns p-1 and p: A <- G A G^T, G = [[c, s], [-s, c]]
+          const int lo = std::max(0, p - 1 - b - 1), hi = std::min(n - 1, p + b + 1);
+          for (int k = lo; k <= hi; ++k) {
+            if (k == p - 1 || k == p) continue;
+            const double a1 = Z(p - 1, k), a2 = Z(p, k);
+            const double n1v = c * a1 + s * a2, n2v = -s * a1 + c * a2;
+            Z(p - 1, k) = n1v; Z(k, p - 1) = n1v;
+            Z(p, k) = n2v; Z(k, p) = n2v;
+          }
+          const double a11 = Z(p - 1, p - 1), a12 = Z(p - 1, p), a22 = Z(p, p);
+          Z(p - 1, p - 1) = c * c * a11 + 2.0 * c * s * a12 + s * s * a22;
+          Z(p, p) = s * s * a11 - 2.0 * c * s * a12 + c * c * a22;
+          const double o = c * s * (a22 - a11) + (c * c - s * s) * a12;
+          Z(p - 1, p) = o; Z(p, p - 1) = o;
+          Z(p, col) = 0.0; Z(col, p) = 0.0;
+        }
+        // the rotation fills (p + b, p - 1); chase it one band-width down
+        col = p - 1;
+        p += b;
+      }
+    }
+  }
+  std::vector<double> d(n), e(n, 0.0);
+  for (int i = 0; i < n; ++i) d[i] = Z(i, i);
+  for (int i = 1; i < n; ++i) e[i] = Z(i, i - 1);
+  if (!tql2(n, d, e, nullptr)) return false;
+  std::sort(d.begin(), d.end());
+  std::memcpy(w, d.data(), sizeof(double) * n);
+  return true;
+}
+
 int host_cholesky_upper(int n, const double* G, double* R, double rel_tol) {
   double dmax = 0.0;
   for (int i = 0; i < n; ++i) dmax = std::max(dmax, std::fabs(G[(size_t)i * n + i]));

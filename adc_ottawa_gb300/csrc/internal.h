@@ -225,6 +225,7 @@ struct Ctx {
   float* d_Bt32 = nullptr;        // fp32 B^T values (when bf16 is not safe)
   float* d_diag32 = nullptr;
   int mixed_bf16 = 1;             // 1: B^T stored as bf16, 0: fp32
+  int dense_df = 0;               // FP64 GEMMs in double-float on the FP32 pipe
   int64_t nnz_kept = 0;           // reference noffd
   int64_t nnz_ph = 0;             // kept ph-ph entries
   int64_t* d_rowcount = nullptr;  // kept entries per double row (for COO export)
@@ -305,6 +306,7 @@ void free_mlp(Ctx* c);
 // Symmetric eigen-decomposition (Householder tridiagonalisation + implicit QL).
 // A: n x n column-major (upper triangle used); w ascending; V eigenvectors.
 bool host_syev(int n, const double* A, int lda, double* w, double* V);
+bool host_sbev_values(int n, int kd, const double* A, int lda, double* w);
 // Cholesky of SPD G (n x n col-major) -> upper R with G = R^T R; returns the
 // first column whose pivot fell below rel_tol * max diag (or -1 on success).
 int host_cholesky_upper(int n, const double* G, double* R, double rel_tol);

@@ -253,7 +253,11 @@ struct LanczosGPU {
       }
     }
     if (tmat_out) std::memcpy(tmat_out, T.data(), sizeof(double) * T.size());
-    if (evals_out || ritz_out) {
+    if (evals_out && !ritz_out) {
+      // diagmat_banded with eigenvalues only: band reduction, O(nvec^2 b)
+      if (!host_sbev_values(nvec, b, T.data(), nvec, evals_out))
+        return set_err(c, ADCGPU_EIGEN_FAILED, "diagonalisation of the Lanczos T matrix failed");
+    } else if (evals_out || ritz_out) {
       // diagmat_banded: dsbev('V','L') on the lower band (kd = b)
       std::vector<double> Tb((size_t)nvec * nvec, 0.0), w(nvec), E;
       for (int cc = 0; cc < nvec; ++cc)

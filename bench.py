@@ -47,6 +47,11 @@ def parse():
     ap.add_argument("--no-fp64", action="store_true", help="skip the FP64 GPU comparison solve")
     ap.add_argument("--no-e2e", action="store_true")
     ap.add_argument("--no-cpu", action="store_true")
+    ap.add_argument("--suite", default="davidson", choices=["davidson", "lanczos", "sil", "batch"],
+                    help="davidson: the headline solve (default); lanczos: nocc=10/nvirt=110 block Lanczos, "
+                         "b=10, 300 cycles; sil: 32 wavepackets on the nocc=10/nvirt=110 matrix, Krylov dim 15, "
+                         "dt=0.05 au (--sil-steps steps timed); batch: 64 seeded systems, 8 roots each")
+    ap.add_argument("--sil-steps", type=int, default=20)
     return ap.parse_args()
 
 
@@ -312,9 +317,92 @@ def run_reference(args):
     print(json.dumps(line), flush=True)
 
 
+def _secondary_line(metric, value, unit, steps, warmup, config, **extra):
+    line = {"metric": metric, "value": value, "unit": unit, "n_gpus": 1, "steps": steps, "warmup": warmup,
+            "ms_per_step": value * 1e3 if unit == "s" else None, "higher_is_better": unit != "s",
+            "scaling": "weak", "vs_baseline": None, "dtype": "f64", "data": "synthetic", "config": config}
+    line.update(extra)
+    print(json.dumps(line), flush=True)
+
+
+def run_lanczos(args):
+    """Config 2 block Lanczos: b = 10 seeded uniform start vectors, 300 cycles
+    (nvec = 3000), FP64 throughout, T and its eigenvalues returned."""
+    from adc_ottawa_gb300 import ADCGPU_FP64, AdcGpu, synth_system, synth_uniform_block
+
+    no, nv, b, ncyc = 10, 110, 10, 300
+    e, eri = synth_system(no, nv, 2024)
+    g = AdcGpu(0)
+    g.set_orbitals(no, nv, e)
+    g.set_eri_packed(eri)
+    g.write_fspace_adc2_1(None, precision=ADCGPU_FP64)
+    q0 = synth_uniform_block(g.ndim, b, 99)
+    for _ in range(max(1, args.warmup)):
+        g.lancdiag_block(q0, ncyc, orthotype=0, want_tmat=False)
+    g.sigma_stats(reset=True)
+    times = []
+    for _ in range(args.steps):
+        t = time.perf_counter()
+        _, ev, _ = g.lancdiag_block(q0, ncyc, orthotype=0, want_tmat=False)
+        times.append(time.perf_counter() - t)
+    st = g.sigma_stats(reset=True)
+    _secondary_line("block Lanczos 300 cycles, b=10 (nvec 3000), FP64", statistics.mean(times), "s", args.steps,
+                    args.warmup, {"workload": f"ADC(2)-s nocc={no} nvirt={nv} N={g.ndim} lanczos b={b} ncycles={ncyc}"},
+                    sigma={"calls": st["calls"], "ms": st["ms"],
+                           "gbs": st["alg_bytes"] / max(st["ms"], 1e-9) / 1e6},
+                    lowest=ev[:3].tolist())
+    g.close()
+
+
+def run_sil(args):
+    """Config 4 SIL: 32 seeded wavepackets on the config-2 matrix, Krylov
+    dimension 15, dt = tout/2 = 0.05 au; --sil-steps outer steps are timed
+    and the 2,000-step figure is that rate times 2,000."""
+    from adc_ottawa_gb300 import ADCGPU_FP64, AdcGpu, synth_system, synth_uniform_block
+
+    no, nv, npk, kdim, tout = 10, 110, 32, 15, 0.1
+    e, eri = synth_system(no, nv, 2024)
+    g = AdcGpu(0)
+    g.set_orbitals(no, nv, e)
+    g.set_eri_packed(eri)
+    g.write_fspace_adc2_1(None, precision=ADCGPU_FP64)
+    f = synth_uniform_block(g.ndim, npk, 77)
+    g.propagate_fvec(f, tout, 2 * 0.5 * tout, kdim, 1e-8)
+    nsteps = max(1, args.sil_steps)
+    t = time.perf_counter()
+    a, nmult = g.propagate_fvec(f, tout, nsteps * 0.5 * tout, kdim, 1e-8)
+    dt = time.perf_counter() - t
+    _secondary_line("SIL autocorrelation, 32 wavepackets, kdim 15, dt 0.05 au: seconds per step", dt / nsteps, "s",
+                    nsteps, 1, {"workload": f"ADC(2)-s nocc={no} nvirt={nv} N={g.ndim} sil packets={npk}"},
+                    projected_2000_steps_s=dt / nsteps * 2000, matvec_columns=nmult,
+                    a_last=[float(abs(a[0, -1]))])
+    g.close()
+
+
+def run_batch(args):
+    """Config 4 batch: 64 seeded systems, nocc ~ U{4..12}, nvirt ~ U{30..120},
+    8 roots to 1e-6, mixed precision with the folded preconditioner, solved
+    concurrently (one stream per system)."""
+    from adc_ottawa_gb300 import PRECON_FOLD, batch
+
+    systems = batch.seeded_systems(64)
+    batch.solve_many(systems[:4], nroots=8, precon=PRECON_FOLD)
+    res, wall = batch.solve_many(systems, nroots=8, precon=PRECON_FOLD)
+    _secondary_line("64 systems x 8 roots to 1e-6 (mixed + fold), wall time", wall, "s", 1, 1,
+                    {"workload": "64 seeded ADC(2)-s systems, nocc U{4..12}, nvirt U{30..120}"},
+                    converged=sum(1 for r in res if r["status"] == 0),
+                    total_N=int(sum(r["N"] for r in res)))
+
+
 if __name__ == "__main__":
     a = parse()
     if a.impl == "reference":
         run_reference(a)
+    elif a.suite == "lanczos":
+        run_lanczos(a)
+    elif a.suite == "sil":
+        run_sil(a)
+    elif a.suite == "batch":
+        run_batch(a)
     else:
         run_gb300(a)
