@@ -507,6 +507,249 @@ __global__ void __launch_bounds__(256) k_sigma_p2(GeomDev g, const int2* __restr
   }
 }
 
+// 4 consecutive values from 16-byte aligned shared memory
+template <typename T> struct Vec4;
+template <> struct Vec4<float> {
+  __device__ __forceinline__ static void ld(const float* p, float (&v)[4]) {
+    const float4 q = *reinterpret_cast<const float4*>(p);
+    v[0] = q.x; v[1] = q.y; v[2] = q.z; v[3] = q.w;
+  }
+};
+template <> struct Vec4<double> {
+  __device__ __forceinline__ static void ld(const double* p, double (&v)[4]) {
+    const double2 q0 = reinterpret_cast<const double2*>(p)[0], q1 = reinterpret_cast<const double2*>(p)[1];
+    v[0] = q0.x; v[1] = q0.y; v[2] = q1.x; v[3] = q1.y;
+  }
+};
+
+// 8 values to 16-byte aligned shared memory as vector stores
+template <typename T> struct Store8;
+template <> struct Store8<float> {
+  __device__ __forceinline__ static void go(float* d, const float (&v)[8]) {
+    reinterpret_cast<float4*>(d)[0] = make_float4(v[0], v[1], v[2], v[3]);
+    reinterpret_cast<float4*>(d)[1] = make_float4(v[4], v[5], v[6], v[7]);
+  }
+};
+template <> struct Store8<double> {
+  __device__ __forceinline__ static void go(double* d, const double (&v)[8]) {
+#pragma unroll
+    for (int i = 0; i < 4; ++i) reinterpret_cast<double2*>(d)[i] = make_double2(v[2 * i], v[2 * i + 1]);
+  }
+};
+
+// ---------------------------------------------------------------------------
+// Tiled pass 1: one block per work item (up to TILE_ITEM_ROWS consecutive
+// rows of one slab), all MT columns of a column group at once, so the matrix
+// is streamed once per MT columns instead of once per MC.
+//
+// For a slab (fixed k', l') the C and D segments of its rows form a dense
+// rows x nvP block each, coupling to the fixed singles (a, k') and (a, l'):
+//   W2[r, c] += sum_a C[r, a] Xk[a, c] + D[r, a] Xl[a, c]     (Xk = V[(a,k'), c])
+//   W1[(a, k'), c] += sum_r C[r, a] V2[r, c]   (and D with l')
+// Xk and Xl stay in shared memory for the whole item; each 32-row tile of
+// C|D values is staged once and used for every column; the W1 sums of the
+// item accumulate in shared memory (in T, one 32-row tile at a time) and are
+// added to the TA accumulators of W1 once at the end of the item.
+// Segment A (singles (a', k)) is handled per tile: its W2 part gathers V
+// through L1, its W1 part is reduced over runs of equal a' and added
+// atomically.  Segment B stays with pass 2, as before.
+// Shared memory (bytes): T sW1[nseg*nvP*MT] | T sX[MT*(2nvP+4)] (column-major) |
+// T sCD[RT*(2nvP+4)] | T sA[RT*(noP+4)] | T sV2[RT*MT] | int64 sD[RT] | int sAp[RT]
+// (row strides are multiples of 16 bytes, so the staging stores are 16-byte
+// vector stores, and 4 rows read in one warp fall into different banks).
+// ---------------------------------------------------------------------------
+constexpr int TILE_RT = 32;
+constexpr int TILE_ITEM_ROWS = 1024;
+
+__host__ __device__ inline size_t align16(size_t x) { return (x + 15) / 16 * 16; }
+
+inline size_t tile_smem_bytes(int nvP, int noP, int MT, size_t sT) {
+  size_t b = align16((size_t)2 * nvP * MT * sT);
+  b += align16((size_t)MT * (2 * nvP + 4) * sT);
+  b += align16((size_t)TILE_RT * (2 * nvP + 4) * sT);
+  b += align16((size_t)TILE_RT * (noP + 4) * sT);
+  b += align16((size_t)TILE_RT * MT * sT);
+  b += align16((size_t)TILE_RT * 8);
+  b += align16((size_t)TILE_RT * 4);
+  return b;
+}
+
+template <typename T, typename TV, typename TA, int MT>
+__global__ void __launch_bounds__(256) k_sigma_tile(GeomDev g, const int2* __restrict__ titems, int ntitems,
+                                                    const TV* __restrict__ Bt, const T* __restrict__ diag,
+                                                    const T* __restrict__ V, int64_t ldv, int mcols,
+                                                    T* __restrict__ W, int64_t ldw, TA* __restrict__ W1,
+                                                    int64_t ld1) {
+  constexpr int RT = TILE_RT;
+  extern __shared__ __align__(16) unsigned char smem_raw[];
+  const int no = g.no, nv = g.nv, noP = g.noP, nvP = g.nvP;
+  const int64_t n1 = g.n1;
+  const int CDS = 2 * nvP + 4, AS = noP + 4, KP = 2 * nvP + 4;
+  unsigned char* p = smem_raw;
+  T* sW1 = reinterpret_cast<T*>(p); p += align16((size_t)2 * nvP * MT * sizeof(T));
+  T* sX = reinterpret_cast<T*>(p); p += align16((size_t)MT * (2 * nvP + 4) * sizeof(T));
+  T* sCD = reinterpret_cast<T*>(p); p += align16((size_t)RT * CDS * sizeof(T));
+  T* sA = reinterpret_cast<T*>(p); p += align16((size_t)RT * AS * sizeof(T));
+  T* sV2 = reinterpret_cast<T*>(p); p += align16((size_t)RT * MT * sizeof(T));
+  int64_t* sD = reinterpret_cast<int64_t*>(p); p += align16((size_t)RT * 8);
+  int* sAp = reinterpret_cast<int*>(p);
+  const int tid = threadIdx.x;
+  for (int it = blockIdx.x; it < ntitems; it += gridDim.x) {
+    const int2 item = titems[it];
+    const Double r0 = decode_row(g, item.x);
+    const int cls = r0.cls;
+    const bool twoa = (cls == 1 || cls >= 3);
+    const int nseg = cls >= 2 ? 2 : 1;
+    const int K = nseg * nvP;
+    const int64_t L = g.len[cls];
+    const int offC = twoa ? 2 * noP : noP;
+    const int kp = r0.kp, lp = r0.lp;
+    const TV* base = Bt + g.off[cls];   // row r starts at base + (r - start[cls]) * L
+    __syncthreads();
+    for (int o = tid; o < K * MT; o += 256) {
+      const int k = o % K, c = o / K;
+      const int seg = k / nvP, a = k - seg * nvP;
+      sX[c * KP + k] = (a < nv && c < mcols) ? V[(int64_t)c * ldv + (int64_t)a * no + (seg ? lp : kp)] : T(0);
+      sW1[k * MT + c] = T(0);
+    }
+    for (int row0 = item.x; row0 < item.y; row0 += RT) {
+      const int nrow = min(RT, item.y - row0);
+      __syncthreads();
+      if (tid < RT) {
+        int ap = -1;
+        int64_t d = 0;
+        if (tid < nrow) {
+          const Double rr = decode_row(g, row0 + tid);
+          ap = rr.ap;
+          d = row_to_d(g, rr, row0 + tid);
+        }
+        sAp[tid] = ap;
+        sD[tid] = d;
+      }
+      // C|D and A values, 8 at a time (segments start on 8-value boundaries)
+      const int nchK = K / 8, nchA = noP / 8;
+      for (int o = tid; o < RT * (nchK + nchA); o += 256) {
+        const int rr = o / (nchK + nchA), q = o - rr * (nchK + nchA);
+        T v[8];
+        if (rr < nrow) {
+          const TV* rp = base + (int64_t)(row0 + rr - g.start[cls]) * L + (q < nchK ? offC + 8 * q : 8 * (q - nchK));
+          Load8<T, TV>::go(rp, v);
+        } else {
+#pragma unroll
+          for (int u = 0; u < 8; ++u) v[u] = T(0);
+        }
+        T* dst = q < nchK ? sCD + rr * CDS + 8 * q : sA + rr * AS + 8 * (q - nchK);
+        Store8<T>::go(dst, v);
+      }
+      __syncthreads();
+      for (int o = tid; o < RT * MT; o += 256) {
+        const int rr = o % RT, c = o / RT;
+        sV2[rr * MT + c] = (rr < nrow && c < mcols) ? V[(int64_t)c * ldv + n1 + sD[rr]] : T(0);
+      }
+      __syncthreads();
+      // W2 rows of the tile: 4 x CT output tiles (CT = 4 in FP32, 2 in FP64
+      // to stay within registers), the K sum of each split over S
+      // consecutive lanes (k in chunks of 4) and reduced by shuffles
+      {
+        constexpr int CT = sizeof(T) == 8 ? 2 : 4;
+        constexpr int NMT = (RT / 4) * (MT / CT);
+        constexpr int S = 256 / NMT;
+        const int mt = tid / S, ks = tid % S;
+        const int r0 = 4 * (mt % (RT / 4)), c0 = CT * (mt / (RT / 4));
+        T acc[4][CT];
+#pragma unroll
+        for (int i = 0; i < 4; ++i)
+#pragma unroll
+          for (int cc = 0; cc < CT; ++cc) acc[i][cc] = T(0);
+        for (int k4 = ks; k4 < K / 4; k4 += S) {
+          T a[4][4], x[CT][4];
+#pragma unroll
+          for (int i = 0; i < 4; ++i) Vec4<T>::ld(sCD + (r0 + i) * CDS + 4 * k4, a[i]);
+#pragma unroll
+          for (int cc = 0; cc < CT; ++cc) Vec4<T>::ld(sX + (c0 + cc) * KP + 4 * k4, x[cc]);
+#pragma unroll
+          for (int i = 0; i < 4; ++i)
+#pragma unroll
+            for (int cc = 0; cc < CT; ++cc)
+#pragma unroll
+              for (int jj = 0; jj < 4; ++jj) acc[i][cc] += a[i][jj] * x[cc][jj];
+        }
+#pragma unroll
+        for (int off = S / 2; off > 0; off >>= 1)
+#pragma unroll
+          for (int i = 0; i < 4; ++i)
+#pragma unroll
+            for (int cc = 0; cc < CT; ++cc) acc[i][cc] += __shfl_xor_sync(0xffffffffu, acc[i][cc], off);
+#pragma unroll
+        for (int q = 0; q < 4 * CT; ++q) {
+          if (q % S != ks) continue;
+          const int rr = r0 + q / CT, c = c0 + q % CT;
+          if (rr >= nrow || c >= mcols) continue;
+          const int ap = sAp[rr];
+          const int64_t d = sD[rr];
+          const T* arow = sA + rr * AS;
+          const T* vs = V + (int64_t)c * ldv + (int64_t)ap * no;
+          T sa = T(0);
+          // padded A entries are zero; (ap, kk >= no) stays inside the V column
+#pragma unroll 8
+          for (int kk = 0; kk < noP; ++kk) sa += arow[kk] * vs[kk];
+          W[(int64_t)c * ldw + n1 + d] = diag[n1 + d] * sV2[rr * MT + c] + (sa + acc[q / CT][q % CT]);
+        }
+      }
+      // W1 (C|D): thread owns 4 k x 4 columns; sums over the tile's rows
+      for (int o = tid; o < (K / 4) * (MT / 4); o += 256) {
+        const int kq = o % (K / 4), cg = o / (K / 4);
+        T sm[4][4];
+#pragma unroll
+        for (int i = 0; i < 4; ++i)
+#pragma unroll
+          for (int cc = 0; cc < 4; ++cc) sm[i][cc] = T(0);
+#pragma unroll 4
+        for (int rr = 0; rr < RT; ++rr) {
+          T a[4], v[4];
+          Vec4<T>::ld(sCD + rr * CDS + 4 * kq, a);
+          Vec4<T>::ld(sV2 + rr * MT + 4 * cg, v);
+#pragma unroll
+          for (int i = 0; i < 4; ++i)
+#pragma unroll
+            for (int cc = 0; cc < 4; ++cc) sm[i][cc] += a[i] * v[cc];
+        }
+#pragma unroll
+        for (int i = 0; i < 4; ++i) {
+          T* w = sW1 + (4 * kq + i) * MT + 4 * cg;
+#pragma unroll
+          for (int cc = 0; cc < 4; ++cc) w[cc] += sm[i][cc];
+        }
+      }
+      // W1 (A): runs of equal a' reduced, then added atomically
+      for (int o = tid; o < noP * MT; o += 256) {
+        const int kk = o % noP, c = o / noP;
+        if (kk >= no || c >= mcols) continue;
+        T sacc = T(0);
+        int prev = sAp[0];
+        for (int rr = 0; rr < nrow; ++rr) {
+          const int ap = sAp[rr];
+          if (ap != prev) {
+            if (sacc != T(0)) atomicAdd(&W1[(int64_t)c * ld1 + (int64_t)prev * no + kk], (TA)sacc);
+            sacc = T(0);
+            prev = ap;
+          }
+          sacc += sA[rr * AS + kk] * sV2[rr * MT + c];
+        }
+        if (sacc != T(0)) atomicAdd(&W1[(int64_t)c * ld1 + (int64_t)prev * no + kk], (TA)sacc);
+      }
+    }
+    __syncthreads();
+    for (int o = tid; o < K * MT; o += 256) {
+      const int k = o / MT, c = o - k * MT;
+      const int seg = k / nvP, a = k - seg * nvP;
+      const T v = sW1[o];
+      if (a < nv && c < mcols && v != T(0))
+        atomicAdd(&W1[(int64_t)c * ld1 + (int64_t)a * no + (seg ? lp : kp)], (TA)v);
+    }
+  }
+}
+
 // W1 = diag1 . V1 + A V1 (A symmetric n1 x n1, row-major == column-major).
 template <typename T>
 __global__ void __launch_bounds__(256) k_singles(int n1, const T* __restrict__ A, const T* __restrict__ diag,
@@ -557,6 +800,37 @@ __global__ void k_w1_finalize(int n1, int m, const double* __restrict__ acc, flo
   }
 }
 
+template <typename T, typename TV, typename TA, int MT>
+int launch_tile(Ctx* c, const GeomDev& g, const SigmaPlan* plan, const TV* Bt, const T* diag, const T* V,
+                int64_t ldv, int ncols, T* W, int64_t ldw, TA* W1, int64_t ld1, size_t smem) {
+  auto kern = k_sigma_tile<T, TV, TA, MT>;
+  ADC_CUDA(c, cudaFuncSetAttribute(kern, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem));
+  ADC_CUDA(c, cudaFuncSetAttribute(kern, cudaFuncAttributePreferredSharedMemoryCarveout, 100));
+  const int grid = std::min(plan->ntitems, 152 * 2);
+  kern<<<grid, 256, smem, c->stream>>>(g, plan->d_titems, plan->ntitems, Bt, diag, V, ldv, ncols, W, ldw, W1,
+                                       ld1); ADC_COUNT_LAUNCH();
+  ADC_CUDA(c, cudaGetLastError());
+  return ADCGPU_OK;
+}
+
+// pass 2 (segment B) for mc <= 4 columns
+template <typename T, typename TV, typename TA>
+int launch_p2(Ctx* c, const GeomDev& g, const SigmaPlan* plan, int mc, const TV* Bt, const T* V, int64_t ldv,
+              T* W, int64_t ldw, TA* W1, int64_t ld1) {
+  const int g2 = std::min(plan->nitems, 152 * 8 * 8) / 8 + 1;
+  const int gs = g.noP <= 8 ? 1 : (g.noP <= 16 ? 2 : 4);
+  cudaStream_t s = c->stream;
+#define P2(MC, GS) \
+  k_sigma_p2<T, TV, TA, MC, GS><<<g2, 256, 0, s>>>(g, plan->d_items, plan->nitems, Bt, V, ldv, W, ldw, W1, ld1)
+  if (mc == 4) { if (gs == 1) P2(4, 1); else if (gs == 2) P2(4, 2); else P2(4, 4); }
+  else if (mc == 2) { if (gs == 1) P2(2, 1); else if (gs == 2) P2(2, 2); else P2(2, 4); }
+  else { if (gs == 1) P2(1, 1); else if (gs == 2) P2(1, 2); else P2(1, 4); }
+#undef P2
+  ADC_COUNT_LAUNCH();
+  ADC_CUDA(c, cudaGetLastError());
+  return ADCGPU_OK;
+}
+
 template <typename T, typename TV>
 int sigma_impl(Ctx* c, int m, const T* dV, int64_t ldv, T* dW, int64_t ldw, const T* A, const T* diag,
                const TV* Bt) {
@@ -595,7 +869,45 @@ int sigma_impl(Ctx* c, int m, const T* dV, int64_t ldv, T* dW, int64_t ldw, cons
     ADC_CUDA(c, cudaMemsetAsync(plan->d_acc, 0, need, s));
     W1base = reinterpret_cast<TAcc*>(plan->d_acc);
   }
+  // tiled pass 1 (k_sigma_tile) when its shared memory fits: widest column
+  // group first; segment B still runs through pass 2 in groups of <= 4
+  // FP32: 16 columns keep two blocks per SM (their loads overlap the other's
+  // arithmetic); FP64 is bound by the FP64 pipe at one block per SM
+  constexpr int MTMAX = 16;
+  const size_t smax = 227 * 1024;
+  int mt_fit = 0;
+  for (int mt = MTMAX; mt >= 8 && !mt_fit; mt /= 2)
+    if (tile_smem_bytes(G.nvP, G.noP, mt, sizeof(T)) <= smax) mt_fit = mt;
+  // a column tile always computes MT columns: below 16 columns the per-warp
+  // pass 1 is faster
+  const bool tiled = plan->tiled && plan->d_titems && mt_fit > 0 && m >= 16;
   int c0 = 0;
+  while (tiled && c0 < m) {
+    const int left = m - c0;
+    const int mt = left > 8 && mt_fit >= 16 ? 16 : 8;
+    const int ncols = std::min(left, mt);
+    const T* V = dV + (int64_t)c0 * ldv;
+    T* W = dW + (int64_t)c0 * ldw;
+    TAcc* W1 = sizeof(T) == 8 ? reinterpret_cast<TAcc*>(W) : W1base + (int64_t)c0 * n1;
+    const int64_t ld1 = sizeof(T) == 8 ? ldw : (int64_t)n1;
+    const size_t smem = tile_smem_bytes(G.nvP, G.noP, mt, sizeof(T));
+    if (mt == 16) ST((launch_tile<T, TV, TAcc, 16>(c, g, plan, Bt, diag, V, ldv, ncols, W, ldw, W1, ld1, smem)));
+    else ST((launch_tile<T, TV, TAcc, 8>(c, g, plan, Bt, diag, V, ldv, ncols, W, ldw, W1, ld1, smem)));
+    ADC_CUDA(c, cudaGetLastError());
+    // segment B: pass 2 over the same columns
+    int b0 = 0;
+    while (plan->nitems && b0 < ncols) {
+      const int lb = ncols - b0;
+      const int mc = lb >= 4 ? 4 : (lb >= 2 ? 2 : 1);
+      const T* Vb = V + (int64_t)b0 * ldv;
+      T* Wb = W + (int64_t)b0 * ldw;
+      TAcc* W1b = W1 + (int64_t)b0 * ld1;
+      ST((launch_p2<T, TV, TAcc>(c, g, plan, mc, Bt, Vb, ldv, Wb, ldw, W1b, ld1)));
+      ADC_CUDA(c, cudaGetLastError());
+      b0 += mc;
+    }
+    c0 += ncols;
+  }
   while (c0 < m) {
     const int left = m - c0;
     const T* V = dV + (int64_t)c0 * ldv;
@@ -661,12 +973,16 @@ __global__ void k_to_bf16(const double* __restrict__ x, __nv_bfloat16* __restric
 // with a' < b'.
 int build_chunks(Ctx* c, int chunk) {
   const Geometry& G = c->geom;
-  std::vector<int2> chunks, items;
+  std::vector<int2> chunks, items, titems;
   for (int cls = 0; cls < 5; ++cls) {
     const int64_t r0 = G.start[cls], r1 = G.start[cls + 1], sl = G.slab_len(cls);
     for (int64_t s0 = r0; s0 < r1; s0 += sl) {
       for (int64_t a = s0; a < s0 + sl; a += chunk)
         chunks.push_back(make_int2((int)a, (int)std::min<int64_t>(a + chunk, s0 + sl)));
+      // tiled pass 1: equal pieces of at most TILE_ITEM_ROWS rows per slab
+      const int64_t npc = (sl + TILE_ITEM_ROWS - 1) / TILE_ITEM_ROWS, per = (sl + npc - 1) / npc;
+      for (int64_t a = s0; a < s0 + sl; a += per)
+        titems.push_back(make_int2((int)a, (int)std::min<int64_t>(a + per, s0 + sl)));
       if (cls == 1 || cls >= 3)
         for (int bp = 1; bp < G.nv; ++bp) items.push_back(make_int2((int)s0, bp));
     }
@@ -675,8 +991,12 @@ int build_chunks(Ctx* c, int chunk) {
   if (!plan) { plan = new SigmaPlan; c->sigma_plan = plan; }
   if (plan->d_chunks) cudaFree(plan->d_chunks);
   if (plan->d_items) cudaFree(plan->d_items);
-  plan->d_chunks = plan->d_items = nullptr;
+  if (plan->d_titems) cudaFree(plan->d_titems);
+  plan->d_chunks = plan->d_items = plan->d_titems = nullptr;
   int st;
+  if ((st = dmalloc(c, (void**)&plan->d_titems, sizeof(int2) * titems.size()))) return st;
+  ADC_CUDA(c, cudaMemcpy(plan->d_titems, titems.data(), sizeof(int2) * titems.size(), cudaMemcpyHostToDevice));
+  plan->ntitems = (int)titems.size();
   if ((st = dmalloc(c, (void**)&plan->d_chunks, sizeof(int2) * chunks.size()))) return st;
   if ((st = dmalloc(c, (void**)&plan->d_items, sizeof(int2) * std::max<size_t>(items.size(), 1)))) return st;
   ADC_CUDA(c, cudaMemcpy(plan->d_chunks, chunks.data(), sizeof(int2) * chunks.size(), cudaMemcpyHostToDevice));
@@ -698,6 +1018,7 @@ void free_sigma_plan(Ctx* c) {
   if (!plan) return;
   if (plan->d_chunks) cudaFree(plan->d_chunks);
   if (plan->d_items) cudaFree(plan->d_items);
+  if (plan->d_titems) cudaFree(plan->d_titems);
   if (plan->d_acc) cudaFree(plan->d_acc);
   delete plan;
   c->sigma_plan = nullptr;
@@ -748,37 +1069,50 @@ extern "C" int adcgpu_sigma_autotune(adcgpu_ctx* h, int m, int* best_chunk, int*
   const int chunks[] = {16, 64, 256};
   const int mcs[] = {1, 2, 4};
   double best = 1e30;
-  int bc = plan->chunk, bm = plan->mc_cap[mixed ? 1 : 0], bs = plan->staged;
+  int bc = plan->chunk, bm = plan->mc_cap[mixed ? 1 : 0], bs = plan->staged, bt = plan->tiled;
+  auto time_once = [&]() {
+    double t = 1e30;
+    for (int rep = 0; rep < 3; ++rep) {
+      cudaEventRecord(c->ev0, c->stream);
+      st = mixed ? sigma_fp32(c, m, (const float*)dv, N, (float*)dw, N)
+                 : sigma_fp64(c, m, (const double*)dv, N, (double*)dw, N);
+      cudaEventRecord(c->ev1, c->stream);
+      cudaEventSynchronize(c->ev1);
+      float ms = 0.f;
+      cudaEventElapsedTime(&ms, c->ev0, c->ev1);
+      if (rep > 0) t = std::min(t, (double)ms);
+    }
+    return t;
+  };
+  // the tiled pass 1 (one candidate), then the per-warp shapes
+  plan->tiled = 1;
+  {
+    const double t = time_once();
+    if (t < best) { best = t; bt = 1; }
+  }
+  plan->tiled = 0;
   for (int ch : chunks) {
-    if ((st = build_chunks(c, ch))) break;
+    if (st || (st = build_chunks(c, ch))) break;
     for (int stg = 0; stg < 2; ++stg)
     for (int mc : mcs) {
       if (!mixed && mc > 2) continue;
       plan->mc_cap[mixed ? 1 : 0] = mc;
       plan->staged = stg;
-      double t = 1e30;
-      for (int rep = 0; rep < 3; ++rep) {
-        cudaEventRecord(c->ev0, c->stream);
-        st = mixed ? sigma_fp32(c, m, (const float*)dv, N, (float*)dw, N)
-                   : sigma_fp64(c, m, (const double*)dv, N, (double*)dw, N);
-        cudaEventRecord(c->ev1, c->stream);
-        cudaEventSynchronize(c->ev1);
-        float ms = 0.f;
-        cudaEventElapsedTime(&ms, c->ev0, c->ev1);
-        if (rep > 0) t = std::min(t, (double)ms);
-      }
-      if (t < best) { best = t; bc = ch; bm = mc; bs = stg; }
+      const double t = time_once();
+      if (t < best) { best = t; bc = ch; bm = mc; bs = stg; bt = 0; }
     }
   }
   sigma_stats_flush(c);
   c->st_calls = 0; c->st_cols = 0; c->st_ms = 0.0; c->st_bytes = 0.0;
   plan->mc_cap[mixed ? 1 : 0] = bm;
   plan->staged = bs;
+  plan->tiled = bt;
   if (!st) st = build_chunks(c, bc);
   dfree(c, dv, 0);
   dfree(c, dw, 0);
   if (best_chunk) *best_chunk = bc;
-  if (best_mc) *best_mc = bm + 8 * bs;   // bit 3: staged pass-1 variant
+  // bit 3: staged pass-1 variant; bit 4: per-warp pass 1 instead of the tiled one
+  if (best_mc) *best_mc = bm + 8 * bs + 16 * (bt ? 0 : 1);
   if (best_ms) *best_ms = best;
   return st;
 }
@@ -791,6 +1125,7 @@ extern "C" int adcgpu_sigma_set_shape(adcgpu_ctx* h, int chunk, int mc_fp64, int
   if (!c->have_matrix) return set_err(c, ADCGPU_NO_MATRIX, "build the matrix first");
   SigmaPlan* plan = reinterpret_cast<SigmaPlan*>(c->sigma_plan);
   plan->staged = ((mc_fp64 | mc_fp32) & 8) ? 1 : 0;
+  plan->tiled = ((mc_fp64 | mc_fp32) & 16) ? 0 : 1;
   plan->mc_cap[0] = std::min(mc_fp64 & 7, 2);
   plan->mc_cap[1] = std::min(mc_fp32 & 7, 4);
   return build_chunks(c, chunk);

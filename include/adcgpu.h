@@ -323,13 +323,17 @@ int adcgpu_sigma_stats(adcgpu_ctx* ctx, double* out4, int reset);
    All calls share the array: calls that overlap on the GPU race. */
 int adcgpu_sigma_device_noalloc(adcgpu_ctx* ctx, int m, const void* dv, void* dw, int64_t ld);
 
-/* Autotuner of the sigma kernels' launch shape: pass-1 rows per warp work
-   item (16..256) and vector columns per pass (1, 2, 4), timed with CUDA
-   events for m columns on the built matrix; the fastest shape is kept in the
-   context and returned (the Python layer caches it in a JSON file). */
+/* Autotuner of the sigma kernels' launch shape: the tiled pass 1 against
+   the per-warp pass 1 with its rows per work item (16..256), columns per
+   pass (1, 2, 4) and staging, timed with CUDA events for m columns on the
+   built matrix; the fastest shape is kept in the context and returned in
+   the encoding of adcgpu_sigma_set_shape (the Python layer caches it in a
+   JSON file). */
 int adcgpu_sigma_autotune(adcgpu_ctx* ctx, int m, int* best_chunk, int* best_mc, double* best_ms);
 
-/* Applies a launch shape (e.g. from the autotuner's cache). */
+/* Applies a launch shape (e.g. from the autotuner's cache).  In mc_fp64 /
+   mc_fp32, bits 0-2 give the columns per pass, bit 3 selects the staged
+   per-warp pass 1, bit 4 the per-warp pass 1 instead of the tiled one. */
 int adcgpu_sigma_set_shape(adcgpu_ctx* ctx, int chunk, int mc_fp64, int mc_fp32);
 
 #ifdef __cplusplus
