@@ -14,6 +14,7 @@
 
 #include "internal.h"
 #include "dense.h"
+#include "df.h"
 
 namespace adcgpu {
 
@@ -101,37 +102,6 @@ __global__ void k_gemm_tn_reduce(int p, int q, int nblk, int ntile, const TA* __
   }
 }
 
-// ---------------------------------------------------------------------------
-// Double-float ("DF") arithmetic for FP64-accurate GEMMs on the FP32 pipe.
-// A double x is held as hi + lo with hi = fl32(x), lo = fl32(x - hi)
-// (48 significant bits).  A product of two such pairs is formed exactly in
-// its leading part with an FMA (Dekker's two-product) plus the two cross
-// terms; sums use Knuth's two-sum, so a step sum of 32 products carries
-// ~2^-44 relative error before it is added to an FP64 accumulator.  On GB300
-// the FP32 pipe issues 64 FMAs for every FP64 FMA, and one DF multiply-add
-// costs about 12 FP32 instructions.
-// ---------------------------------------------------------------------------
-struct df { float hi, lo; };
-
-__device__ __forceinline__ df df_split(double x) {
-  const float h = (float)x;
-  return df{h, (float)(x - (double)h)};
-}
-
-// s += a * b
-__device__ __forceinline__ void df_fma(df& s, df a, df b) {
-  const float p = a.hi * b.hi;
-  float e = fmaf(a.hi, b.hi, -p);
-  e = fmaf(a.hi, b.lo, e);
-  e = fmaf(a.lo, b.hi, e);
-  const float t = s.hi + p;
-  const float v = t - s.hi;
-  const float err = (s.hi - (t - v)) + (p - v);
-  s.lo += err + e;
-  s.hi = t;
-}
-
-__device__ __forceinline__ double df_value(df s) { return (double)s.hi + (double)s.lo; }
 
 // k_gemm_tn_part for FP64 inputs with DF step sums and FP64 accumulators.
 __global__ void __launch_bounds__(256) k_gemm_tn_part_df(int64_t N, int p, int q, const double* __restrict__ A,

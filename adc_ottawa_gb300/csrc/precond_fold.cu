@@ -38,12 +38,12 @@ template <typename T>
 __global__ void k_fold_prep(int64_t N, int n1, const T* __restrict__ R, int64_t ldr, const double* __restrict__ lam,
                             const T* __restrict__ hii, T* __restrict__ Tout, int64_t ldt) {
   const int c = blockIdx.y;
-  const double l = lam[c];
+  const T l = (T)lam[c];
   for (int64_t i = blockIdx.x * (int64_t)blockDim.x + threadIdx.x; i < N; i += (int64_t)gridDim.x * blockDim.x) {
     T t = T(0);
     if (i >= n1) {
-      const double den = l - (double)hii[i];
-      t = den != 0.0 ? T((double)R[(int64_t)c * ldr + i] / den) : T(0);
+      const T den = l - hii[i];
+      t = den != T(0) ? R[(int64_t)c * ldr + i] / den : T(0);
     }
     Tout[(int64_t)c * ldt + i] = t;
   }

@@ -18,6 +18,7 @@
 
 #include <type_traits>
 
+#include "df.h"
 #include "internal.h"
 
 namespace adcgpu {
@@ -507,8 +508,35 @@ __global__ void __launch_bounds__(256) k_sigma_p2(GeomDev g, const int2* __restr
   }
 }
 
+// Arithmetic of the tiled pass 1.  Native: values, vectors and sums in T.
+// DF (FP64 inputs only): the C|D values and the vectors are held in shared
+// memory as double-float pairs and multiplied on the FP32 pipe (df.h); the
+// segment-A part, the diagonal term and the per-item W1 sums stay in FP64.
+template <typename T> struct NativeArith {
+  typedef T S;
+  __device__ __forceinline__ static S from(T x) { return x; }
+  __device__ __forceinline__ static S zero() { return T(0); }
+  __device__ __forceinline__ static void fma(S& acc, S a, S b) { acc += a * b; }
+  __device__ __forceinline__ static S shfl_add(S a, int off) { return a + __shfl_xor_sync(0xffffffffu, a, off); }
+  __device__ __forceinline__ static T value(S a) { return a; }
+};
+struct DfArith {
+  typedef df S;
+  __device__ __forceinline__ static S from(double x) { return df_split(x); }
+  __device__ __forceinline__ static S zero() { return df{0.f, 0.f}; }
+  __device__ __forceinline__ static void fma(S& acc, S a, S b) { df_fma(acc, a, b); }
+  __device__ __forceinline__ static S shfl_add(S a, int off) {
+    return df_add(a, df{__shfl_xor_sync(0xffffffffu, a.hi, off), __shfl_xor_sync(0xffffffffu, a.lo, off)});
+  }
+  __device__ __forceinline__ static double value(S a) { return df_value(a); }
+};
+
+template <typename T> struct DfArithSel { typedef NativeArith<T> type; };
+template <> struct DfArithSel<double> { typedef DfArith type; };
+template <typename T> using DfArithFor = typename DfArithSel<T>::type;
+
 // 4 consecutive values from 16-byte aligned shared memory
-template <typename T> struct Vec4;
+template <typename S> struct Vec4;
 template <> struct Vec4<float> {
   __device__ __forceinline__ static void ld(const float* p, float (&v)[4]) {
     const float4 q = *reinterpret_cast<const float4*>(p);
@@ -521,9 +549,15 @@ template <> struct Vec4<double> {
     v[0] = q0.x; v[1] = q0.y; v[2] = q1.x; v[3] = q1.y;
   }
 };
+template <> struct Vec4<df> {
+  __device__ __forceinline__ static void ld(const df* p, df (&v)[4]) {
+    const float4 q0 = reinterpret_cast<const float4*>(p)[0], q1 = reinterpret_cast<const float4*>(p)[1];
+    v[0] = df{q0.x, q0.y}; v[1] = df{q0.z, q0.w}; v[2] = df{q1.x, q1.y}; v[3] = df{q1.z, q1.w};
+  }
+};
 
 // 8 values to 16-byte aligned shared memory as vector stores
-template <typename T> struct Store8;
+template <typename S> struct Store8;
 template <> struct Store8<float> {
   __device__ __forceinline__ static void go(float* d, const float (&v)[8]) {
     reinterpret_cast<float4*>(d)[0] = make_float4(v[0], v[1], v[2], v[3]);
@@ -534,6 +568,13 @@ template <> struct Store8<double> {
   __device__ __forceinline__ static void go(double* d, const double (&v)[8]) {
 #pragma unroll
     for (int i = 0; i < 4; ++i) reinterpret_cast<double2*>(d)[i] = make_double2(v[2 * i], v[2 * i + 1]);
+  }
+};
+template <> struct Store8<df> {
+  __device__ __forceinline__ static void go(df* d, const df (&v)[8]) {
+#pragma unroll
+    for (int i = 0; i < 4; ++i)
+      reinterpret_cast<float4*>(d)[i] = make_float4(v[2 * i].hi, v[2 * i].lo, v[2 * i + 1].hi, v[2 * i + 1].lo);
   }
 };
 
@@ -547,39 +588,42 @@ template <> struct Store8<double> {
 //   W2[r, c] += sum_a C[r, a] Xk[a, c] + D[r, a] Xl[a, c]     (Xk = V[(a,k'), c])
 //   W1[(a, k'), c] += sum_r C[r, a] V2[r, c]   (and D with l')
 // Xk and Xl stay in shared memory for the whole item; each 32-row tile of
-// C|D values is staged once and used for every column; the W1 sums of the
-// item accumulate in shared memory (in T, one 32-row tile at a time) and are
-// added to the TA accumulators of W1 once at the end of the item.
-// Segment A (singles (a', k)) is handled per tile: its W2 part gathers V
-// through L1, its W1 part is reduced over runs of equal a' and added
-// atomically.  Segment B stays with pass 2, as before.
-// Shared memory (bytes): T sW1[nseg*nvP*MT] | T sX[MT*(2nvP+4)] (column-major) |
-// T sCD[RT*(2nvP+4)] | T sA[RT*(noP+4)] | T sV2[RT*MT] | int64 sD[RT] | int sAp[RT]
-// (row strides are multiples of 16 bytes, so the staging stores are 16-byte
-// vector stores, and 4 rows read in one warp fall into different banks).
+// C|D values is staged once and used for every column.  W2: 4 x CT output
+// tiles, the K sum of each split over S lanes and reduced by shuffles.  W1:
+// 4 k x 4 columns per thread over the tile's rows, added per tile to the
+// item's sums in shared memory (T), which go to the TA accumulators of W1
+// once at the end of the item.  Segment A (singles (a', k)) is handled per
+// tile: its W2 part gathers V through L1, its W1 part is reduced over runs
+// of equal a' and added atomically.  Segment B stays with pass 2.
+// Shared memory (bytes): T sW1[nseg*nvP*MT] | S sX[MT*(2nvP+4)] (column-major)
+// | S sCD[RT*(2nvP+4)] | T sA[RT*(noP+4)] | S sV2[RT*MT] | int64 sD[RT] |
+// int sAp[RT] (row strides are multiples of 16 bytes, so the staging stores
+// are 16-byte vector stores, and 4 rows read in one warp fall into
+// different banks).
 // ---------------------------------------------------------------------------
 constexpr int TILE_RT = 32;
 constexpr int TILE_ITEM_ROWS = 1024;
 
 __host__ __device__ inline size_t align16(size_t x) { return (x + 15) / 16 * 16; }
 
-inline size_t tile_smem_bytes(int nvP, int noP, int MT, size_t sT) {
+inline size_t tile_smem_bytes(int nvP, int noP, int MT, size_t sT, size_t sS) {
   size_t b = align16((size_t)2 * nvP * MT * sT);
-  b += align16((size_t)MT * (2 * nvP + 4) * sT);
-  b += align16((size_t)TILE_RT * (2 * nvP + 4) * sT);
+  b += align16((size_t)MT * (2 * nvP + 4) * sS);
+  b += align16((size_t)TILE_RT * (2 * nvP + 4) * sS);
   b += align16((size_t)TILE_RT * (noP + 4) * sT);
-  b += align16((size_t)TILE_RT * MT * sT);
+  b += align16((size_t)TILE_RT * MT * sS);
   b += align16((size_t)TILE_RT * 8);
   b += align16((size_t)TILE_RT * 4);
   return b;
 }
 
-template <typename T, typename TV, typename TA, int MT>
-__global__ void __launch_bounds__(256) k_sigma_tile(GeomDev g, const int2* __restrict__ titems, int ntitems,
+template <typename T, typename TV, typename TA, int MT, typename AR>
+__global__ void __launch_bounds__(256, 1) k_sigma_tile(GeomDev g, const int2* __restrict__ titems, int ntitems,
                                                     const TV* __restrict__ Bt, const T* __restrict__ diag,
                                                     const T* __restrict__ V, int64_t ldv, int mcols,
                                                     T* __restrict__ W, int64_t ldw, TA* __restrict__ W1,
                                                     int64_t ld1) {
+  typedef typename AR::S S;
   constexpr int RT = TILE_RT;
   extern __shared__ __align__(16) unsigned char smem_raw[];
   const int no = g.no, nv = g.nv, noP = g.noP, nvP = g.nvP;
@@ -587,10 +631,10 @@ __global__ void __launch_bounds__(256) k_sigma_tile(GeomDev g, const int2* __res
   const int CDS = 2 * nvP + 4, AS = noP + 4, KP = 2 * nvP + 4;
   unsigned char* p = smem_raw;
   T* sW1 = reinterpret_cast<T*>(p); p += align16((size_t)2 * nvP * MT * sizeof(T));
-  T* sX = reinterpret_cast<T*>(p); p += align16((size_t)MT * (2 * nvP + 4) * sizeof(T));
-  T* sCD = reinterpret_cast<T*>(p); p += align16((size_t)RT * CDS * sizeof(T));
+  S* sX = reinterpret_cast<S*>(p); p += align16((size_t)MT * (2 * nvP + 4) * sizeof(S));
+  S* sCD = reinterpret_cast<S*>(p); p += align16((size_t)RT * CDS * sizeof(S));
   T* sA = reinterpret_cast<T*>(p); p += align16((size_t)RT * AS * sizeof(T));
-  T* sV2 = reinterpret_cast<T*>(p); p += align16((size_t)RT * MT * sizeof(T));
+  S* sV2 = reinterpret_cast<S*>(p); p += align16((size_t)RT * MT * sizeof(S));
   int64_t* sD = reinterpret_cast<int64_t*>(p); p += align16((size_t)RT * 8);
   int* sAp = reinterpret_cast<int*>(p);
   const int tid = threadIdx.x;
@@ -609,7 +653,8 @@ __global__ void __launch_bounds__(256) k_sigma_tile(GeomDev g, const int2* __res
     for (int o = tid; o < K * MT; o += 256) {
       const int k = o % K, c = o / K;
       const int seg = k / nvP, a = k - seg * nvP;
-      sX[c * KP + k] = (a < nv && c < mcols) ? V[(int64_t)c * ldv + (int64_t)a * no + (seg ? lp : kp)] : T(0);
+      sX[c * KP + k] =
+          AR::from((a < nv && c < mcols) ? V[(int64_t)c * ldv + (int64_t)a * no + (seg ? lp : kp)] : T(0));
       sW1[k * MT + c] = T(0);
     }
     for (int row0 = item.x; row0 < item.y; row0 += RT) {
@@ -638,51 +683,56 @@ __global__ void __launch_bounds__(256) k_sigma_tile(GeomDev g, const int2* __res
 #pragma unroll
           for (int u = 0; u < 8; ++u) v[u] = T(0);
         }
-        T* dst = q < nchK ? sCD + rr * CDS + 8 * q : sA + rr * AS + 8 * (q - nchK);
-        Store8<T>::go(dst, v);
+        if (q < nchK) {
+          S w[8];
+#pragma unroll
+          for (int u = 0; u < 8; ++u) w[u] = AR::from(v[u]);
+          Store8<S>::go(sCD + rr * CDS + 8 * q, w);
+        } else {
+          Store8<T>::go(sA + rr * AS + 8 * (q - nchK), v);
+        }
       }
       __syncthreads();
       for (int o = tid; o < RT * MT; o += 256) {
         const int rr = o % RT, c = o / RT;
-        sV2[rr * MT + c] = (rr < nrow && c < mcols) ? V[(int64_t)c * ldv + n1 + sD[rr]] : T(0);
+        sV2[rr * MT + c] = AR::from((rr < nrow && c < mcols) ? V[(int64_t)c * ldv + n1 + sD[rr]] : T(0));
       }
       __syncthreads();
-      // W2 rows of the tile: 4 x CT output tiles (CT = 4 in FP32, 2 in FP64
-      // to stay within registers), the K sum of each split over S
-      // consecutive lanes (k in chunks of 4) and reduced by shuffles
+      // W2 rows of the tile: 4 x CT output tiles (CT = 4 for FP32 values, 2
+      // for 8-byte ones, to stay within registers)
       {
-        constexpr int CT = sizeof(T) == 8 ? 2 : 4;
+        constexpr int CT = sizeof(S) == 4 ? 4 : 2;
         constexpr int NMT = (RT / 4) * (MT / CT);
-        constexpr int S = 256 / NMT;
-        const int mt = tid / S, ks = tid % S;
+        constexpr int SPL = 256 / NMT;
+        const int mt = tid / SPL, ks = tid % SPL;
         const int r0 = 4 * (mt % (RT / 4)), c0 = CT * (mt / (RT / 4));
-        T acc[4][CT];
+        S acc[4][CT];
 #pragma unroll
         for (int i = 0; i < 4; ++i)
 #pragma unroll
-          for (int cc = 0; cc < CT; ++cc) acc[i][cc] = T(0);
-        for (int k4 = ks; k4 < K / 4; k4 += S) {
-          T a[4][4], x[CT][4];
+          for (int cc = 0; cc < CT; ++cc) acc[i][cc] = AR::zero();
+        for (int k4 = ks; k4 < K / 4; k4 += SPL) {
+          S a[4][4], x[CT][4];
 #pragma unroll
-          for (int i = 0; i < 4; ++i) Vec4<T>::ld(sCD + (r0 + i) * CDS + 4 * k4, a[i]);
+          for (int i = 0; i < 4; ++i) Vec4<S>::ld(sCD + (r0 + i) * CDS + 4 * k4, a[i]);
 #pragma unroll
-          for (int cc = 0; cc < CT; ++cc) Vec4<T>::ld(sX + (c0 + cc) * KP + 4 * k4, x[cc]);
+          for (int cc = 0; cc < CT; ++cc) Vec4<S>::ld(sX + (c0 + cc) * KP + 4 * k4, x[cc]);
 #pragma unroll
           for (int i = 0; i < 4; ++i)
 #pragma unroll
             for (int cc = 0; cc < CT; ++cc)
 #pragma unroll
-              for (int jj = 0; jj < 4; ++jj) acc[i][cc] += a[i][jj] * x[cc][jj];
+              for (int jj = 0; jj < 4; ++jj) AR::fma(acc[i][cc], a[i][jj], x[cc][jj]);
         }
 #pragma unroll
-        for (int off = S / 2; off > 0; off >>= 1)
+        for (int off = SPL / 2; off > 0; off >>= 1)
 #pragma unroll
           for (int i = 0; i < 4; ++i)
 #pragma unroll
-            for (int cc = 0; cc < CT; ++cc) acc[i][cc] += __shfl_xor_sync(0xffffffffu, acc[i][cc], off);
+            for (int cc = 0; cc < CT; ++cc) acc[i][cc] = AR::shfl_add(acc[i][cc], off);
 #pragma unroll
         for (int q = 0; q < 4 * CT; ++q) {
-          if (q % S != ks) continue;
+          if (q % SPL != ks) continue;
           const int rr = r0 + q / CT, c = c0 + q % CT;
           if (rr >= nrow || c >= mcols) continue;
           const int ap = sAp[rr];
@@ -693,32 +743,33 @@ __global__ void __launch_bounds__(256) k_sigma_tile(GeomDev g, const int2* __res
           // padded A entries are zero; (ap, kk >= no) stays inside the V column
 #pragma unroll 8
           for (int kk = 0; kk < noP; ++kk) sa += arow[kk] * vs[kk];
-          W[(int64_t)c * ldw + n1 + d] = diag[n1 + d] * sV2[rr * MT + c] + (sa + acc[q / CT][q % CT]);
+          W[(int64_t)c * ldw + n1 + d] =
+              diag[n1 + d] * AR::value(sV2[rr * MT + c]) + (sa + AR::value(acc[q / CT][q % CT]));
         }
       }
       // W1 (C|D): thread owns 4 k x 4 columns; sums over the tile's rows
       for (int o = tid; o < (K / 4) * (MT / 4); o += 256) {
         const int kq = o % (K / 4), cg = o / (K / 4);
-        T sm[4][4];
+        S sm[4][4];
 #pragma unroll
         for (int i = 0; i < 4; ++i)
 #pragma unroll
-          for (int cc = 0; cc < 4; ++cc) sm[i][cc] = T(0);
-#pragma unroll 4
+          for (int cc = 0; cc < 4; ++cc) sm[i][cc] = AR::zero();
+#pragma unroll 2
         for (int rr = 0; rr < RT; ++rr) {
-          T a[4], v[4];
-          Vec4<T>::ld(sCD + rr * CDS + 4 * kq, a);
-          Vec4<T>::ld(sV2 + rr * MT + 4 * cg, v);
+          S a[4], v[4];
+          Vec4<S>::ld(sCD + rr * CDS + 4 * kq, a);
+          Vec4<S>::ld(sV2 + rr * MT + 4 * cg, v);
 #pragma unroll
           for (int i = 0; i < 4; ++i)
 #pragma unroll
-            for (int cc = 0; cc < 4; ++cc) sm[i][cc] += a[i] * v[cc];
+            for (int cc = 0; cc < 4; ++cc) AR::fma(sm[i][cc], a[i], v[cc]);
         }
 #pragma unroll
         for (int i = 0; i < 4; ++i) {
           T* w = sW1 + (4 * kq + i) * MT + 4 * cg;
 #pragma unroll
-          for (int cc = 0; cc < 4; ++cc) w[cc] += sm[i][cc];
+          for (int cc = 0; cc < 4; ++cc) w[cc] += AR::value(sm[i][cc]);
         }
       }
       // W1 (A): runs of equal a' reduced, then added atomically
@@ -734,7 +785,7 @@ __global__ void __launch_bounds__(256) k_sigma_tile(GeomDev g, const int2* __res
             sacc = T(0);
             prev = ap;
           }
-          sacc += sA[rr * AS + kk] * sV2[rr * MT + c];
+          sacc += sA[rr * AS + kk] * AR::value(sV2[rr * MT + c]);
         }
         if (sacc != T(0)) atomicAdd(&W1[(int64_t)c * ld1 + (int64_t)prev * no + kk], (TA)sacc);
       }
@@ -778,6 +829,61 @@ __global__ void __launch_bounds__(256) k_singles(int n1, const T* __restrict__ A
   if (r < n1 && c < m) W[(int64_t)c * ldw + r] = diag[r] * V[(int64_t)c * ldv + r] + acc;
 }
 
+// W1 = diag1 . V1 + A V1 as a register-tiled GEMM: block tile 32 rows x 32
+// columns, K staged 32 at a time, 128 threads with 4 x 2 outputs each.
+// Used by the sigma product and by the folded preconditioner's MINRES.
+template <typename T>
+__global__ void __launch_bounds__(128) k_singles_gemm(int n1, const T* __restrict__ A, const T* __restrict__ diag,
+                                                      const T* __restrict__ V, int64_t ldv, T* __restrict__ W,
+                                                      int64_t ldw, int m) {
+  __shared__ __align__(16) T sA[32][36];   // sA[k][r]
+  __shared__ T sV[32][33];                 // sV[k][c]
+  const int tid = threadIdx.x;
+  const int tx = tid & 15, ty = tid >> 4;   // columns 2tx, 2tx+1; rows 4ty..4ty+3
+  const int r0 = blockIdx.x * 32, c0 = blockIdx.y * 32;
+  T acc[4][2];
+#pragma unroll
+  for (int i = 0; i < 4; ++i) { acc[i][0] = T(0); acc[i][1] = T(0); }
+  for (int k0 = 0; k0 < n1; k0 += 32) {
+    __syncthreads();
+#pragma unroll
+    for (int l = tid; l < 32 * 32; l += 128) {
+      const int kk = l & 31, rr = l >> 5;
+      const int r = r0 + rr, k = k0 + kk;
+      sA[kk][rr] = (r < n1 && k < n1) ? A[(int64_t)r * n1 + k] : T(0);
+      const int c = c0 + rr;
+      sV[kk][rr] = (c < m && k < n1) ? V[(int64_t)c * ldv + k] : T(0);
+    }
+    __syncthreads();
+#pragma unroll 8
+    for (int kk = 0; kk < 32; ++kk) {
+      T a[4];
+#pragma unroll
+      for (int i = 0; i < 4; ++i) a[i] = sA[kk][4 * ty + i];
+      const T b0 = sV[kk][2 * tx], b1 = sV[kk][2 * tx + 1];
+#pragma unroll
+      for (int i = 0; i < 4; ++i) { acc[i][0] += a[i] * b0; acc[i][1] += a[i] * b1; }
+    }
+  }
+#pragma unroll
+  for (int j = 0; j < 2; ++j) {
+    const int c = c0 + 2 * tx + j;
+    if (c >= m) continue;
+#pragma unroll
+    for (int i = 0; i < 4; ++i) {
+      const int r = r0 + 4 * ty + i;
+      if (r < n1) W[(int64_t)c * ldw + r] = diag[r] * V[(int64_t)c * ldv + r] + acc[i][j];
+    }
+  }
+}
+
+template <typename T>
+void launch_singles(Ctx* c, int m, const T* A, const T* diag, const T* V, int64_t ldv, T* W, int64_t ldw) {
+  const int n1 = (int)c->geom.n1;
+  dim3 grid((n1 + 31) / 32, (m + 31) / 32);
+  k_singles_gemm<T><<<grid, 128, 0, c->stream>>>(n1, A, diag, V, ldv, W, ldw, m); ADC_COUNT_LAUNCH();
+}
+
 // Close the statistics window of the previous sigma call (its stop event
 // has completed by the time the next call or a read of the stats happens).
 void sigma_stats_flush(Ctx* c) {
@@ -803,7 +909,9 @@ __global__ void k_w1_finalize(int n1, int m, const double* __restrict__ acc, flo
 template <typename T, typename TV, typename TA, int MT>
 int launch_tile(Ctx* c, const GeomDev& g, const SigmaPlan* plan, const TV* Bt, const T* diag, const T* V,
                 int64_t ldv, int ncols, T* W, int64_t ldw, TA* W1, int64_t ld1, size_t smem) {
-  auto kern = k_sigma_tile<T, TV, TA, MT>;
+  // FP64 inputs in the mixed ladder's refinement: double-float arithmetic
+  auto kern = (sizeof(T) == 8 && c->dense_df) ? k_sigma_tile<T, TV, TA, MT, DfArithFor<T>>
+                                              : k_sigma_tile<T, TV, TA, MT, NativeArith<T>>;
   ADC_CUDA(c, cudaFuncSetAttribute(kern, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem));
   ADC_CUDA(c, cudaFuncSetAttribute(kern, cudaFuncAttributePreferredSharedMemoryCarveout, 100));
   const int grid = std::min(plan->ntitems, 152 * 2);
@@ -845,8 +953,7 @@ int sigma_impl(Ctx* c, int m, const T* dV, int64_t ldv, T* dW, int64_t ldw, cons
   ADC_CUDA(c, cudaEventRecord(c->st_ev0, s));
   GeomDev g = to_dev(G);
   // singles block first (plain stores), then the coupling adds atomically
-  dim3 gs((n1 + 63) / 64, (m + 3) / 4);
-  k_singles<T><<<gs, 256, 0, s>>>(n1, A, diag, dV, ldv, dW, ldw, m); ADC_COUNT_LAUNCH();
+  launch_singles<T>(c, m, A, diag, dV, ldv, dW, ldw);
   ADC_CUDA(c, cudaGetLastError());
   SigmaPlan* plan = reinterpret_cast<SigmaPlan*>(c->sigma_plan);
   if (!plan) return set_err(c, ADCGPU_NO_MATRIX, "sigma plan missing");
@@ -877,7 +984,7 @@ int sigma_impl(Ctx* c, int m, const T* dV, int64_t ldv, T* dW, int64_t ldw, cons
   const size_t smax = 227 * 1024;
   int mt_fit = 0;
   for (int mt = MTMAX; mt >= 8 && !mt_fit; mt /= 2)
-    if (tile_smem_bytes(G.nvP, G.noP, mt, sizeof(T)) <= smax) mt_fit = mt;
+    if (tile_smem_bytes(G.nvP, G.noP, mt, sizeof(T), sizeof(T)) <= smax) mt_fit = mt;
   // a column tile always computes MT columns: below 16 columns the per-warp
   // pass 1 is faster
   const bool tiled = plan->tiled && plan->d_titems && mt_fit > 0 && m >= 16;
@@ -890,7 +997,7 @@ int sigma_impl(Ctx* c, int m, const T* dV, int64_t ldv, T* dW, int64_t ldw, cons
     T* W = dW + (int64_t)c0 * ldw;
     TAcc* W1 = sizeof(T) == 8 ? reinterpret_cast<TAcc*>(W) : W1base + (int64_t)c0 * n1;
     const int64_t ld1 = sizeof(T) == 8 ? ldw : (int64_t)n1;
-    const size_t smem = tile_smem_bytes(G.nvP, G.noP, mt, sizeof(T));
+    const size_t smem = tile_smem_bytes(G.nvP, G.noP, mt, sizeof(T), sizeof(T));
     if (mt == 16) ST((launch_tile<T, TV, TAcc, 16>(c, g, plan, Bt, diag, V, ldv, ncols, W, ldw, W1, ld1, smem)));
     else ST((launch_tile<T, TV, TAcc, 8>(c, g, plan, Bt, diag, V, ldv, ncols, W, ldw, W1, ld1, smem)));
     ADC_CUDA(c, cudaGetLastError());
@@ -1138,17 +1245,13 @@ int sigma_fp64(Ctx* c, int m, const double* dV, int64_t ldv, double* dW, int64_t
 // W = Hss V for the dense singles block alone (diag1 + A), m columns of n1
 // rows: the inner product of the folded preconditioner's MINRES solve.
 int singles_block_product(Ctx* c, int m, const double* V, int64_t ldv, double* W, int64_t ldw) {
-  const int n1 = (int)c->geom.n1;
-  k_singles<double><<<dim3((n1 + 63) / 64, (m + 3) / 4), 256, 0, c->stream>>>(n1, c->d_A, c->d_diag, V, ldv, W, ldw,
-                                                                              m); ADC_COUNT_LAUNCH();
+  launch_singles<double>(c, m, c->d_A, c->d_diag, V, ldv, W, ldw);
   ADC_CUDA(c, cudaGetLastError());
   return ADCGPU_OK;
 }
 int singles_block_product(Ctx* c, int m, const float* V, int64_t ldv, float* W, int64_t ldw) {
-  const int n1 = (int)c->geom.n1;
   if (!c->d_A32 || !c->d_diag32) return set_err(c, ADCGPU_NO_MATRIX, "FP32 singles block missing");
-  k_singles<float><<<dim3((n1 + 63) / 64, (m + 3) / 4), 256, 0, c->stream>>>(n1, c->d_A32, c->d_diag32, V, ldv, W,
-                                                                             ldw, m); ADC_COUNT_LAUNCH();
+  launch_singles<float>(c, m, c->d_A32, c->d_diag32, V, ldv, W, ldw);
   ADC_CUDA(c, cudaGetLastError());
   return ADCGPU_OK;
 }
