@@ -291,7 +291,8 @@ struct SigmaPlan {
   int chunk = 64;             // rows per pass-1 work item (autotuned)
   int mc_cap[2] = {2, 4};     // columns per pass for FP64 / FP32 vectors (autotuned)
   int staged = 1;             // pass 1 through a cp.async shared-memory ring (autotuned)
-  int tiled = 1;              // pass 1 as k_sigma_tile when its shared memory fits
+  int tiled = 1;              // pass 1 tiled when its shared memory fits (1: tensor cores for
+                              // BF16 values, 2: CUDA cores only, 0: per-warp pass 1)
   int2* d_titems = nullptr;   // tiled pass 1: [row_begin, row_end) inside one slab
   int ntitems = 0;
   void* d_acc = nullptr;      // FP64 accumulator of the singles rows (FP32 path)

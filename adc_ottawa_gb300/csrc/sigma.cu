@@ -801,6 +801,236 @@ __global__ void __launch_bounds__(256, 1) k_sigma_tile(GeomDev g, const int2* __
   }
 }
 
+// ---------------------------------------------------------------------------
+// Tiled pass 1 on the tensor cores (BF16 values, FP32 vectors): the same
+// work items and tiles as k_sigma_tile, 16 columns per pass.  The vectors
+// enter as BF16 hi + lo pairs (x = hi + lo to ~2^-17), each product is two
+// mma.sync m16n8k16 (BF16 in, FP32 accumulate).
+//   warps 0-3: W2[32 x 16] = C|D[32 x K] . X[K x 16]   (one 16 x 8 tile each)
+//   warps 4-7: W1^T[16 x K] += V2^T[16 x 32] . C|D[32 x K], the item's sums
+//              held in the accumulators, added to W1 (FP64) at the end.
+// K is rounded up to 16 with zero padding.  Segment A and the diagonal term
+// stay on the CUDA cores as in k_sigma_tile; segment B stays with pass 2.
+// Shared memory (bytes): bf16 sCD[RT][2nvP+8] | bf16 sCDt[2nvP+8][RT+8] |
+// bf16 sXh, sXl[16][2nvP+8] | bf16 sV2h, sV2l[16][RT+8] | f32 sV2f[RT][16] |
+// f32 sA[RT][noP+4] | int64 sD[RT] | int sAp[RT]
+// ---------------------------------------------------------------------------
+constexpr int MMA_MT = 16;
+constexpr int MMA_RTP = TILE_RT + 8;
+
+inline size_t tile_mma_smem_bytes(int nvP, int noP) {
+  const size_t KP = (size_t)2 * nvP + 8;
+  size_t b = align16((size_t)TILE_RT * KP * 2);
+  b += align16(KP * MMA_RTP * 2);
+  b += 2 * align16((size_t)MMA_MT * KP * 2);
+  b += 2 * align16((size_t)MMA_MT * MMA_RTP * 2);
+  b += align16((size_t)TILE_RT * MMA_MT * 4);
+  b += align16((size_t)TILE_RT * (noP + 4) * 4);
+  b += align16((size_t)TILE_RT * 8);
+  b += align16((size_t)TILE_RT * 4);
+  return b;
+}
+
+__device__ __forceinline__ void mma16816(float (&c)[4], const uint32_t (&a)[4], uint32_t b0, uint32_t b1) {
+  asm volatile(
+      "mma.sync.aligned.m16n8k16.row.col.f32.bf16.bf16.f32 {%0,%1,%2,%3}, {%4,%5,%6,%7}, {%8,%9}, "
+      "{%0,%1,%2,%3};\n"
+      : "+f"(c[0]), "+f"(c[1]), "+f"(c[2]), "+f"(c[3])
+      : "r"(a[0]), "r"(a[1]), "r"(a[2]), "r"(a[3]), "r"(b0), "r"(b1));
+}
+
+__device__ __forceinline__ uint32_t ld_u32(const __nv_bfloat16* p) { return *reinterpret_cast<const uint32_t*>(p); }
+
+template <typename TA>
+__global__ void __launch_bounds__(256, 2) k_sigma_tile_mma(GeomDev g, const int2* __restrict__ titems, int ntitems,
+                                                           const __nv_bfloat16* __restrict__ Bt,
+                                                           const float* __restrict__ diag,
+                                                           const float* __restrict__ V, int64_t ldv, int mcols,
+                                                           float* __restrict__ W, int64_t ldw, TA* __restrict__ W1,
+                                                           int64_t ld1) {
+  constexpr int RT = TILE_RT, MT = MMA_MT, RTP = MMA_RTP;
+  constexpr int NT1 = 16;                  // W1 n-tile slots per warp (K/8 <= 64)
+  extern __shared__ __align__(16) unsigned char smem_raw[];
+  const int no = g.no, nv = g.nv, noP = g.noP, nvP = g.nvP;
+  const int64_t n1 = g.n1;
+  // row stride 4 nvP + 16 bytes: an odd multiple of 16, so the 8 rows of a
+  // fragment load fall into 8 different 16-byte bank groups
+  const int KP = 2 * nvP + 8, AS = noP + 4;
+  unsigned char* p = smem_raw;
+  __nv_bfloat16* sCD = reinterpret_cast<__nv_bfloat16*>(p); p += align16((size_t)RT * KP * 2);
+  __nv_bfloat16* sCDt = reinterpret_cast<__nv_bfloat16*>(p); p += align16((size_t)KP * RTP * 2);
+  __nv_bfloat16* sXh = reinterpret_cast<__nv_bfloat16*>(p); p += align16((size_t)MT * KP * 2);
+  __nv_bfloat16* sXl = reinterpret_cast<__nv_bfloat16*>(p); p += align16((size_t)MT * KP * 2);
+  __nv_bfloat16* sV2h = reinterpret_cast<__nv_bfloat16*>(p); p += align16((size_t)MT * RTP * 2);
+  __nv_bfloat16* sV2l = reinterpret_cast<__nv_bfloat16*>(p); p += align16((size_t)MT * RTP * 2);
+  float* sV2f = reinterpret_cast<float*>(p); p += align16((size_t)RT * MT * 4);
+  float* sA = reinterpret_cast<float*>(p); p += align16((size_t)RT * AS * 4);
+  int64_t* sD = reinterpret_cast<int64_t*>(p); p += align16((size_t)RT * 8);
+  int* sAp = reinterpret_cast<int*>(p);
+  const int tid = threadIdx.x, lane = tid & 31, warp = tid >> 5;
+  const int gid = lane >> 2, tig = lane & 3;
+  for (int it = blockIdx.x; it < ntitems; it += gridDim.x) {
+    const int2 item = titems[it];
+    const Double r0 = decode_row(g, item.x);
+    const int cls = r0.cls;
+    const bool twoa = (cls == 1 || cls >= 3);
+    const int nseg = cls >= 2 ? 2 : 1;
+    const int K = nseg * nvP, K16 = (K + 15) / 16 * 16;
+    const int64_t L = g.len[cls];
+    const int offC = twoa ? 2 * noP : noP;
+    const int kp = r0.kp, lp = r0.lp;
+    const __nv_bfloat16* base = Bt + g.off[cls];
+    float acc1[NT1][4];
+#pragma unroll
+    for (int j = 0; j < NT1; ++j) acc1[j][0] = acc1[j][1] = acc1[j][2] = acc1[j][3] = 0.f;
+    __syncthreads();
+    for (int o = tid; o < K16 * MT; o += 256) {
+      const int k = o % K16, c = o / K16;
+      const int seg = k / nvP, a = k - seg * nvP;
+      const float x = (k < K && a < nv && c < mcols) ? V[(int64_t)c * ldv + (int64_t)a * no + (seg ? lp : kp)] : 0.f;
+      const __nv_bfloat16 h = __float2bfloat16(x);
+      sXh[c * KP + k] = h;
+      sXl[c * KP + k] = __float2bfloat16(x - __bfloat162float(h));
+    }
+    for (int row0 = item.x; row0 < item.y; row0 += RT) {
+      const int nrow = min(RT, item.y - row0);
+      __syncthreads();
+      if (tid < RT) {
+        int ap = -1;
+        int64_t d = 0;
+        if (tid < nrow) {
+          const Double rr = decode_row(g, row0 + tid);
+          ap = rr.ap;
+          d = row_to_d(g, rr, row0 + tid);
+        }
+        sAp[tid] = ap;
+        sD[tid] = d;
+      }
+      // C|D chunks (8 values) row-major and transposed, zero past K; then A
+      const int nch16 = K16 / 8, nchK = K / 8, nchA = noP / 8;
+      for (int o = tid; o < RT * (nch16 + nchA); o += 256) {
+        const int rr = o % RT, q = o / RT;
+        const int64_t roff = (int64_t)(row0 + rr - g.start[cls]) * L;
+        if (q < nch16) {
+          uint4 u = make_uint4(0u, 0u, 0u, 0u);
+          if (rr < nrow && q < nchK) u = __ldg(reinterpret_cast<const uint4*>(base + roff + offC + 8 * q));
+          *reinterpret_cast<uint4*>(sCD + rr * KP + 8 * q) = u;
+          const __nv_bfloat16* e = reinterpret_cast<const __nv_bfloat16*>(&u);
+#pragma unroll
+          for (int v = 0; v < 8; ++v) sCDt[(8 * q + v) * RTP + rr] = e[v];
+        } else {
+          const int qa = q - nch16;
+          float v[8];
+          if (rr < nrow) Load8<float, __nv_bfloat16>::go(base + roff + 8 * qa, v);
+          else {
+#pragma unroll
+            for (int w = 0; w < 8; ++w) v[w] = 0.f;
+          }
+          Store8<float>::go(sA + rr * AS + 8 * qa, v);
+        }
+      }
+      __syncthreads();
+      for (int o = tid; o < RT * MT; o += 256) {
+        const int rr = o % RT, c = o / RT;
+        const float x = (rr < nrow && c < mcols) ? V[(int64_t)c * ldv + n1 + sD[rr]] : 0.f;
+        sV2f[rr * MT + c] = x;
+        const __nv_bfloat16 h = __float2bfloat16(x);
+        sV2h[c * RTP + rr] = h;
+        sV2l[c * RTP + rr] = __float2bfloat16(x - __bfloat162float(h));
+      }
+      __syncthreads();
+      if (warp < 4) {
+        // W2 tile: rows 16 (warp & 1).., columns 8 (warp >> 1)..
+        const int m0 = 16 * (warp & 1), n0 = 8 * (warp >> 1);
+        float acc[4] = {0.f, 0.f, 0.f, 0.f};
+        for (int k0 = 0; k0 < K16; k0 += 16) {
+          uint32_t a[4];
+          a[0] = ld_u32(sCD + (m0 + gid) * KP + k0 + 2 * tig);
+          a[1] = ld_u32(sCD + (m0 + gid + 8) * KP + k0 + 2 * tig);
+          a[2] = ld_u32(sCD + (m0 + gid) * KP + k0 + 2 * tig + 8);
+          a[3] = ld_u32(sCD + (m0 + gid + 8) * KP + k0 + 2 * tig + 8);
+          const int xo = (n0 + gid) * KP + k0 + 2 * tig;
+          mma16816(acc, a, ld_u32(sXh + xo), ld_u32(sXh + xo + 8));
+          mma16816(acc, a, ld_u32(sXl + xo), ld_u32(sXl + xo + 8));
+        }
+#pragma unroll
+        for (int h = 0; h < 4; ++h) {
+          const int rr = m0 + gid + 8 * (h >> 1), c = n0 + 2 * tig + (h & 1);
+          if (rr >= nrow || c >= mcols) continue;
+          const int ap = sAp[rr];
+          const int64_t d = sD[rr];
+          const float* arow = sA + rr * AS;
+          const float* vs = V + (int64_t)c * ldv + (int64_t)ap * no;
+          float sa = 0.f;
+          // padded A entries are zero; (ap, kk >= no) stays inside the V column
+#pragma unroll 8
+          for (int kk = 0; kk < noP; ++kk) sa += arow[kk] * vs[kk];
+          W[(int64_t)c * ldw + n1 + d] = diag[n1 + d] * sV2f[rr * MT + c] + (sa + acc[h]);
+        }
+      } else {
+        // W1^T += V2^T . C|D: n-tiles nt = (warp - 4) + 4 j over K/8
+        const int w4 = warp - 4;
+#pragma unroll
+        for (int ks = 0; ks < RT; ks += 16) {
+          uint32_t ah[4], al[4];
+          ah[0] = ld_u32(sV2h + gid * RTP + ks + 2 * tig);
+          ah[1] = ld_u32(sV2h + (gid + 8) * RTP + ks + 2 * tig);
+          ah[2] = ld_u32(sV2h + gid * RTP + ks + 2 * tig + 8);
+          ah[3] = ld_u32(sV2h + (gid + 8) * RTP + ks + 2 * tig + 8);
+          al[0] = ld_u32(sV2l + gid * RTP + ks + 2 * tig);
+          al[1] = ld_u32(sV2l + (gid + 8) * RTP + ks + 2 * tig);
+          al[2] = ld_u32(sV2l + gid * RTP + ks + 2 * tig + 8);
+          al[3] = ld_u32(sV2l + (gid + 8) * RTP + ks + 2 * tig + 8);
+#pragma unroll
+          for (int j = 0; j < NT1; ++j) {
+            const int nt = w4 + 4 * j;
+            if (nt < K / 8) {
+              const int bo = (8 * nt + gid) * RTP + ks + 2 * tig;
+              const uint32_t b0 = ld_u32(sCDt + bo), b1 = ld_u32(sCDt + bo + 8);
+              mma16816(acc1[j], ah, b0, b1);
+              mma16816(acc1[j], al, b0, b1);
+            }
+          }
+        }
+      }
+      // W1 (A): runs of equal a' reduced, then added atomically
+      for (int o = tid; o < noP * MT; o += 256) {
+        const int kk = o % noP, c = o / noP;
+        if (kk >= no || c >= mcols) continue;
+        float sacc = 0.f;
+        int prev = sAp[0];
+        for (int rr = 0; rr < nrow; ++rr) {
+          const int ap = sAp[rr];
+          if (ap != prev) {
+            if (sacc != 0.f) atomicAdd(&W1[(int64_t)c * ld1 + (int64_t)prev * no + kk], (TA)sacc);
+            sacc = 0.f;
+            prev = ap;
+          }
+          sacc += sA[rr * AS + kk] * sV2f[rr * MT + c];
+        }
+        if (sacc != 0.f) atomicAdd(&W1[(int64_t)c * ld1 + (int64_t)prev * no + kk], (TA)sacc);
+      }
+    }
+    // the item's W1 (C|D) sums: accumulator (c = gid + 8 (h >> 1), k = 8 nt + 2 tig + (h & 1))
+    if (warp >= 4) {
+      const int w4 = warp - 4;
+#pragma unroll
+      for (int j = 0; j < NT1; ++j) {
+        const int nt = w4 + 4 * j;
+        if (nt >= K / 8) continue;
+#pragma unroll
+        for (int h = 0; h < 4; ++h) {
+          const int c = gid + 8 * (h >> 1), k = 8 * nt + 2 * tig + (h & 1);
+          const int seg = k / nvP, a = k - seg * nvP;
+          const float v = acc1[j][h];
+          if (c < mcols && a < nv && v != 0.f)
+            atomicAdd(&W1[(int64_t)c * ld1 + (int64_t)a * no + (seg ? lp : kp)], (TA)v);
+        }
+      }
+    }
+  }
+}
+
 // W1 = diag1 . V1 + A V1 (A symmetric n1 x n1, row-major == column-major).
 template <typename T>
 __global__ void __launch_bounds__(256) k_singles(int n1, const T* __restrict__ A, const T* __restrict__ diag,
@@ -921,6 +1151,20 @@ int launch_tile(Ctx* c, const GeomDev& g, const SigmaPlan* plan, const TV* Bt, c
   return ADCGPU_OK;
 }
 
+template <typename TA>
+int launch_tile_mma(Ctx* c, const GeomDev& g, const SigmaPlan* plan, const __nv_bfloat16* Bt, const float* diag,
+                    const float* V, int64_t ldv, int ncols, float* W, int64_t ldw, TA* W1, int64_t ld1) {
+  const size_t smem = tile_mma_smem_bytes(g.nvP, g.noP);
+  auto kern = k_sigma_tile_mma<TA>;
+  ADC_CUDA(c, cudaFuncSetAttribute(kern, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem));
+  ADC_CUDA(c, cudaFuncSetAttribute(kern, cudaFuncAttributePreferredSharedMemoryCarveout, 100));
+  const int grid = std::min(plan->ntitems, 152 * 2);
+  kern<<<grid, 256, smem, c->stream>>>(g, plan->d_titems, plan->ntitems, Bt, diag, V, ldv, ncols, W, ldw, W1,
+                                       ld1); ADC_COUNT_LAUNCH();
+  ADC_CUDA(c, cudaGetLastError());
+  return ADCGPU_OK;
+}
+
 // pass 2 (segment B) for mc <= 4 columns
 template <typename T, typename TV, typename TA>
 int launch_p2(Ctx* c, const GeomDev& g, const SigmaPlan* plan, int mc, const TV* Bt, const T* V, int64_t ldv,
@@ -998,6 +1242,21 @@ int sigma_impl(Ctx* c, int m, const T* dV, int64_t ldv, T* dW, int64_t ldw, cons
     TAcc* W1 = sizeof(T) == 8 ? reinterpret_cast<TAcc*>(W) : W1base + (int64_t)c0 * n1;
     const int64_t ld1 = sizeof(T) == 8 ? ldw : (int64_t)n1;
     const size_t smem = tile_smem_bytes(G.nvP, G.noP, mt, sizeof(T), sizeof(T));
+    if constexpr (std::is_same<TV, __nv_bfloat16>::value) {
+      if (plan->tiled == 1 && tile_mma_smem_bytes(G.nvP, G.noP) <= smax) {
+        // tensor-core tile: 16 columns per pass
+        const int nc = std::min(left, MMA_MT);
+        ST((launch_tile_mma<TAcc>(c, g, plan, Bt, diag, V, ldv, nc, W, ldw, W1, ld1)));
+        for (int b0 = 0; plan->nitems && b0 < nc;) {
+          const int lb = nc - b0, mc = lb >= 4 ? 4 : (lb >= 2 ? 2 : 1);
+          ST((launch_p2<T, TV, TAcc>(c, g, plan, mc, Bt, V + (int64_t)b0 * ldv, ldv, W + (int64_t)b0 * ldw, ldw,
+                                     W1 + (int64_t)b0 * ld1, ld1)));
+          b0 += mc;
+        }
+        c0 += nc;
+        continue;
+      }
+    }
     if (mt == 16) ST((launch_tile<T, TV, TAcc, 16>(c, g, plan, Bt, diag, V, ldv, ncols, W, ldw, W1, ld1, smem)));
     else ST((launch_tile<T, TV, TAcc, 8>(c, g, plan, Bt, diag, V, ldv, ncols, W, ldw, W1, ld1, smem)));
     ADC_CUDA(c, cudaGetLastError());
@@ -1232,7 +1491,7 @@ extern "C" int adcgpu_sigma_set_shape(adcgpu_ctx* h, int chunk, int mc_fp64, int
   if (!c->have_matrix) return set_err(c, ADCGPU_NO_MATRIX, "build the matrix first");
   SigmaPlan* plan = reinterpret_cast<SigmaPlan*>(c->sigma_plan);
   plan->staged = ((mc_fp64 | mc_fp32) & 8) ? 1 : 0;
-  plan->tiled = ((mc_fp64 | mc_fp32) & 16) ? 0 : 1;
+  plan->tiled = ((mc_fp64 | mc_fp32) & 16) ? 0 : (((mc_fp64 | mc_fp32) & 32) ? 2 : 1);
   plan->mc_cap[0] = std::min(mc_fp64 & 7, 2);
   plan->mc_cap[1] = std::min(mc_fp32 & 7, 4);
   return build_chunks(c, chunk);

@@ -333,7 +333,8 @@ int adcgpu_sigma_autotune(adcgpu_ctx* ctx, int m, int* best_chunk, int* best_mc,
 
 /* Applies a launch shape (e.g. from the autotuner's cache).  In mc_fp64 /
    mc_fp32, bits 0-2 give the columns per pass, bit 3 selects the staged
-   per-warp pass 1, bit 4 the per-warp pass 1 instead of the tiled one. */
+   per-warp pass 1, bit 4 the per-warp pass 1 instead of the tiled one, bit
+   5 the CUDA-core tiled pass 1 instead of the tensor-core one (BF16 values). */
 int adcgpu_sigma_set_shape(adcgpu_ctx* ctx, int chunk, int mc_fp64, int mc_fp32);
 
 #ifdef __cplusplus

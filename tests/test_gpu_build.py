@@ -205,3 +205,23 @@ def test_sigma_launch_shapes_agree(gpu, prec, tmp_path):
     y = g.sigma(x)
     assert np.abs(y - ref).max() <= tol * np.abs(ref).max()
     g.close()
+
+
+@pytest.mark.parametrize("prec", [0, 1])
+def test_sigma_tiled_passes_agree(gpu, prec):
+    """20 columns (a 16-column tile pass and 4 more): the tiled pass 1 (tensor
+    cores for BF16 values, CUDA cores otherwise) and the CUDA-core tile agree
+    with the per-warp pass 1.  FP64: to roundoff.  BF16 values: the tensor-core
+    pass carries the vectors as BF16 hi + lo pairs (~2^-17 relative)."""
+    from adc_ottawa_gb300._native import lib
+
+    g, e, eri = make(6, 30, 11, precision=prec)
+    x = np.random.RandomState(5).standard_normal((g.ndim, 20))
+    assert lib().adcgpu_sigma_set_shape(g._h, 64, 2 | 16, 4 | 16) == 0     # per-warp
+    ref = g.sigma(x)
+    scale = np.abs(ref).max()
+    for bits, tol in ((32, 1e-12 if prec == 0 else 1e-5), (0, 1e-12 if prec == 0 else 2e-4)):
+        assert lib().adcgpu_sigma_set_shape(g._h, 64, 2 | bits, 4 | bits) == 0
+        y = g.sigma(x)
+        assert np.abs(y - ref).max() <= tol * scale, (bits, np.abs(y - ref).max() / scale)
+    g.close()
