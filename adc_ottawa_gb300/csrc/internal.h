@@ -103,10 +103,11 @@ __host__ __device__ inline int64_t pair_index(int x, int y, int n) {
 }
 
 __host__ __device__ inline void pair_decode(int64_t p, int n, int& x, int& y) {
-  // invert pair_index: estimate the row from the quadratic, then correct
-  const double b = 2.0 * n - 1.0;
-  double disc = b * b - 8.0 * (double)p;
-  int xx = (int)((b - sqrt(disc > 0.0 ? disc : 0.0)) * 0.5);
+  // invert pair_index: estimate the row from the quadratic (FP32 is enough
+  // for an estimate; GB300's FP64 square root is slow), then correct exactly
+  const float b = 2.0f * (float)n - 1.0f;
+  float disc = b * b - 8.0f * (float)p;
+  int xx = (int)((b - sqrtf(disc > 0.0f ? disc : 0.0f)) * 0.5f);
   if (xx < 0) xx = 0;
   if (xx > n - 2) xx = n - 2;
   while (xx > 0 && pair_index(xx, xx + 1, n) > p) --xx;

@@ -811,23 +811,25 @@ __global__ void __launch_bounds__(256, 1) k_sigma_tile(GeomDev g, const int2* __
 //              held in the accumulators, added to W1 (FP64) at the end.
 // K is rounded up to 16 with zero padding.  Segment A and the diagonal term
 // stay on the CUDA cores as in k_sigma_tile; segment B stays with pass 2.
-// Shared memory (bytes): bf16 sCD[RT][2nvP+8] | bf16 sCDt[2nvP+8][RT+8] |
-// bf16 sXh, sXl[16][2nvP+8] | bf16 sV2h, sV2l[16][RT+8] | f32 sV2f[RT][16] |
-// f32 sA[RT][noP+4] | int64 sD[RT] | int sAp[RT]
+// The raw C|D and A values of tile t+1 stream into a second stage with
+// cp.async (zero-filled past K and past the item's rows) while tile t is
+// multiplied; the transposed copy used by W1 is built in shared memory.
+// Shared memory: see tile_mma_smem_bytes.
 // ---------------------------------------------------------------------------
 constexpr int MMA_MT = 16;
 constexpr int MMA_RTP = TILE_RT + 8;
 
 inline size_t tile_mma_smem_bytes(int nvP, int noP) {
   const size_t KP = (size_t)2 * nvP + 8;
-  size_t b = align16((size_t)TILE_RT * KP * 2);
-  b += align16(KP * MMA_RTP * 2);
-  b += 2 * align16((size_t)MMA_MT * KP * 2);
-  b += 2 * align16((size_t)MMA_MT * MMA_RTP * 2);
-  b += align16((size_t)TILE_RT * MMA_MT * 4);
-  b += align16((size_t)TILE_RT * (noP + 4) * 4);
-  b += align16((size_t)TILE_RT * 8);
-  b += align16((size_t)TILE_RT * 4);
+  size_t b = 2 * align16((size_t)TILE_RT * KP * 2);           // raw C|D tiles (2 stages)
+  b += 2 * align16((size_t)TILE_RT * noP * 2);                // raw A tiles (2 stages)
+  b += align16(KP * MMA_RTP * 2);                             // transposed C|D
+  b += 2 * align16((size_t)MMA_MT * KP * 2);                  // X hi, lo
+  b += 2 * align16((size_t)MMA_MT * MMA_RTP * 2);             // V2^T hi, lo
+  b += align16((size_t)TILE_RT * MMA_MT * 4);                 // V2 (f32)
+  b += align16((size_t)TILE_RT * (noP + 4) * 4);              // A (f32)
+  b += 2 * align16((size_t)TILE_RT * 8);                      // d (2 stages)
+  b += 2 * align16((size_t)TILE_RT * 4);                      // a' (2 stages)
   return b;
 }
 
@@ -840,6 +842,12 @@ __device__ __forceinline__ void mma16816(float (&c)[4], const uint32_t (&a)[4], 
 }
 
 __device__ __forceinline__ uint32_t ld_u32(const __nv_bfloat16* p) { return *reinterpret_cast<const uint32_t*>(p); }
+
+// 16-byte cp.async that reads src_bytes (16 or 0) and zero-fills the rest
+__device__ __forceinline__ void cp_async16_zf(void* smem, const void* gmem, int src_bytes) {
+  unsigned s = (unsigned)__cvta_generic_to_shared(smem);
+  asm volatile("cp.async.cg.shared.global [%0], [%1], 16, %2;\n" ::"r"(s), "l"(gmem), "r"(src_bytes));
+}
 
 template <typename TA>
 __global__ void __launch_bounds__(256, 2) k_sigma_tile_mma(GeomDev g, const int2* __restrict__ titems, int ntitems,
@@ -857,7 +865,10 @@ __global__ void __launch_bounds__(256, 2) k_sigma_tile_mma(GeomDev g, const int2
   // fragment load fall into 8 different 16-byte bank groups
   const int KP = 2 * nvP + 8, AS = noP + 4;
   unsigned char* p = smem_raw;
-  __nv_bfloat16* sCD = reinterpret_cast<__nv_bfloat16*>(p); p += align16((size_t)RT * KP * 2);
+  __nv_bfloat16* const sCDr0 = reinterpret_cast<__nv_bfloat16*>(p); p += align16((size_t)RT * KP * 2);
+  __nv_bfloat16* const sCDr1 = reinterpret_cast<__nv_bfloat16*>(p); p += align16((size_t)RT * KP * 2);
+  __nv_bfloat16* const sAr0 = reinterpret_cast<__nv_bfloat16*>(p); p += align16((size_t)RT * noP * 2);
+  __nv_bfloat16* const sAr1 = reinterpret_cast<__nv_bfloat16*>(p); p += align16((size_t)RT * noP * 2);
   __nv_bfloat16* sCDt = reinterpret_cast<__nv_bfloat16*>(p); p += align16((size_t)KP * RTP * 2);
   __nv_bfloat16* sXh = reinterpret_cast<__nv_bfloat16*>(p); p += align16((size_t)MT * KP * 2);
   __nv_bfloat16* sXl = reinterpret_cast<__nv_bfloat16*>(p); p += align16((size_t)MT * KP * 2);
@@ -865,8 +876,10 @@ __global__ void __launch_bounds__(256, 2) k_sigma_tile_mma(GeomDev g, const int2
   __nv_bfloat16* sV2l = reinterpret_cast<__nv_bfloat16*>(p); p += align16((size_t)MT * RTP * 2);
   float* sV2f = reinterpret_cast<float*>(p); p += align16((size_t)RT * MT * 4);
   float* sA = reinterpret_cast<float*>(p); p += align16((size_t)RT * AS * 4);
-  int64_t* sD = reinterpret_cast<int64_t*>(p); p += align16((size_t)RT * 8);
-  int* sAp = reinterpret_cast<int*>(p);
+  int64_t* const sD0 = reinterpret_cast<int64_t*>(p); p += align16((size_t)RT * 8);
+  int64_t* const sD1 = reinterpret_cast<int64_t*>(p); p += align16((size_t)RT * 8);
+  int* const sAp0 = reinterpret_cast<int*>(p); p += align16((size_t)RT * 4);
+  int* const sAp1 = reinterpret_cast<int*>(p);
   const int tid = threadIdx.x, lane = tid & 31, warp = tid >> 5;
   const int gid = lane >> 2, tig = lane & 3;
   for (int it = blockIdx.x; it < ntitems; it += gridDim.x) {
@@ -879,11 +892,32 @@ __global__ void __launch_bounds__(256, 2) k_sigma_tile_mma(GeomDev g, const int2
     const int64_t L = g.len[cls];
     const int offC = twoa ? 2 * noP : noP;
     const int kp = r0.kp, lp = r0.lp;
-    const __nv_bfloat16* base = Bt + g.off[cls];
+    const __nv_bfloat16* base = Bt + g.off[cls];   // row r starts at base + (r - start[cls]) * L
+    const int nch16 = K16 / 8, nchK = K / 8, nchA = noP / 8;
+    // raw C|D (row-major, zero past K) and A values of rows [r, r + RT) into stage b
+    auto issue = [&](int rbeg, int b) {
+      const int nr = min(RT, item.y - rbeg);
+      for (int o = tid; o < RT * (nch16 + nchA); o += 256) {
+        const int rr = o % RT, q = o / RT;
+        const int64_t roff = (int64_t)(rbeg + rr - g.start[cls]) * L;
+        if (q < nch16) {
+          const bool ok = rr < nr && q < nchK;
+          cp_async16_zf((b ? sCDr1 : sCDr0) + rr * KP + 8 * q, ok ? (const void*)(base + roff + offC + 8 * q) : (const void*)base,
+                        ok ? 16 : 0);
+        } else {
+          const int qa = q - nch16;
+          const bool ok = rr < nr;
+          cp_async16_zf((b ? sAr1 : sAr0) + rr * noP + 8 * qa, ok ? (const void*)(base + roff + 8 * qa) : (const void*)base,
+                        ok ? 16 : 0);
+        }
+      }
+    };
     float acc1[NT1][4];
 #pragma unroll
     for (int j = 0; j < NT1; ++j) acc1[j][0] = acc1[j][1] = acc1[j][2] = acc1[j][3] = 0.f;
-    __syncthreads();
+    __syncthreads();   // the previous item is done with every buffer
+    issue(item.x, 0);
+    cp_async_commit();
     for (int o = tid; o < K16 * MT; o += 256) {
       const int k = o % K16, c = o / K16;
       const int seg = k / nvP, a = k - seg * nvP;
@@ -892,10 +926,13 @@ __global__ void __launch_bounds__(256, 2) k_sigma_tile_mma(GeomDev g, const int2
       sXh[c * KP + k] = h;
       sXl[c * KP + k] = __float2bfloat16(x - __bfloat162float(h));
     }
-    for (int row0 = item.x; row0 < item.y; row0 += RT) {
+    int t = 0;
+    for (int row0 = item.x; row0 < item.y; row0 += RT, ++t) {
+      const int b = t & 1;
       const int nrow = min(RT, item.y - row0);
-      __syncthreads();
-      if (tid < RT) {
+      int64_t* sD = b ? sD1 : sD0;
+      int* sAp = b ? sAp1 : sAp0;
+      if (tid < RT) {   // stage b's row data is not read by the previous tile
         int ap = -1;
         int64_t d = 0;
         if (tid < nrow) {
@@ -906,30 +943,26 @@ __global__ void __launch_bounds__(256, 2) k_sigma_tile_mma(GeomDev g, const int2
         sAp[tid] = ap;
         sD[tid] = d;
       }
-      // C|D chunks (8 values) row-major and transposed, zero past K; then A
-      const int nch16 = K16 / 8, nchK = K / 8, nchA = noP / 8;
-      for (int o = tid; o < RT * (nch16 + nchA); o += 256) {
-        const int rr = o % RT, q = o / RT;
-        const int64_t roff = (int64_t)(row0 + rr - g.start[cls]) * L;
-        if (q < nch16) {
-          uint4 u = make_uint4(0u, 0u, 0u, 0u);
-          if (rr < nrow && q < nchK) u = __ldg(reinterpret_cast<const uint4*>(base + roff + offC + 8 * q));
-          *reinterpret_cast<uint4*>(sCD + rr * KP + 8 * q) = u;
-          const __nv_bfloat16* e = reinterpret_cast<const __nv_bfloat16*>(&u);
-#pragma unroll
-          for (int v = 0; v < 8; ++v) sCDt[(8 * q + v) * RTP + rr] = e[v];
-        } else {
-          const int qa = q - nch16;
-          float v[8];
-          if (rr < nrow) Load8<float, __nv_bfloat16>::go(base + roff + 8 * qa, v);
-          else {
-#pragma unroll
-            for (int w = 0; w < 8; ++w) v[w] = 0.f;
-          }
-          Store8<float>::go(sA + rr * AS + 8 * qa, v);
-        }
-      }
+      cp_async_wait<0>();
       __syncthreads();
+      // prefetch the next tile into the other stage (its last readers, the
+      // previous tile's products, are past the barrier above)
+      if (row0 + RT < item.y) issue(row0 + RT, b ^ 1);
+      cp_async_commit();
+      const __nv_bfloat16* sCD = b ? sCDr1 : sCDr0;
+      for (int o = tid; o < RT * nch16; o += 256) {
+        const int rr = o % RT, q = o / RT;
+        const uint4 u = *reinterpret_cast<const uint4*>(sCD + rr * KP + 8 * q);
+        const __nv_bfloat16* e = reinterpret_cast<const __nv_bfloat16*>(&u);
+#pragma unroll
+        for (int v = 0; v < 8; ++v) sCDt[(8 * q + v) * RTP + rr] = e[v];
+      }
+      for (int o = tid; o < RT * nchA; o += 256) {
+        const int rr = o % RT, qa = o / RT;
+        float v[8];
+        FromSmem8<float, __nv_bfloat16>::go((b ? sAr1 : sAr0) + rr * noP + 8 * qa, v);
+        Store8<float>::go(sA + rr * AS + 8 * qa, v);
+      }
       for (int o = tid; o < RT * MT; o += 256) {
         const int rr = o % RT, c = o / RT;
         const float x = (rr < nrow && c < mcols) ? V[(int64_t)c * ldv + n1 + sD[rr]] : 0.f;
@@ -1010,6 +1043,8 @@ __global__ void __launch_bounds__(256, 2) k_sigma_tile_mma(GeomDev g, const int2
         }
         if (sacc != 0.f) atomicAdd(&W1[(int64_t)c * ld1 + (int64_t)prev * no + kk], (TA)sacc);
       }
+      // sCDt, sA and the V2 arrays are rebuilt after the next barrier
+      __syncthreads();
     }
     // the item's W1 (C|D) sums: accumulator (c = gid + 8 (h >> 1), k = 8 nt + 2 tig + (h & 1))
     if (warp >= 4) {
@@ -1029,6 +1064,7 @@ __global__ void __launch_bounds__(256, 2) k_sigma_tile_mma(GeomDev g, const int2
       }
     }
   }
+  cp_async_wait<0>();
 }
 
 // W1 = diag1 . V1 + A V1 (A symmetric n1 x n1, row-major == column-major).
@@ -1165,7 +1201,7 @@ int launch_tile_mma(Ctx* c, const GeomDev& g, const SigmaPlan* plan, const __nv_
   return ADCGPU_OK;
 }
 
-// pass 2 (segment B) for mc <= 4 columns
+// pass 2 (segment B) for mc <= 4 columns (8 with FP32 vectors)
 template <typename T, typename TV, typename TA>
 int launch_p2(Ctx* c, const GeomDev& g, const SigmaPlan* plan, int mc, const TV* Bt, const T* V, int64_t ldv,
               T* W, int64_t ldw, TA* W1, int64_t ld1) {
@@ -1174,6 +1210,14 @@ int launch_p2(Ctx* c, const GeomDev& g, const SigmaPlan* plan, int mc, const TV*
   cudaStream_t s = c->stream;
 #define P2(MC, GS) \
   k_sigma_p2<T, TV, TA, MC, GS><<<g2, 256, 0, s>>>(g, plan->d_items, plan->nitems, Bt, V, ldv, W, ldw, W1, ld1)
+  if constexpr (sizeof(T) == 4) {
+    if (mc == 8) {
+      if (gs == 1) P2(8, 1); else if (gs == 2) P2(8, 2); else P2(8, 4);
+      ADC_COUNT_LAUNCH();
+      ADC_CUDA(c, cudaGetLastError());
+      return ADCGPU_OK;
+    }
+  }
   if (mc == 4) { if (gs == 1) P2(4, 1); else if (gs == 2) P2(4, 2); else P2(4, 4); }
   else if (mc == 2) { if (gs == 1) P2(2, 1); else if (gs == 2) P2(2, 2); else P2(2, 4); }
   else { if (gs == 1) P2(1, 1); else if (gs == 2) P2(1, 2); else P2(1, 4); }
@@ -1248,7 +1292,7 @@ int sigma_impl(Ctx* c, int m, const T* dV, int64_t ldv, T* dW, int64_t ldw, cons
         const int nc = std::min(left, MMA_MT);
         ST((launch_tile_mma<TAcc>(c, g, plan, Bt, diag, V, ldv, nc, W, ldw, W1, ld1)));
         for (int b0 = 0; plan->nitems && b0 < nc;) {
-          const int lb = nc - b0, mc = lb >= 4 ? 4 : (lb >= 2 ? 2 : 1);
+          const int lb = nc - b0, mc = lb >= 8 ? 8 : (lb >= 4 ? 4 : (lb >= 2 ? 2 : 1));
           ST((launch_p2<T, TV, TAcc>(c, g, plan, mc, Bt, V + (int64_t)b0 * ldv, ldv, W + (int64_t)b0 * ldw, ldw,
                                      W1 + (int64_t)b0 * ld1, ld1)));
           b0 += mc;
@@ -1264,7 +1308,7 @@ int sigma_impl(Ctx* c, int m, const T* dV, int64_t ldv, T* dW, int64_t ldw, cons
     int b0 = 0;
     while (plan->nitems && b0 < ncols) {
       const int lb = ncols - b0;
-      const int mc = lb >= 4 ? 4 : (lb >= 2 ? 2 : 1);
+      const int mc = (sizeof(T) == 4 && lb >= 8) ? 8 : (lb >= 4 ? 4 : (lb >= 2 ? 2 : 1));
       const T* Vb = V + (int64_t)b0 * ldv;
       T* Wb = W + (int64_t)b0 * ldw;
       TAcc* W1b = W1 + (int64_t)b0 * ld1;
