@@ -103,7 +103,7 @@ __global__ void k_gemm_tn_reduce(int p, int q, int nblk, int ntile, const TA* __
 }
 
 
-// k_gemm_tn_part for FP64 inputs with DF step sums and FP64 accumulators.
+// k_gemm_tn_part for FP64 inputs: DF step sums added to DF accumulators.
 __global__ void __launch_bounds__(256) k_gemm_tn_part_df(int64_t N, int p, int q, const double* __restrict__ A,
                                                          int64_t lda, const double* __restrict__ B, int64_t ldb,
                                                          double* __restrict__ part, int64_t rows_per_blk) {
@@ -115,9 +115,9 @@ __global__ void __launch_bounds__(256) k_gemm_tn_part_df(int64_t N, int p, int q
   const int p0 = tp * TN_P, q0 = tq * TN_Q;
   const int tid = threadIdx.x;
   const int ti = tid & 15, tj = tid >> 4;
-  double acc[4][2];
+  df acc[4][2];
 #pragma unroll
-  for (int u = 0; u < 4; ++u) { acc[u][0] = 0.0; acc[u][1] = 0.0; }
+  for (int u = 0; u < 4; ++u) { acc[u][0] = df{0.f, 0.f}; acc[u][1] = df{0.f, 0.f}; }
   const int64_t r_begin = blockIdx.x * rows_per_blk;
   const int64_t r_end = min(N, r_begin + rows_per_blk);
   for (int64_t r0 = r_begin; r0 < r_end; r0 += TN_ROWS) {
@@ -147,13 +147,13 @@ __global__ void __launch_bounds__(256) k_gemm_tn_part_df(int64_t N, int p, int q
       }
     }
 #pragma unroll
-    for (int u = 0; u < 4; ++u) { acc[u][0] += df_value(st[u][0]); acc[u][1] += df_value(st[u][1]); }
+    for (int u = 0; u < 4; ++u) { acc[u][0] = df_add(acc[u][0], st[u][0]); acc[u][1] = df_add(acc[u][1], st[u][1]); }
   }
   double* out = part + ((int64_t)blockIdx.x * gridDim.y + tile) * (TN_P * TN_Q);
 #pragma unroll
   for (int u = 0; u < 4; ++u) {
-    out[(ti + 16 * u) * TN_Q + tj] = acc[u][0];
-    out[(ti + 16 * u) * TN_Q + tj + 16] = acc[u][1];
+    out[(ti + 16 * u) * TN_Q + tj] = df_value(acc[u][0]);
+    out[(ti + 16 * u) * TN_Q + tj + 16] = df_value(acc[u][1]);
   }
 }
 
@@ -215,8 +215,7 @@ __global__ void __launch_bounds__(256) k_gemm_nn(int64_t N, int p, int q, T alph
   }
 }
 
-// k_gemm_nn for FP64 operands with DF products; the K sum is flushed to FP64
-// accumulators after every NN_K step.
+// k_gemm_nn for FP64 operands with DF products and DF sums over all of K.
 __global__ void __launch_bounds__(256) k_gemm_nn_df(int64_t N, int p, int q, double alpha,
                                                     const double* __restrict__ A, int64_t lda,
                                                     const double* __restrict__ B, int ldb, double beta,
@@ -227,11 +226,11 @@ __global__ void __launch_bounds__(256) k_gemm_nn_df(int64_t N, int p, int q, dou
   const int tx = tid & 15, ty = tid >> 4;
   const int64_t m0 = (int64_t)blockIdx.x * NN_M;
   const int n0 = blockIdx.y * NN_N;
-  double acc[8][4];
+  df acc[8][4];
 #pragma unroll
   for (int i = 0; i < 8; ++i)
 #pragma unroll
-    for (int j = 0; j < 4; ++j) acc[i][j] = 0.0;
+    for (int j = 0; j < 4; ++j) acc[i][j] = df{0.f, 0.f};
   for (int k0 = 0; k0 < p; k0 += NN_K) {
     __syncthreads();
     for (int l = tid; l < NN_K * NN_M; l += 256) {
@@ -244,11 +243,6 @@ __global__ void __launch_bounds__(256) k_gemm_nn_df(int64_t N, int p, int q, dou
       sB[kk][cc] = df_split((k0 + kk < p && n0 + cc < q) ? B[(int64_t)(n0 + cc) * ldb + k0 + kk] : 0.0);
     }
     __syncthreads();
-    df st[8][4];
-#pragma unroll
-    for (int i = 0; i < 8; ++i)
-#pragma unroll
-      for (int j = 0; j < 4; ++j) st[i][j] = df{0.f, 0.f};
 #pragma unroll 2
     for (int kk = 0; kk < NN_K; ++kk) {
       df a[8], b[4];
@@ -259,12 +253,8 @@ __global__ void __launch_bounds__(256) k_gemm_nn_df(int64_t N, int p, int q, dou
 #pragma unroll
       for (int i = 0; i < 8; ++i)
 #pragma unroll
-        for (int j = 0; j < 4; ++j) df_fma(st[i][j], a[i], b[j]);
+        for (int j = 0; j < 4; ++j) df_fma(acc[i][j], a[i], b[j]);
     }
-#pragma unroll
-    for (int i = 0; i < 8; ++i)
-#pragma unroll
-      for (int j = 0; j < 4; ++j) acc[i][j] += df_value(st[i][j]);
   }
 #pragma unroll
   for (int j = 0; j < 4; ++j) {
@@ -275,7 +265,7 @@ __global__ void __launch_bounds__(256) k_gemm_nn_df(int64_t N, int p, int q, dou
       const int64_t r = m0 + 8 * ty + i;
       if (r < N) {
         double prev = beta == 0.0 ? 0.0 : beta * C[(int64_t)col * ldc + r];
-        C[(int64_t)col * ldc + r] = prev + alpha * acc[i][j];
+        C[(int64_t)col * ldc + r] = prev + alpha * df_value(acc[i][j]);
       }
     }
   }

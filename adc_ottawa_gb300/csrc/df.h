@@ -13,9 +13,26 @@ namespace adcgpu {
 
 struct df { float hi, lo; };
 
+// Split without FP64 arithmetic (GB300's FP64 pipe, which also converts
+// between double and float, is 64x slower than the FP32 pipe): hi takes the
+// sign, exponent and leading 24 significant bits of x, lo the next bits
+// (together 47-48 bits; the split truncates).  |x| below 2^-126 gives 0
+// (values of that size do not occur in these products).
 __device__ __forceinline__ df df_split(double x) {
-  const float h = (float)x;
-  return df{h, (float)(x - (double)h)};
+  const unsigned long long u = (unsigned long long)__double_as_longlong(x);
+  const unsigned sgn = (unsigned)(u >> 32) & 0x80000000u;
+  const int e = (int)((u >> 52) & 0x7ff);
+  const int eh = e - 1023 + 127;
+  if (eh <= 0) return df{0.f, 0.f};
+  if (eh >= 255) return df{(float)x, 0.f};   // out of float range (and inf/nan)
+  const float hi = __int_as_float((int)(sgn | ((unsigned)eh << 23) | ((unsigned)(u >> 29) & 0x7fffffu)));
+  const unsigned r = (unsigned)(u & 0x1fffffffull);   // the 29 mantissa bits below hi
+  if (r == 0u) return df{hi, 0.f};
+  const int msb = 31 - __clz((int)r);
+  const int el = e - 1075 + msb + 127;
+  if (el <= 0) return df{hi, 0.f};
+  const unsigned ml = (msb >= 23 ? (r >> (msb - 23)) : (r << (23 - msb))) & 0x7fffffu;
+  return df{hi, __int_as_float((int)(sgn | ((unsigned)el << 23) | ml))};
 }
 
 // s += a * b

@@ -510,13 +510,15 @@ __global__ void __launch_bounds__(256) k_sigma_p2(GeomDev g, const int2* __restr
 
 // Arithmetic of the tiled pass 1.  Native: values, vectors and sums in T.
 // DF (FP64 inputs only): the C|D values and the vectors are held in shared
-// memory as double-float pairs and multiplied on the FP32 pipe (df.h); the
-// segment-A part, the diagonal term and the per-item W1 sums stay in FP64.
+// memory as double-float pairs and multiplied on the FP32 pipe (df.h), the
+// per-item W1 sums are double-float too; the segment-A part and the
+// diagonal term stay in FP64.
 template <typename T> struct NativeArith {
   typedef T S;
   __device__ __forceinline__ static S from(T x) { return x; }
   __device__ __forceinline__ static S zero() { return T(0); }
   __device__ __forceinline__ static void fma(S& acc, S a, S b) { acc += a * b; }
+  __device__ __forceinline__ static S add(S a, S b) { return a + b; }
   __device__ __forceinline__ static S shfl_add(S a, int off) { return a + __shfl_xor_sync(0xffffffffu, a, off); }
   __device__ __forceinline__ static T value(S a) { return a; }
 };
@@ -525,6 +527,7 @@ struct DfArith {
   __device__ __forceinline__ static S from(double x) { return df_split(x); }
   __device__ __forceinline__ static S zero() { return df{0.f, 0.f}; }
   __device__ __forceinline__ static void fma(S& acc, S a, S b) { df_fma(acc, a, b); }
+  __device__ __forceinline__ static S add(S a, S b) { return df_add(a, b); }
   __device__ __forceinline__ static S shfl_add(S a, int off) {
     return df_add(a, df{__shfl_xor_sync(0xffffffffu, a.hi, off), __shfl_xor_sync(0xffffffffu, a.lo, off)});
   }
@@ -595,7 +598,7 @@ template <> struct Store8<df> {
 // once at the end of the item.  Segment A (singles (a', k)) is handled per
 // tile: its W2 part gathers V through L1, its W1 part is reduced over runs
 // of equal a' and added atomically.  Segment B stays with pass 2.
-// Shared memory (bytes): T sW1[nseg*nvP*MT] | S sX[MT*(2nvP+4)] (column-major)
+// Shared memory (bytes): S sW1[nseg*nvP*MT] | S sX[MT*(2nvP+4)] (column-major)
 // | S sCD[RT*(2nvP+4)] | T sA[RT*(noP+4)] | S sV2[RT*MT] | int64 sD[RT] |
 // int sAp[RT] (row strides are multiples of 16 bytes, so the staging stores
 // are 16-byte vector stores, and 4 rows read in one warp fall into
@@ -630,7 +633,7 @@ __global__ void __launch_bounds__(256, 1) k_sigma_tile(GeomDev g, const int2* __
   const int64_t n1 = g.n1;
   const int CDS = 2 * nvP + 4, AS = noP + 4, KP = 2 * nvP + 4;
   unsigned char* p = smem_raw;
-  T* sW1 = reinterpret_cast<T*>(p); p += align16((size_t)2 * nvP * MT * sizeof(T));
+  S* sW1 = reinterpret_cast<S*>(p); p += align16((size_t)2 * nvP * MT * sizeof(S));
   S* sX = reinterpret_cast<S*>(p); p += align16((size_t)MT * (2 * nvP + 4) * sizeof(S));
   S* sCD = reinterpret_cast<S*>(p); p += align16((size_t)RT * CDS * sizeof(S));
   T* sA = reinterpret_cast<T*>(p); p += align16((size_t)RT * AS * sizeof(T));
@@ -655,7 +658,7 @@ __global__ void __launch_bounds__(256, 1) k_sigma_tile(GeomDev g, const int2* __
       const int seg = k / nvP, a = k - seg * nvP;
       sX[c * KP + k] =
           AR::from((a < nv && c < mcols) ? V[(int64_t)c * ldv + (int64_t)a * no + (seg ? lp : kp)] : T(0));
-      sW1[k * MT + c] = T(0);
+      sW1[k * MT + c] = AR::zero();
     }
     for (int row0 = item.x; row0 < item.y; row0 += RT) {
       const int nrow = min(RT, item.y - row0);
@@ -767,9 +770,9 @@ __global__ void __launch_bounds__(256, 1) k_sigma_tile(GeomDev g, const int2* __
         }
 #pragma unroll
         for (int i = 0; i < 4; ++i) {
-          T* w = sW1 + (4 * kq + i) * MT + 4 * cg;
+          S* w = sW1 + (4 * kq + i) * MT + 4 * cg;
 #pragma unroll
-          for (int cc = 0; cc < 4; ++cc) w[cc] += AR::value(sm[i][cc]);
+          for (int cc = 0; cc < 4; ++cc) w[cc] = AR::add(w[cc], sm[i][cc]);
         }
       }
       // W1 (A): runs of equal a' reduced, then added atomically
@@ -794,7 +797,7 @@ __global__ void __launch_bounds__(256, 1) k_sigma_tile(GeomDev g, const int2* __
     for (int o = tid; o < K * MT; o += 256) {
       const int k = o / MT, c = o - k * MT;
       const int seg = k / nvP, a = k - seg * nvP;
-      const T v = sW1[o];
+      const T v = AR::value(sW1[o]);
       if (a < nv && c < mcols && v != T(0))
         atomicAdd(&W1[(int64_t)c * ld1 + (int64_t)a * no + (seg ? lp : kp)], (TA)v);
     }
