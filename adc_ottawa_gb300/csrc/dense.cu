@@ -23,6 +23,21 @@ namespace {
 constexpr int TN_ROWS = 32;     // rows staged per step
 constexpr int TN_P = 64, TN_Q = 32;   // output tile
 
+// Accumulator helpers: plain types add; df accumulates with two-sums.
+template <typename A> __device__ __forceinline__ A acc_zero() { return A(0); }
+template <> __device__ __forceinline__ df acc_zero<df>() { return df{0.f, 0.f}; }
+template <typename A, typename X> __device__ __forceinline__ void acc_add(A& a, X x) { a += (A)x; }
+__device__ __forceinline__ void acc_add(df& a, float x) { a = df_add(a, df{x, 0.f}); }
+template <typename R, typename A> __device__ __forceinline__ R acc_value(A a) { return (R)a; }
+template <> __device__ __forceinline__ double acc_value<double, df>(df a) { return df_value(a); }
+
+// double -> float without the FP64 pipe (truncating: relative error < 2^-23)
+template <typename T, typename TB> __device__ __forceinline__ T to_t(TB x) { return (T)x; }
+template <> __device__ __forceinline__ float to_t<float, double>(double x) { return df_split(x).hi; }
+
+__device__ __forceinline__ void sq_add(double& a, double v) { a += v * v; }
+__device__ __forceinline__ void sq_add(df& a, float v) { df_fma(a, df{v, 0.f}, df{v, 0.f}); }
+
 // Partial C tiles: part[(blk * ntile + tile) * TN_P * TN_Q + ...]
 // Block: a range of rows; output tile TN_P x TN_Q (64 x 32); thread -> 8
 // outputs (p = ti + 16 u, q = tj + 16 v), conflict-free shared-memory reads.
@@ -41,9 +56,13 @@ __global__ void __launch_bounds__(256) k_gemm_tn_part(int64_t N, int p, int q, c
   const int p0 = tp * TN_P, q0 = tq * TN_Q;
   const int tid = threadIdx.x;
   const int ti = tid & 15, tj = tid >> 4;
-  TA acc[4][2];
+  // FP32 inputs: the step sums go into double-float accumulators (FP32-pipe
+  // two-sums) instead of FP64 adds; FP64 inputs accumulate in FP64
+  typedef typename std::conditional<std::is_same<T, float>::value && std::is_same<TA, double>::value, df, TA>::type
+      TAcc;
+  TAcc acc[4][2];
 #pragma unroll
-  for (int u = 0; u < 4; ++u) { acc[u][0] = TA(0); acc[u][1] = TA(0); }
+  for (int u = 0; u < 4; ++u) { acc[u][0] = acc_zero<TAcc>(); acc[u][1] = acc_zero<TAcc>(); }
   const int64_t r_begin = blockIdx.x * rows_per_blk;
   const int64_t r_end = min(N, r_begin + rows_per_blk);
   for (int64_t r0 = r_begin; r0 < r_end; r0 += TN_ROWS) {
@@ -73,13 +92,13 @@ __global__ void __launch_bounds__(256) k_gemm_tn_part(int64_t N, int p, int q, c
       }
     }
 #pragma unroll
-    for (int u = 0; u < 4; ++u) { acc[u][0] += (TA)st[u][0]; acc[u][1] += (TA)st[u][1]; }
+    for (int u = 0; u < 4; ++u) { acc_add(acc[u][0], st[u][0]); acc_add(acc[u][1], st[u][1]); }
   }
   TA* out = part + ((int64_t)blockIdx.x * gridDim.y + tile) * (TN_P * TN_Q);
 #pragma unroll
   for (int u = 0; u < 4; ++u) {
-    out[(ti + 16 * u) * TN_Q + tj] = acc[u][0];
-    out[(ti + 16 * u) * TN_Q + tj + 16] = acc[u][1];
+    out[(ti + 16 * u) * TN_Q + tj] = acc_value<TA>(acc[u][0]);
+    out[(ti + 16 * u) * TN_Q + tj + 16] = acc_value<TA>(acc[u][1]);
   }
 }
 
@@ -184,7 +203,7 @@ __global__ void __launch_bounds__(256) k_gemm_nn(int64_t N, int p, int q, T alph
     }
     for (int l = tid; l < NN_K * NN_N; l += 256) {
       const int kk = l / NN_N, cc = l % NN_N;
-      sB[kk][cc] = (k0 + kk < p && n0 + cc < q) ? (T)B[(int64_t)(n0 + cc) * ldb + k0 + kk] : T(0);
+      sB[kk][cc] = (k0 + kk < p && n0 + cc < q) ? to_t<T, TB>(B[(int64_t)(n0 + cc) * ldb + k0 + kk]) : T(0);
     }
     __syncthreads();
 #pragma unroll
@@ -332,12 +351,16 @@ __global__ void k_resid(int64_t N, int nb, const T* __restrict__ X, const T* __r
   __shared__ double red[8];
   const int lane = threadIdx.x & 31, w = threadIdx.x >> 5;
   for (int i = 0; i < nb; ++i) {
-    double s2 = 0.0;
+    // FP32 vectors: squares summed in double-float on the FP32 pipe
+    typedef typename std::conditional<std::is_same<T, float>::value, df, double>::type TS;
+    TS s2a = acc_zero<TS>();
+    const T li = (T)lam[i];
     for (int64_t r = blockIdx.x * (int64_t)blockDim.x + threadIdx.x; r < N; r += (int64_t)gridDim.x * blockDim.x) {
-      T v = -WY[(int64_t)i * ld + r] + (T)lam[i] * X[(int64_t)i * ld + r];
+      T v = -WY[(int64_t)i * ld + r] + li * X[(int64_t)i * ld + r];
       Rout[(int64_t)i * ld + r] = v;
-      s2 += (double)v * (double)v;
+      sq_add(s2a, v);
     }
+    double s2 = acc_value<double>(s2a);
     for (int o = 16; o; o >>= 1) s2 += __shfl_xor_sync(0xffffffffu, s2, o);
     if (lane == 0) red[w] = s2;
     __syncthreads();
