@@ -510,9 +510,8 @@ __global__ void __launch_bounds__(256) k_sigma_p2(GeomDev g, const int2* __restr
 
 // Arithmetic of the tiled pass 1.  Native: values, vectors and sums in T.
 // DF (FP64 inputs only): the C|D values and the vectors are held in shared
-// memory as double-float pairs and multiplied on the FP32 pipe (df.h), the
-// per-item W1 sums are double-float too; the segment-A part and the
-// diagonal term stay in FP64.
+// memory as double-float pairs and multiplied on the FP32 pipe (df.h), and so
+// are segment A and the per-item W1 sums; only the diagonal term is FP64.
 template <typename T> struct NativeArith {
   typedef T S;
   __device__ __forceinline__ static S from(T x) { return x; }
@@ -521,6 +520,7 @@ template <typename T> struct NativeArith {
   __device__ __forceinline__ static S add(S a, S b) { return a + b; }
   __device__ __forceinline__ static S shfl_add(S a, int off) { return a + __shfl_xor_sync(0xffffffffu, a, off); }
   __device__ __forceinline__ static T value(S a) { return a; }
+  __device__ __forceinline__ static bool nonzero(S a) { return a != T(0); }
 };
 struct DfArith {
   typedef df S;
@@ -532,6 +532,7 @@ struct DfArith {
     return df_add(a, df{__shfl_xor_sync(0xffffffffu, a.hi, off), __shfl_xor_sync(0xffffffffu, a.lo, off)});
   }
   __device__ __forceinline__ static double value(S a) { return df_value(a); }
+  __device__ __forceinline__ static bool nonzero(S a) { return a.hi != 0.f || a.lo != 0.f; }
 };
 
 template <typename T> struct DfArithSel { typedef NativeArith<T> type; };
@@ -599,7 +600,7 @@ template <> struct Store8<df> {
 // tile: its W2 part gathers V through L1, its W1 part is reduced over runs
 // of equal a' and added atomically.  Segment B stays with pass 2.
 // Shared memory (bytes): S sW1[nseg*nvP*MT] | S sX[MT*(2nvP+4)] (column-major)
-// | S sCD[RT*(2nvP+4)] | T sA[RT*(noP+4)] | S sV2[RT*MT] | int64 sD[RT] |
+// | S sCD[RT*(2nvP+4)] | S sA[RT*(noP+4)] | S sV2[RT*MT] | int64 sD[RT] |
 // int sAp[RT] (row strides are multiples of 16 bytes, so the staging stores
 // are 16-byte vector stores, and 4 rows read in one warp fall into
 // different banks).
@@ -613,7 +614,7 @@ inline size_t tile_smem_bytes(int nvP, int noP, int MT, size_t sT, size_t sS) {
   size_t b = align16((size_t)2 * nvP * MT * sT);
   b += align16((size_t)MT * (2 * nvP + 4) * sS);
   b += align16((size_t)TILE_RT * (2 * nvP + 4) * sS);
-  b += align16((size_t)TILE_RT * (noP + 4) * sT);
+  b += align16((size_t)TILE_RT * (noP + 4) * sS);
   b += align16((size_t)TILE_RT * MT * sS);
   b += align16((size_t)TILE_RT * 8);
   b += align16((size_t)TILE_RT * 4);
@@ -636,7 +637,7 @@ __global__ void __launch_bounds__(256, 1) k_sigma_tile(GeomDev g, const int2* __
   S* sW1 = reinterpret_cast<S*>(p); p += align16((size_t)2 * nvP * MT * sizeof(S));
   S* sX = reinterpret_cast<S*>(p); p += align16((size_t)MT * (2 * nvP + 4) * sizeof(S));
   S* sCD = reinterpret_cast<S*>(p); p += align16((size_t)RT * CDS * sizeof(S));
-  T* sA = reinterpret_cast<T*>(p); p += align16((size_t)RT * AS * sizeof(T));
+  S* sA = reinterpret_cast<S*>(p); p += align16((size_t)RT * AS * sizeof(S));
   S* sV2 = reinterpret_cast<S*>(p); p += align16((size_t)RT * MT * sizeof(S));
   int64_t* sD = reinterpret_cast<int64_t*>(p); p += align16((size_t)RT * 8);
   int* sAp = reinterpret_cast<int*>(p);
@@ -686,14 +687,10 @@ __global__ void __launch_bounds__(256, 1) k_sigma_tile(GeomDev g, const int2* __
 #pragma unroll
           for (int u = 0; u < 8; ++u) v[u] = T(0);
         }
-        if (q < nchK) {
-          S w[8];
+        S w[8];
 #pragma unroll
-          for (int u = 0; u < 8; ++u) w[u] = AR::from(v[u]);
-          Store8<S>::go(sCD + rr * CDS + 8 * q, w);
-        } else {
-          Store8<T>::go(sA + rr * AS + 8 * (q - nchK), v);
-        }
+        for (int u = 0; u < 8; ++u) w[u] = AR::from(v[u]);
+        Store8<S>::go(q < nchK ? sCD + rr * CDS + 8 * q : sA + rr * AS + 8 * (q - nchK), w);
       }
       __syncthreads();
       for (int o = tid; o < RT * MT; o += 256) {
@@ -740,14 +737,13 @@ __global__ void __launch_bounds__(256, 1) k_sigma_tile(GeomDev g, const int2* __
           if (rr >= nrow || c >= mcols) continue;
           const int ap = sAp[rr];
           const int64_t d = sD[rr];
-          const T* arow = sA + rr * AS;
+          const S* arow = sA + rr * AS;
           const T* vs = V + (int64_t)c * ldv + (int64_t)ap * no;
-          T sa = T(0);
+          S sa = acc[q / CT][q % CT];
           // padded A entries are zero; (ap, kk >= no) stays inside the V column
 #pragma unroll 8
-          for (int kk = 0; kk < noP; ++kk) sa += arow[kk] * vs[kk];
-          W[(int64_t)c * ldw + n1 + d] =
-              diag[n1 + d] * AR::value(sV2[rr * MT + c]) + (sa + AR::value(acc[q / CT][q % CT]));
+          for (int kk = 0; kk < noP; ++kk) AR::fma(sa, arow[kk], AR::from(vs[kk]));
+          W[(int64_t)c * ldw + n1 + d] = diag[n1 + d] * AR::value(sV2[rr * MT + c]) + AR::value(sa);
         }
       }
       // W1 (C|D): thread owns 4 k x 4 columns; sums over the tile's rows
@@ -779,18 +775,18 @@ __global__ void __launch_bounds__(256, 1) k_sigma_tile(GeomDev g, const int2* __
       for (int o = tid; o < noP * MT; o += 256) {
         const int kk = o % noP, c = o / noP;
         if (kk >= no || c >= mcols) continue;
-        T sacc = T(0);
+        S sacc = AR::zero();
         int prev = sAp[0];
         for (int rr = 0; rr < nrow; ++rr) {
           const int ap = sAp[rr];
           if (ap != prev) {
-            if (sacc != T(0)) atomicAdd(&W1[(int64_t)c * ld1 + (int64_t)prev * no + kk], (TA)sacc);
-            sacc = T(0);
+            if (AR::nonzero(sacc)) atomicAdd(&W1[(int64_t)c * ld1 + (int64_t)prev * no + kk], (TA)AR::value(sacc));
+            sacc = AR::zero();
             prev = ap;
           }
-          sacc += sA[rr * AS + kk] * AR::value(sV2[rr * MT + c]);
+          AR::fma(sacc, sA[rr * AS + kk], sV2[rr * MT + c]);
         }
-        if (sacc != T(0)) atomicAdd(&W1[(int64_t)c * ld1 + (int64_t)prev * no + kk], (TA)sacc);
+        if (AR::nonzero(sacc)) atomicAdd(&W1[(int64_t)c * ld1 + (int64_t)prev * no + kk], (TA)AR::value(sacc));
       }
     }
     __syncthreads();
