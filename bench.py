@@ -47,10 +47,12 @@ def parse():
     ap.add_argument("--no-fp64", action="store_true", help="skip the FP64 GPU comparison solve")
     ap.add_argument("--no-e2e", action="store_true")
     ap.add_argument("--no-cpu", action="store_true")
-    ap.add_argument("--suite", default="davidson", choices=["davidson", "lanczos", "sil", "batch"],
+    ap.add_argument("--suite", default="davidson", choices=["davidson", "lanczos", "sil", "batch", "learned"],
                     help="davidson: the headline solve (default); lanczos: nocc=10/nvirt=110 block Lanczos, "
                          "b=10, 300 cycles; sil: 32 wavepackets on the nocc=10/nvirt=110 matrix, Krylov dim 15, "
-                         "dt=0.05 au (--sil-steps steps timed); batch: 64 seeded systems, 8 roots each")
+                         "dt=0.05 au (--sil-steps steps timed); batch: 64 seeded systems, 8 roots each; "
+                         "learned: nocc=20/nvirt=240, 30 roots, diagonal vs learned vs folded preconditioner")
+    ap.add_argument("--train-systems", type=int, default=200)
     ap.add_argument("--sil-steps", type=int, default=20)
     return ap.parse_args()
 
@@ -394,6 +396,54 @@ def run_batch(args):
                     total_N=int(sum(r["N"] for r in res)))
 
 
+def run_learned(args):
+    """nocc=20, nvirt=240 (N = 11,527,200), 30 roots to 1e-6 on the mixed
+    ladder with the diagonal (DPR), learned (MLP trained here by the
+    library's kernels on --train-systems seeded small systems) and folded
+    preconditioners: iterations and wall time of each."""
+    import numpy as np
+
+    from adc_ottawa_gb300 import (ADCGPU_MIXED, PRECON_DPR, PRECON_FOLD, PRECON_MLP, AdcGpu, autotune,
+                                  mlp_train, synth_system)
+
+    t = time.perf_counter()
+    samples = []
+    for no_, nv_, seed in mlp_train.random_systems(args.train_systems):
+        samples += mlp_train.make_samples(no_, nv_, seed)
+    params, losses = mlp_train.train(samples, steps=600)
+    train_s = time.perf_counter() - t
+    no, nv, nroots = 20, 240, 30
+    e, eri = synth_system(no, nv, 11)
+    g = AdcGpu(0)
+    g.set_orbitals(no, nv, e)
+    g.set_eri_packed(eri)
+    t = time.perf_counter()
+    nnz = g.write_fspace_adc2_1(None, precision=ADCGPU_MIXED)
+    build_s = time.perf_counter() - t
+    autotune.tune(g, max(nroots + 5, 2 * nroots), ADCGPU_MIXED)
+    mlp_train.load_into(g, params)
+    rows, ref = {}, None
+    for name, pc in (("diagonal", PRECON_DPR), ("learned", PRECON_MLP), ("fold", PRECON_FOLD)):
+        t = time.perf_counter()
+        r = g.davdiag_block(nroots, TOL, precon=pc, precision=ADCGPU_MIXED, want_vectors=False,
+                            raise_on_nonconv=False, maxiter=200)
+        sec = time.perf_counter() - t
+        if ref is None:
+            ref = r.evals
+        rows[name] = {"seconds": sec, "iterations": r.iterations,
+                      "phase_iterations": [r.iters_bf16, r.iters_fp32, r.iters_fp64], "status": r.status,
+                      "max_abs_dE_vs_diagonal": float(np.abs(r.evals - ref).max())}
+    _secondary_line("30 roots to 1e-6 on nocc=20/nvirt=240: mixed ladder with the learned preconditioner",
+                    rows["learned"]["seconds"], "s", 1, 0,
+                    {"workload": f"ADC(2)-s nocc={no} nvirt={nv} N={g.ndim} davidson {nroots} roots tol {TOL}",
+                     "nnz_kept": nnz, "build_s": build_s},
+                    preconditioners=rows, training={"systems": args.train_systems, "samples": len(samples),
+                                                   "seconds": train_s,
+                                                   "loss_first_last": [float(losses[:30].mean()),
+                                                                       float(losses[-30:].mean())]})
+    g.close()
+
+
 if __name__ == "__main__":
     a = parse()
     if a.impl == "reference":
@@ -404,5 +454,7 @@ if __name__ == "__main__":
         run_sil(a)
     elif a.suite == "batch":
         run_batch(a)
+    elif a.suite == "learned":
+        run_learned(a)
     else:
         run_gb300(a)
