@@ -80,6 +80,10 @@ struct DavidsonGPU {
   int nstates, blocksize, maxvec, niter, ipre;
   bool ldeflate;
   double tol;
+  // lower-precision phases of the mixed ladder: stop (not converged) when
+  // the largest residual of the unconverged roots has not fallen by 10 %
+  // within this many iterations (0: never), i.e. at the phase's floor
+  int stall_iters = 0;
   const T* hii;            // device diagonal in T
   const MlpPrecond* mlp = nullptr;
   // device arrays
@@ -251,6 +255,8 @@ struct DavidsonGPU {
 
     int currdim = blocksize, bs_curr = blocksize, maxvec_curr = maxvec, nstates_curr = nstates;
     int nconv = 0, nconv_prev = 0, nW = 0, iters = 0;
+    double stall_best = 1e300;
+    int stall_since = 0;
     std::vector<double> val(maxvec), vec((size_t)maxvec * maxvec), lam(blocksize), norm(blocksize), Y;
     std::vector<double> S;
     for (int k = 1; k <= niter; ++k) {
@@ -293,6 +299,13 @@ struct DavidsonGPU {
       for (int i = 0; i < nstates_curr; ++i)
         if (norm[i] < tol) ++nconv;
       if (nconv == nstates) break;
+      if (stall_iters > 0) {
+        double cur = 0.0;
+        for (int i = 0; i < nstates_curr; ++i)
+          if (!(norm[i] < tol)) cur = std::max(cur, norm[i]);
+        if (cur < 0.9 * stall_best) { stall_best = cur; stall_since = 0; }
+        else if (++stall_since >= stall_iters) break;
+      }
 
       // subspace_expansion
       const bool deflated = ldeflate && nconv > nconv_prev;
@@ -523,6 +536,7 @@ int davidson_solve(Ctx* c, const adcgpu_dav_params* p, double* evals, double* ev
       D.niter = p->maxiter; D.ipre = p->precon; D.ldeflate = p->ldfl != 0;
       D.tol = std::max(p->davtol, phase == 0 ? tol_b : tol_f);
       D.hii = c->d_diag32; D.mlp = mlp;
+      D.stall_iters = 12;
       int it = 0, nc = 0;
       st = D.run(hdiag, nguess ? 2 : guess_kind, p->guessdim, g32, nguess, ev, g32, blocksize, &nguess, &it, &nc);
       inf.iterations += it; inf.nmult += D.nmult; inf.sigma_seconds += D.sigma_s;

@@ -178,7 +178,9 @@ typedef struct {
                         over to the FP32-valued phase (0: 1e-2; <0: skip)    */
   double tol_fp32;   /* MIXED: residual at which the FP32 phase hands over to
                         the FP64 refinement (0: 1e-5 with ADCGPU_PRECON_FOLD,
-                        5e-6 otherwise)                                      */
+                        5e-6 otherwise); the BF16 and FP32 phases also hand
+                        over when their largest residual has not fallen by
+                        10 % in 12 iterations (their precision floor)        */
 } adcgpu_dav_params;
 
 typedef struct {
