@@ -11,6 +11,20 @@ namespace adcgpu {
 
 std::atomic<unsigned long long> g_kernel_launches{0};
 
+int smem_optin_max(Ctx* c) {
+  static std::atomic<int> cached[64];
+  const int dev = (c && c->device >= 0 && c->device < 64) ? c->device : 0;
+  int v = cached[dev].load();
+  if (v <= 0) {
+    if (cudaDeviceGetAttribute(&v, cudaDevAttrMaxSharedMemoryPerBlockOptin, dev) != cudaSuccess || v <= 0) {
+      cudaGetLastError();
+      v = 48 * 1024;
+    }
+    cached[dev].store(v);
+  }
+  return v;
+}
+
 int set_err(Ctx* c, int code, const std::string& msg) {
   if (c) c->err = msg;
   return code;

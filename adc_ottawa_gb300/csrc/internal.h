@@ -257,6 +257,8 @@ extern std::atomic<unsigned long long> g_kernel_launches;
 
 // error helpers
 int set_err(Ctx* c, int code, const std::string& msg);
+// the device's opt-in maximum of dynamic shared memory per block (cached)
+int smem_optin_max(Ctx* c);
 // propagate a non-zero status
 #define ST(x)                 \
   do {                        \

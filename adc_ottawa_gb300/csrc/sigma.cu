@@ -1177,7 +1177,9 @@ int launch_tile(Ctx* c, const GeomDev& g, const SigmaPlan* plan, const TV* Bt, c
   // FP64 inputs in the mixed ladder's refinement: double-float arithmetic
   auto kern = (sizeof(T) == 8 && c->dense_df) ? k_sigma_tile<T, TV, TA, MT, DfArithFor<T>>
                                               : k_sigma_tile<T, TV, TA, MT, NativeArith<T>>;
-  ADC_CUDA(c, cudaFuncSetAttribute(kern, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem));
+  // the cap is a property of the kernel, shared by every context and host
+  // thread: set it to the device's opt-in maximum, never to this call's size
+  ADC_CUDA(c, cudaFuncSetAttribute(kern, cudaFuncAttributeMaxDynamicSharedMemorySize, smem_optin_max(c)));
   ADC_CUDA(c, cudaFuncSetAttribute(kern, cudaFuncAttributePreferredSharedMemoryCarveout, 100));
   const int grid = std::min(plan->ntitems, 152 * 2);
   kern<<<grid, 256, smem, c->stream>>>(g, plan->d_titems, plan->ntitems, Bt, diag, V, ldv, ncols, W, ldw, W1,
@@ -1191,7 +1193,7 @@ int launch_tile_mma(Ctx* c, const GeomDev& g, const SigmaPlan* plan, const __nv_
                     const float* V, int64_t ldv, int ncols, float* W, int64_t ldw, TA* W1, int64_t ld1) {
   const size_t smem = tile_mma_smem_bytes(g.nvP, g.noP);
   auto kern = k_sigma_tile_mma<TA>;
-  ADC_CUDA(c, cudaFuncSetAttribute(kern, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem));
+  ADC_CUDA(c, cudaFuncSetAttribute(kern, cudaFuncAttributeMaxDynamicSharedMemorySize, smem_optin_max(c)));
   ADC_CUDA(c, cudaFuncSetAttribute(kern, cudaFuncAttributePreferredSharedMemoryCarveout, 100));
   const int grid = std::min(plan->ntitems, 152 * 2);
   kern<<<grid, 256, smem, c->stream>>>(g, plan->d_titems, plan->ntitems, Bt, diag, V, ldv, ncols, W, ldw, W1,
@@ -1268,7 +1270,7 @@ int sigma_impl(Ctx* c, int m, const T* dV, int64_t ldv, T* dW, int64_t ldw, cons
   // FP32: 16 columns keep two blocks per SM (their loads overlap the other's
   // arithmetic); FP64 is bound by the FP64 pipe at one block per SM
   constexpr int MTMAX = 16;
-  const size_t smax = 227 * 1024;
+  const size_t smax = (size_t)smem_optin_max(c);
   int mt_fit = 0;
   for (int mt = MTMAX; mt >= 8 && !mt_fit; mt /= 2)
     if (tile_smem_bytes(G.nvP, G.noP, mt, sizeof(T), sizeof(T)) <= smax) mt_fit = mt;
