@@ -5,6 +5,8 @@
 #include <cstring>
 #include <vector>
 
+#include <cmath>
+
 #include "internal.h"
 
 namespace adcgpu {
@@ -50,7 +52,18 @@ void dfree(Ctx* c, void* p, size_t bytes) {
   if (bytes) c->dev_bytes -= (int64_t)bytes;
 }
 
+static void join_diag_order(Ctx* c) {
+  if (c->diag_order_thread.joinable()) c->diag_order_thread.join();
+}
+
+const std::vector<int64_t>& diag_order(Ctx* c) {
+  join_diag_order(c);
+  return c->diag_order;
+}
+
 static void free_matrix(Ctx* c) {
+  join_diag_order(c);
+  c->diag_order.clear();
   void** ps[] = {(void**)&c->d_diag, (void**)&c->d_A, (void**)&c->d_Bt, (void**)&c->d_A32, (void**)&c->d_Bt16,
                  (void**)&c->d_Bt32, (void**)&c->d_diag32, (void**)&c->d_rowcount, &c->d_ws};
   for (void** p : ps) {
@@ -234,6 +247,16 @@ int adcgpu_build_adc2s(adcgpu_ctx* h, int ndim, const int32_t* kpq, int64_t* nof
     if (st) return st;
   }
   ADC_CUDA(c, cudaStreamSynchronize(c->stream));
+  {
+    // the guess selection order of |hii| (initvec_ondiag), sorted on a host
+    // thread while the caller goes on (it depends only on the diagonal)
+    std::vector<double> ah((size_t)c->geom.N);
+    ADC_CUDA(c, cudaMemcpy(ah.data(), c->d_diag, sizeof(double) * ah.size(), cudaMemcpyDeviceToHost));
+    c->diag_order_thread = std::thread([c, ah = std::move(ah)]() mutable {
+      for (double& x : ah) x = std::fabs(x);
+      host_heapsort_index((int64_t)ah.size(), ah.data(), c->diag_order);
+    });
+  }
   c->flag = flag;
   c->have_matrix = true;
   if (noffd_out) *noffd_out = c->nnz_kept;

@@ -209,10 +209,9 @@ struct DavidsonGPU {
   // initvec_ondiag (block_davidson.f90:463-532): unit vectors at the
   // blocksize smallest |hii| in heapsort order.
   int guess_ondiag(const std::vector<double>& hdiag) {
-    std::vector<double> ah(N);
-    for (int64_t i = 0; i < N; ++i) ah[i] = std::fabs(hdiag[i]);
-    std::vector<int64_t> indx;
-    host_heapsort_index(N, ah.data(), indx);
+    (void)hdiag;
+    const std::vector<int64_t>& indx = diag_order(c);   // heapsort of |hii|, from the build
+    if ((int64_t)indx.size() != N) return set_err(c, ADCGPU_NO_MATRIX, "diagonal order missing");
     const T one = T(1);
     for (int i = 0; i < blocksize; ++i) {
       int64_t k = indx[i] - 1;

@@ -41,6 +41,7 @@
 #include <cuda_runtime.h>
 #include <stdint.h>
 #include <atomic>
+#include <thread>
 #include <string>
 #include <vector>
 
@@ -227,6 +228,11 @@ struct Ctx {
   float* d_diag32 = nullptr;
   int mixed_bf16 = 1;             // 1: B^T stored as bf16, 0: fp32
   int dense_df = 0;               // FP64 GEMMs in double-float on the FP32 pipe
+  // heapsort order (1-based, the reference's dsortindxa1 tie order) of |hii|,
+  // the initvec_ondiag guess selection: computed on a host thread from the
+  // end of the matrix build, joined by the first solve that needs it
+  std::vector<int64_t> diag_order;
+  std::thread diag_order_thread;
   int64_t nnz_kept = 0;           // reference noffd
   int64_t nnz_ph = 0;             // kept ph-ph entries
   int64_t* d_rowcount = nullptr;  // kept entries per double row (for COO export)
@@ -259,6 +265,8 @@ extern std::atomic<unsigned long long> g_kernel_launches;
 int set_err(Ctx* c, int code, const std::string& msg);
 // the device's opt-in maximum of dynamic shared memory per block (cached)
 int smem_optin_max(Ctx* c);
+// |hii| heapsort order of the built matrix (waits for the build's host thread)
+const std::vector<int64_t>& diag_order(Ctx* c);
 // propagate a non-zero status
 #define ST(x)                 \
   do {                        \
