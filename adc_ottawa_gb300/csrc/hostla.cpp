@@ -239,32 +239,37 @@ void host_triu_inverse(int n, const double* R, double* Ri) {
 // The order of equal keys is that of the heap construction, as in the
 // reference, because the Davidson guess vectors are taken from it.
 void host_heapsort_index(int64_t n, const double* arrin, std::vector<int64_t>& indx) {
+  // The keys travel with their indices (one array of pairs), so a sift step
+  // reads one location instead of an index and then its key; comparisons and
+  // moves are those of the index-array formulation, so the permutation, and
+  // the order of ties, is the same.
+  struct KI { double key; int64_t idx; };
   indx.resize(n);
-  for (int64_t i = 0; i < n; ++i) indx[i] = i + 1;
-  if (n == 1) return;
-  auto arr = [&](int64_t k) { return arrin[k - 1]; };
-  int64_t l = n / 2 + 1, ir = n, indxt, i, j;
-  double q;
+  if (n <= 0) return;
+  if (n == 1) { indx[0] = 1; return; }
+  std::vector<KI> h((size_t)n);
+  for (int64_t i = 0; i < n; ++i) h[i] = KI{arrin[i], i + 1};
+  int64_t l = n / 2 + 1, ir = n, i, j;
+  KI t;
   for (;;) {
     if (l > 1) {
       l = l - 1;
-      indxt = indx[l - 1];
-      q = arr(indxt);
+      t = h[l - 1];
     } else {
-      indxt = indx[ir - 1];
-      q = arr(indxt);
-      indx[ir - 1] = indx[0];
+      t = h[ir - 1];
+      h[ir - 1] = h[0];
       ir = ir - 1;
-      if (ir == 1) { indx[0] = indxt; return; }
+      if (ir == 1) { h[0] = t; break; }
     }
     i = l; j = l + l;
     while (j <= ir) {
-      if (j < ir && arr(indx[j - 1]) < arr(indx[j])) j = j + 1;
-      if (q < arr(indx[j - 1])) { indx[i - 1] = indx[j - 1]; i = j; j = j + j; }
+      if (j < ir && h[j - 1].key < h[j].key) j = j + 1;
+      if (t.key < h[j - 1].key) { h[i - 1] = h[j - 1]; i = j; j = j + j; }
       else j = ir + 1;
     }
-    indx[i - 1] = indxt;
+    h[i - 1] = t;
   }
+  for (int64_t k = 0; k < n; ++k) indx[k] = h[k].idx;
 }
 
 }  // namespace adcgpu
