@@ -1,0 +1,75 @@
+"""The library's host linear algebra (csrc/hostla.cpp), on the CPU:
+
+- the band reduction that gives the Lanczos T eigenvalues (dsbev('N') in
+  diagmat_banded, block_lanczos.f90:2006-2052) against dense numpy eigvalsh;
+- the dense tred2/tql2 eigensolver against numpy;
+- the heapsort that selects the Davidson guess vectors (dsortindxa1,
+  initvec_ondiag block_davidson.f90:463-532) against the oracle's
+  restatement, including the order of ties.
+"""
+import os
+import shutil
+import subprocess
+
+import numpy as np
+import pytest
+
+import oracle
+
+ROOT = os.path.dirname(os.path.dirname(os.path.abspath(__file__)))
+
+
+@pytest.fixture(scope="module")
+def driver(tmp_path_factory):
+    gxx = shutil.which("g++")
+    if gxx is None:
+        pytest.skip("g++ not available")
+    nvcc = shutil.which("nvcc")
+    cuda_home = os.environ.get("CUDA_HOME") or (os.path.dirname(os.path.dirname(nvcc)) if nvcc else "")
+    cuda_inc = os.path.join(cuda_home, "include")
+    if not os.path.exists(os.path.join(cuda_inc, "cuda_runtime.h")):
+        pytest.skip("CUDA headers not found")
+    out = str(tmp_path_factory.mktemp("hostla") / "hostla_driver")
+    cmd = [gxx, "-O2", "-std=c++17", "-I", os.path.join(ROOT, "adc_ottawa_gb300", "csrc"), "-I", cuda_inc,
+           os.path.join(ROOT, "tests", "host", "hostla_driver.cpp"),
+           os.path.join(ROOT, "adc_ottawa_gb300", "csrc", "hostla.cpp"), "-o", out]
+    subprocess.run(cmd, check=True)
+    return out
+
+
+def run(driver, mode, header, data, tmp_path, out_dtype, n):
+    fin, fout = str(tmp_path / "in.bin"), str(tmp_path / "out.bin")
+    with open(fin, "wb") as f:
+        f.write(np.array(header, np.int32).tobytes())
+        f.write(np.ascontiguousarray(data, np.float64).tobytes(order="F"))
+    subprocess.run([driver, mode, fin, fout], check=True)
+    return np.fromfile(fout, out_dtype, n)
+
+
+@pytest.mark.parametrize("n,kd", [(1, 0), (7, 1), (50, 3), (300, 10), (640, 10)])
+def test_band_eigenvalues(driver, tmp_path, n, kd):
+    rs = np.random.RandomState(n + kd)
+    A = np.zeros((n, n))
+    for d in range(kd + 1):
+        v = rs.standard_normal(n - d)
+        A[np.arange(d, n), np.arange(n - d)] = v
+        A[np.arange(n - d), np.arange(d, n)] = v
+    w = run(driver, "sbev", [n, kd], np.asfortranarray(A), tmp_path, np.float64, n)
+    ref = np.linalg.eigvalsh(A)
+    assert np.abs(w - ref).max() <= 1e-12 * max(1.0, np.abs(ref).max())
+
+
+def test_dense_eigenvalues(driver, tmp_path):
+    rs = np.random.RandomState(3)
+    B = rs.standard_normal((120, 120))
+    A = B + B.T
+    w = run(driver, "syev", [120], np.asfortranarray(A), tmp_path, np.float64, 120)
+    assert np.abs(w - np.linalg.eigvalsh(A)).max() <= 1e-12 * np.abs(A).max() * 10
+
+
+@pytest.mark.parametrize("n", [1, 6, 1000, 65537])
+def test_heapsort_matches_reference_order(built, driver, tmp_path, n):
+    rs = np.random.RandomState(n)
+    arr = np.round(rs.uniform(0.0, 3.0, n) * 4) / 4          # many ties
+    idx = run(driver, "heap", [n], arr, tmp_path, np.int64, n)
+    assert np.array_equal(idx, oracle.heapsort_index(arr).astype(np.int64))
