@@ -25,15 +25,6 @@ namespace adcgpu {
 
 namespace {
 
-template <typename TV> __device__ __forceinline__ float tofloat(TV x);
-template <> __device__ __forceinline__ float tofloat<float>(float x) { return x; }
-template <> __device__ __forceinline__ float tofloat<__nv_bfloat16>(__nv_bfloat16 x) { return __bfloat162float(x); }
-
-template <typename T, typename TV> struct Acc;
-template <> struct Acc<double, double> { __device__ static double v(double x) { return x; } };
-template <> struct Acc<float, float> { __device__ static float v(float x) { return x; } };
-template <> struct Acc<float, __nv_bfloat16> { __device__ static float v(__nv_bfloat16 x) { return __bfloat162float(x); } };
-
 // 8 consecutive stored values -> T (one 16-byte load for BF16, two for FP32,
 // four for FP64; segments start on 16-byte boundaries).
 template <typename T, typename TV> struct Load8;
