@@ -32,6 +32,7 @@ class DavParams(C.Structure):
         ("refine", C.c_int),
         ("tol_bf16", C.c_double),
         ("tol_fp32", C.c_double),
+        ("refine_block", C.c_int),
     ]
 
 

@@ -210,10 +210,11 @@ class AdcGpu:
                       precon: int = PRECON_DPR, ldfl: bool = True, lsubdiag: bool = False, guessdim: int = 800,
                       precision: int = ADCGPU_FP64, refine: int = 0, tol_bf16: float = 0.0,
                       tol_fp32: float = 0.0, want_vectors: bool = True,
-                      raise_on_nonconv: bool = True) -> DavidsonResult:
+                      raise_on_nonconv: bool = True, refine_block: int = 0) -> DavidsonResult:
         p = DavParams(davstates=davstates, dmain=dmain, maxsubdim=maxsubdim, maxiter=maxiter, precon=precon,
                       ldfl=int(ldfl), lsubdiag=int(lsubdiag), guessdim=guessdim, davtol=davtol,
-                      precision=precision, refine=refine, tol_bf16=tol_bf16, tol_fp32=tol_fp32)
+                      precision=precision, refine=refine, tol_bf16=tol_bf16, tol_fp32=tol_fp32,
+                      refine_block=refine_block)
         ev = np.empty(davstates)
         vec = np.empty((self.ndim, davstates), order="F") if want_vectors else None
         info = DavInfo()

@@ -551,8 +551,15 @@ int davidson_solve(Ctx* c, const adcgpu_dav_params* p, double* evals, double* ev
     ST((convert<float, double>(c, g32, g64, (int64_t)N * nguess)));
     dfree(c, g32, 0);
     DavidsonGPU<double> F;
-    F.c = c; F.N = N; F.nstates = nstates; F.blocksize = blocksize;
-    F.maxvec = (p->refine > 1 ? p->refine : 4) * blocksize;
+    // refinement block: fewer columns than the solver's block (FP64 columns
+    // are the expensive ones), but with room above the wanted roots; a block
+    // of exactly davstates can lose a root (measured: 20 roots at
+    // nocc=16/nvirt=180 converged to a wrong set)
+    const int rdef = std::min(blocksize, std::max(nstates + 10, nstates + nstates / 2));
+    const int rblock = p->refine_block == 0 ? rdef
+                       : ((p->refine_block >= nstates && p->refine_block <= blocksize) ? p->refine_block : blocksize);
+    F.c = c; F.N = N; F.nstates = nstates; F.blocksize = rblock;
+    F.maxvec = (p->refine > 1 ? p->refine : 4) * rblock;
     F.niter = p->maxiter; F.ipre = precon64;
     F.ldeflate = p->ldfl != 0; F.tol = p->davtol; F.hii = c->d_diag;
     int it2 = 0, nc2 = 0, nout = 0;

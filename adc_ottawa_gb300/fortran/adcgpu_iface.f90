@@ -25,6 +25,7 @@ module adcgpu_iface
      real(c_double) :: davtol
      integer(c_int) :: precision, refine
      real(c_double) :: tol_bf16, tol_fp32
+     integer(c_int) :: refine_block
   end type adcgpu_dav_params
 
   type, bind(C) :: adcgpu_dav_info

@@ -181,6 +181,10 @@ typedef struct {
                         5e-6 otherwise); the BF16 and FP32 phases also hand
                         over when their largest residual has not fallen by
                         10 % in 12 iterations (their precision floor)        */
+  int refine_block;  /* MIXED: block size of the FP64 refinement, between
+                        davstates and the solver's blocksize (0: min(blocksize,
+                        max(davstates + 10, 1.5 davstates))); a block of
+                        exactly davstates can miss a root                    */
 } adcgpu_dav_params;
 
 typedef struct {
