@@ -8,6 +8,9 @@ and argument meaning of the Fortran routine it replaces:
   lancdiag_block       source/eigen/block_lanczos.f90:28-81
   silstep              source/propagation/sillib.f90:108-393
   propagate_fvec       source/propagation/fvecprop.f90:27-105 (autocorrelation)
+  chebyshev_auto       source/propagation/chebyspec.f90:246-330
+  project_psi0         source/propagation/chebyspec.f90:398-470
+  spectral_bounds      source/propagation/specbounds.f90:121-205
 
 Failures raise AdcGpuError carrying the library status code; the reference
 calls error_control/STOP in the same places (iomod.f90:94-112).
@@ -264,3 +267,98 @@ class AdcGpu:
                                           C.byref(ntimes), C.byref(nmult)), "propagate_fvec")
         a = out[..., 0] + 1j * out[..., 1]
         return a[:, : ntimes.value], int(nmult.value)
+
+    # -- Chebyshev order-domain autocorrelation ------------------------------------
+    def spectral_bounds(self, precon: int = PRECON_OLSEN) -> np.ndarray:
+        """spectral_bounds(bounds,'c','davlanc',...) (specbounds.f90:121-205):
+        the unwidened [Emin, Emax] estimate."""
+        b = np.zeros(2)
+        self._check(lib().adcgpu_spectral_bounds(self._h, precon, ptr(b)), "spectral_bounds")
+        return b
+
+    def chebyshev_auto(self, q0: np.ndarray, bounds, chebyord: int, save1h1p: bool = False):
+        """C_k, k = 0..2 ord, of chebyshev_auto (chebyspec.f90:246-330) for each
+        column of q0 (ord = chebyord rounded down to even).  Returns
+        (auto[nvec, 2 ord + 1], q1h1p[nvec, ord + 1, n1] or None)."""
+        q = np.asfortranarray(q0, np.float64)
+        if q.ndim == 1:
+            q = q.reshape(-1, 1, order="F")
+        nvec = q.shape[1]
+        b = np.ascontiguousarray(bounds, np.float64)
+        ordmax = max(chebyord, 0)
+        out = np.zeros((nvec, 2 * ordmax + 1))
+        h1 = np.zeros((nvec, ordmax + 1, self.nocc * self.nvirt)) if save1h1p else None
+        o = C.c_int(0)
+        self._check(lib().adcgpu_chebyshev_auto(self._h, nvec, ptr(q), ptr(b), chebyord, ptr(out), ptr(h1),
+                                                C.byref(o)), "chebyshev_auto")
+        o = o.value
+        return out[:, : 2 * o + 1], (h1[:, : o + 1] if save1h1p else None)
+
+    def project_psi0(self, q0: np.ndarray, bounds, chebyord: int, projen: float) -> np.ndarray:
+        """project_psi0 (chebyspec.f90:398-470) on a copy of q0 (columns)."""
+        q = np.array(q0, np.float64, order="F", copy=True)
+        one = q.ndim == 1
+        if one:
+            q = q.reshape(-1, 1, order="F")
+        b = np.ascontiguousarray(bounds, np.float64)
+        self._check(lib().adcgpu_chebyshev_project(self._h, q.shape[1], ptr(q), ptr(b), chebyord, projen),
+                    "project_psi0")
+        return q[:, 0] if one else q
+
+
+def fortran_e(x: float, w: int = 21, d: int = 14) -> str:
+    """Fortran Ew.d edit descriptor (0.ddddE+xx form, as gfortran writes it)."""
+    x = float(x)
+    if x == 0.0:
+        body = "0." + "0" * d + "E+00"
+    else:
+        m, e = f"{abs(x):.{d - 1}e}".split("e")
+        digits = m.replace(".", "")
+        ex = int(e) + 1
+        body = "0." + digits + (f"E{ex:+03d}" if abs(ex) <= 99 else f"{ex:+04d}")
+    if x < 0.0 or (x == 0.0 and np.signbit(x)):
+        body = "-" + body
+    return body.rjust(w)
+
+
+def write_chebyshev_auto(path: str, bounds, auto) -> None:
+    """The 'chebyauto' file of write_chebyshev_auto (chebyspec.f90:334-368)."""
+    with open(path, "w") as f:
+        f.write("#    Spectral bounds:" + "".join("  " + fortran_e(b) for b in bounds) + "\n\n")
+        f.write("#    Order [k]    C_k\n")
+        for k, c in enumerate(auto):
+            f.write(f"{k:6d}" + " " * 11 + fortran_e(c) + "\n")
+
+
+def write_cheby1h1p(path: str, q1h1p) -> None:
+    """The 'cheby1h1p' file of write_1h1p (chebyspec.f90:372-394): one Fortran
+    unformatted sequential record per order k = 0..ord."""
+    with open(path, "wb") as f:
+        for col in np.asarray(q1h1p, np.float64):
+            rec = np.ascontiguousarray(col).tobytes()
+            mark = np.int32(len(rec)).tobytes()
+            f.write(mark + rec + mark)
+
+
+def chebyshev_auto_order_domain(g: "AdcGpu", q0: np.ndarray, chebyord: int, bounds=None, lprojpsi0: bool = False,
+                                projen: float = 0.0, save1h1p: bool = False, outdir: str | None = None,
+                                precon: int = PRECON_OLSEN):
+    """chebyshev_auto_order_domain (chebyspec.f90:25-116) for the columns of q0:
+    spectral bounds (estimated by spectral_bounds when not given) widened to
+    [0.9 Emin, 1.1 Emax] (:84-85), optional projection onto an energy window
+    (:90), the order-domain autocorrelation, and, with outdir, the files
+    'chebyauto' (and 'cheby1h1p') of the first column.
+    Returns (auto, q1h1p, widened bounds)."""
+    import os
+
+    b = g.spectral_bounds(precon) if bounds is None else np.asarray(bounds, np.float64)
+    b = np.array([0.9 * b[0], 1.1 * b[1]])
+    q = np.asfortranarray(q0, np.float64)
+    if lprojpsi0:
+        q = g.project_psi0(q, b, chebyord, projen)
+    auto, q1 = g.chebyshev_auto(q, b, chebyord, save1h1p)
+    if outdir is not None:
+        write_chebyshev_auto(os.path.join(outdir, "chebyauto"), b, auto[0])
+        if save1h1p:
+            write_cheby1h1p(os.path.join(outdir, "cheby1h1p"), q1[0])
+    return auto, q1, b

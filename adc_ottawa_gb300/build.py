@@ -36,6 +36,7 @@ SOURCES = [
     ("davidson.cu", []),
     ("lanczos.cu", []),
     ("sil.cu", []),
+    ("chebyshev.cu", []),
     ("mlp.cu", []),
 ]
 

@@ -47,13 +47,17 @@ def parse():
     ap.add_argument("--no-fp64", action="store_true", help="skip the FP64 GPU comparison solve")
     ap.add_argument("--no-e2e", action="store_true")
     ap.add_argument("--no-cpu", action="store_true")
-    ap.add_argument("--suite", default="davidson", choices=["davidson", "lanczos", "sil", "batch", "learned"],
+    ap.add_argument("--suite", default="davidson",
+                    choices=["davidson", "lanczos", "sil", "batch", "learned", "cheb"],
                     help="davidson: the headline solve (default); lanczos: nocc=10/nvirt=110 block Lanczos, "
                          "b=10, 300 cycles; sil: 32 wavepackets on the nocc=10/nvirt=110 matrix, Krylov dim 15, "
                          "dt=0.05 au (--sil-steps steps timed); batch: 64 seeded systems, 8 roots each; "
-                         "learned: nocc=20/nvirt=240, 30 roots, diagonal vs learned vs folded preconditioner")
+                         "learned: nocc=20/nvirt=240, 30 roots, diagonal vs learned vs folded preconditioner; "
+                         "cheb: Chebyshev order-domain autocorrelation of 32 start vectors on the "
+                         "nocc=10/nvirt=110 matrix (--cheb-order orders)")
     ap.add_argument("--train-systems", type=int, default=200)
     ap.add_argument("--sil-steps", type=int, default=20)
+    ap.add_argument("--cheb-order", type=int, default=1000)
     return ap.parse_args()
 
 
@@ -390,6 +394,60 @@ def run_sil(args):
     g.close()
 
 
+def run_cheb(args):
+    """Chebyshev order-domain autocorrelation (chebyspec.f90:25-116) on the
+    nocc=10/nvirt=110 matrix: the 'davlanc' spectral bounds, then C_0..C_2K of
+    32 seeded start vectors expanded together (K = --cheb-order); the sigma
+    product's algorithmic bytes over its CUDA-event time give the matvec's
+    bandwidth.  CPU leg: the oracle's expansion of one vector for a few
+    orders, as a per-order rate."""
+    import numpy as np
+
+    from adc_ottawa_gb300 import ADCGPU_FP64, AdcGpu, synth_system, synth_uniform_block
+
+    no, nv, nvec, K = 10, 110, 32, max(2, args.cheb_order)
+    e, eri = synth_system(no, nv, 2024)
+    g = AdcGpu(0)
+    g.set_orbitals(no, nv, e)
+    g.set_eri_packed(eri)
+    g.write_fspace_adc2_1(None, precision=ADCGPU_FP64)
+    t = time.perf_counter()
+    raw = g.spectral_bounds()
+    bounds_s = time.perf_counter() - t
+    bounds = np.array([0.9 * raw[0], 1.1 * raw[1]])
+    q0 = synth_uniform_block(g.ndim, nvec, 77)
+    g.chebyshev_auto(q0, bounds, 4)
+    g.sigma_stats(reset=True)
+    from adc_ottawa_gb300._native import lib
+
+    l0 = int(lib().adcgpu_kernel_launches())
+    t = time.perf_counter()
+    auto, _ = g.chebyshev_auto(q0, bounds, K)
+    dt = time.perf_counter() - t
+    launches = int(lib().adcgpu_kernel_launches()) - l0
+    st = g.sigma_stats(reset=True)
+    sig_gbs = st["alg_bytes"] / (st["ms"] * 1e-3) / 1e9 if st["ms"] > 0 else None
+    extra = {}
+    if not args.no_cpu:
+        import oracle
+
+        cpu_orders = 2
+        diag = g.get_diag()
+        h, oi, oj = g.export_coo()
+        M = oracle.Matrix.from_coo(diag, h, oi, oj)
+        t = time.perf_counter()
+        M.chebyshev_auto(q0[:, 0], bounds, cpu_orders)
+        cpu_s = time.perf_counter() - t
+        extra["cpu_baseline"] = {"value": cpu_s / cpu_orders, "unit": "s per order per vector", "cores": 1,
+                                 "kind": "port", "sample": f"oracle chebyshev_auto, 1 vector, {cpu_orders} orders"}
+    _secondary_line("Chebyshev order-domain autocorrelation, 32 vectors: seconds per order", dt / K, "s", K, 1,
+                    {"workload": f"ADC(2)-s nocc={no} nvirt={nv} N={g.ndim} chebyshev vectors={nvec} order={K}"},
+                    total_s=dt, spectral_bounds=[float(x) for x in raw], spectral_bounds_s=bounds_s,
+                    sigma_ms_share=st["ms"] * 1e-3 / dt, sigma_alg_gbs=sig_gbs, gpu_launches=launches,
+                    c_last=[float(x) for x in auto[0, -3:]], **extra)
+    g.close()
+
+
 def run_batch(args):
     """Config 4 batch: 64 seeded systems, nocc ~ U{4..12}, nvirt ~ U{30..120},
     8 roots to 1e-6, mixed precision with the folded preconditioner, solved
@@ -465,5 +523,7 @@ if __name__ == "__main__":
         run_batch(a)
     elif a.suite == "learned":
         run_learned(a)
+    elif a.suite == "cheb":
+        run_cheb(a)
     else:
         run_gb300(a)

@@ -259,6 +259,41 @@ int adcgpu_autocorr(adcgpu_ctx* ctx, int nwp, const double* f, double tout,
                     int* ntimes_out, int64_t* nmult_out);
 
 /* ---------------------------------------------------------------------------
+ * Chebyshev order-domain autocorrelation (source/propagation/chebyspec.f90,
+ * chebyshev_auto_order_domain :25-116), for nvec start vectors at once.
+ * ------------------------------------------------------------------------- */
+
+/* chebyshev_auto (chebyspec.f90:246-330) with chebyshev_recursion and
+   matxvec_chebyshev_incore (tdselib.f90:1228-1398): q_k = T_k(H_norm) q_0,
+   H_norm = (2/(Emax-Emin)) H - (2 Emin/(Emax-Emin) + 1).  bounds = {Emin, Emax}
+   are used as given (the reference driver widens its estimate to
+   {0.9 Emin, 1.1 Emax} first, :84-85).  chebyord is rounded down to even (ord,
+   chebyshev_initialise :136; written to order_out, may be NULL).
+   q0: ndim x nvec column-major.  auto_out: nvec x (2 ord + 1), layout
+   [vector][k], C_k = <q_0|q_k> for k <= ord and the doubling formulas above.
+   q1h1p (may be NULL, the save1h1p output): the first nocc*nvirt elements of
+   q_0..q_ord, layout [vector][k][n1]. */
+int adcgpu_chebyshev_auto(adcgpu_ctx* ctx, int nvec, const double* q0,
+                          const double* bounds, int chebyord, double* auto_out,
+                          double* q1h1p, int* order_out);
+
+/* project_psi0 (chebyspec.f90:398-470): q0 <- sum_k f_k g_k T_k(H_norm) q0,
+   the Jackson-damped Chebyshev expansion of the step function at projen, in
+   place on the ndim x nvec block q0 (not normalised, as in the reference).
+   ADCGPU_BAD_INPUT when projen lies outside bounds (the reference's acos
+   would return NaN). */
+int adcgpu_chebyshev_project(adcgpu_ctx* ctx, int nvec, double* q0,
+                             const double* bounds, int chebyord, double projen);
+
+/* spectral_bounds_davlanc (specbounds.f90:121-205): bounds[0] from a one-root
+   block Davidson (block 5, subspace 20, 100 iterations, tol 1e-8,
+   initvec_subdiag with 800 configurations, preconditioner precon, 0 = Olsen);
+   bounds[1] the highest Lanczos state energy of a block Lanczos (block 2,
+   100 cycles, PRO) started from init_vec_singlesubspace
+   (block_lanczos.f90:748-923).  Needs ndim >= 200. */
+int adcgpu_spectral_bounds(adcgpu_ctx* ctx, int precon, double* bounds);
+
+/* ---------------------------------------------------------------------------
  * Learned preconditioner (ADCGPU_PRECON_MLP).  No counterpart routine in the
  * reference: it replaces the diagonal preconditioner of dpr
  * (block_davidson.f90:1288-1342) by t = m * r / (lambda - h), m = MLP(features),

@@ -64,6 +64,10 @@ def lib():
         L.orc_autocorr.argtypes = [C.c_void_p, _dp, C.c_double, C.c_double, C.c_int, C.c_double,
                                    _dp, C.POINTER(C.c_int), _i64p]
         L.orc_autocorr.restype = C.c_int
+        L.orc_chebyshev_auto.argtypes = [C.c_void_p, _dp, _dp, C.c_int, _dp, _dp, C.c_int64]
+        L.orc_chebyshev_auto.restype = C.c_int
+        L.orc_chebyshev_project.argtypes = [C.c_void_p, _dp, _dp, C.c_int, C.c_double]
+        L.orc_chebyshev_project.restype = C.c_int
         _lib = L
     return _lib
 
@@ -163,6 +167,62 @@ class Matrix:
         st = lib().orc_autocorr(self.h, _p(f), tout, tfinal, kdim, tol, _p(out), C.byref(ntimes), C.byref(nmult))
         a = out[0::2] + 1j * out[1::2]
         return st, a[: ntimes.value], nmult.value
+
+    def chebyshev_auto(self, q0, bounds, chebyord, n1=0):
+        """C_0..C_2ord of chebyshev_auto (chebyspec.f90:246-330); with n1 > 0
+        also the first n1 elements of q_0..q_ord (the save1h1p array)."""
+        q0 = np.ascontiguousarray(q0, np.float64)
+        bounds = np.ascontiguousarray(bounds, np.float64)
+        out = np.zeros(2 * chebyord + 1)
+        q1 = np.zeros((n1, chebyord + 1), order="F") if n1 else None
+        o = lib().orc_chebyshev_auto(self.h, _p(q0), _p(bounds), chebyord, _p(out),
+                                     _p(q1) if n1 else None, n1)
+        return out[: 2 * o + 1], (q1[:, : o + 1] if n1 else None)
+
+    def chebyshev_project(self, q0, bounds, chebyord, projen):
+        """project_psi0 (chebyspec.f90:398-470) on a copy of q0."""
+        q = np.array(q0, np.float64)
+        bounds = np.ascontiguousarray(bounds, np.float64)
+        lib().orc_chebyshev_project(self.h, _p(q), _p(bounds), chebyord, projen)
+        return q
+
+    def singlesubspace_block(self, blocksize, subdim=800):
+        """init_vec_singlesubspace (block_lanczos.f90:748-923): the lowest
+        blocksize eigenvectors of H restricted to the subdim configurations of
+        largest hii (extended past near-degeneracies < 1e-6), scattered into an
+        N x blocksize block.  The descending heapsort dsortindxa1('D') is the
+        ascending one on negated keys (the same comparisons).  dsyev is
+        numpy's LAPACK here (eigenvector signs are free; the Lanczos
+        eigenvalues do not depend on them)."""
+        diag, h, oi, oj = self.coo()
+        n = len(diag)
+        indx = heapsort_index(-diag)                  # 1-based, descending hii
+        subdim = min(subdim, n)
+        while subdim < n and abs(diag[indx[subdim - 1] - 1] - diag[indx[subdim] - 1]) < 1e-6:
+            subdim += 1
+        sub2full = indx[:subdim] - 1
+        full2sub = np.full(n, -1, np.int64)
+        full2sub[sub2full] = np.arange(subdim)
+        hsub = np.diag(diag[sub2full])
+        keep = (full2sub[oi - 1] >= 0) & (full2sub[oj - 1] >= 0)
+        i1, j1 = full2sub[oi[keep] - 1], full2sub[oj[keep] - 1]
+        hsub[i1, j1] = h[keep]
+        hsub[j1, i1] = h[keep]
+        _, V = np.linalg.eigh(hsub)
+        q = np.zeros((n, blocksize), order="F")
+        q[sub2full, :] = V[:, :blocksize]
+        return q
+
+    def spectral_bounds(self, precon=2, nthreads=0):
+        """spectral_bounds_davlanc (specbounds.f90:121-205): the lowest
+        eigenvalue from a 1-root block Davidson (block 5, subspace 20, tol 1e-8,
+        subspace-diagonalisation guess), the highest from a block Lanczos
+        (block 2, 100 cycles, PRO) started from init_vec_singlesubspace."""
+        st, ev, _, _ = self.davidson(1, 1e-8, blocksize=5, maxvec=20, niter=100, precon=precon, deflate=True,
+                                     subdiag=True, guessdim=800, nthreads=nthreads)
+        q0 = self.singlesubspace_block(2)
+        _, evl = self.block_lanczos(q0, 100, orthotype=1, nthreads=nthreads)
+        return st, np.array([ev[0], evl[-1]])
 
     def __del__(self):
         if getattr(self, "h", None) and _lib is not None:

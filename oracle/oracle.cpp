@@ -1173,3 +1173,110 @@ int orc_autocorr(void* m, const double* fvec, double tout, double tfinal, int kd
 }
 
 }  // extern "C"
+
+// ===========================================================================
+// Chebyshev order-domain autocorrelation: chebyshev_initialise and
+// chebyshev_auto (chebyspec.f90:130-157,246-330), chebyshev_recursion and
+// matxvec_chebyshev_incore (tdselib.f90:1228-1256,1300-1398), and the
+// Jackson-damped energy filter project_psi0 (chebyspec.f90:398-470).
+// ===========================================================================
+namespace {
+
+// v2 = H_norm v1 (:1300-1398): the diagonal product, then the off-diagonal
+// sum accumulated in a zeroed work vector (one thread's tmpvec) and added,
+// then scaled so that [Emin, Emax] maps onto [-1, 1].
+void matxvec_chebyshev(const OrcMatrix& M, const double* bounds, const double* v1, double* v2,
+                       std::vector<double>& tmp) {
+  const int64_t N = M.ndim, nnz = (int64_t)M.h.size();
+  for (int64_t k = 0; k < N; ++k) v2[k] = M.diag[k] * v1[k];
+  tmp.assign(N, 0.0);
+  for (int64_t k = 0; k < nnz; ++k) {
+    int64_t i = M.oi[k] - 1, j = M.oj[k] - 1;
+    tmp[i] = tmp[i] + M.h[k] * v1[j];
+    tmp[j] = tmp[j] + M.h[k] * v1[i];
+  }
+  for (int64_t k = 0; k < N; ++k) v2[k] = v2[k] + tmp[k];
+  const double DeltaE = bounds[1] - bounds[0], Emin = bounds[0];
+  for (int64_t k = 0; k < N; ++k) v2[k] = (2.0 / DeltaE) * v2[k];
+  for (int64_t k = 0; k < N; ++k) v2[k] = v2[k] - (2.0 * (Emin / DeltaE) + 1.0) * v1[k];
+}
+
+// q_k = 2 H_norm q_{k-1} - q_{k-2} (k > 1), q_1 = H_norm q_0 (:1228-1256)
+void chebyshev_recursion(int k, const OrcMatrix& M, const double* bounds, double* qk, const double* qkm1,
+                         const double* qkm2, std::vector<double>& tmp) {
+  matxvec_chebyshev(M, bounds, qkm1, qk, tmp);
+  if (k > 1) for (int64_t i = 0; i < M.ndim; ++i) qk[i] = 2.0 * qk[i];
+  if (k > 1) for (int64_t i = 0; i < M.ndim; ++i) qk[i] = qk[i] - qkm2[i];
+}
+
+double dot_product(int64_t n, const double* a, const double* b) {
+  double s = 0.0;
+  for (int64_t i = 0; i < n; ++i) s = s + a[i] * b[i];
+  return s;
+}
+
+}  // namespace
+
+extern "C" {
+
+// auto_out: 2*ord+1 values C_0..C_2ord, ord = chebyord rounded down to even
+// (returned).  q1h1p (may be null): the first n1 elements of q_0..q_ord,
+// column k at q1h1p + k*n1.
+int orc_chebyshev_auto(void* m, const double* q0, const double* bounds, int chebyord, double* auto_out,
+                       double* q1h1p, int64_t n1) {
+  OrcMatrix* M = (OrcMatrix*)m;
+  const int64_t N = M->ndim;
+  if (chebyord % 2 != 0) chebyord = chebyord - 1;
+  std::vector<double> qk(N, 0.0), qkm1(q0, q0 + N), qkm2(N, 0.0), tmp;
+  for (int k = 0; k <= 2 * chebyord; ++k) auto_out[k] = 0.0;
+  auto_out[0] = dot_product(N, q0, q0);
+  if (q1h1p) std::memcpy(q1h1p, q0, sizeof(double) * n1);
+  for (int k = 1; k <= chebyord; ++k) {
+    chebyshev_recursion(k, *M, bounds, qk.data(), qkm1.data(), qkm2.data(), tmp);
+    auto_out[k] = dot_product(N, q0, qk.data());
+    if (k > chebyord / 2) {
+      auto_out[2 * k] = 2.0 * dot_product(N, qk.data(), qk.data()) - auto_out[0];
+      auto_out[2 * k - 1] = 2.0 * dot_product(N, qkm1.data(), qk.data()) - auto_out[1];
+    }
+    if (q1h1p) std::memcpy(q1h1p + (size_t)k * n1, qk.data(), sizeof(double) * n1);
+    qkm2 = qkm1;
+    qkm1 = qk;
+    std::fill(qk.begin(), qk.end(), 0.0);
+  }
+  return chebyord;
+}
+
+// project_psi0: q0 <- sum_k f_k g_k T_k(H_norm) q0, the Jackson-damped
+// Chebyshev expansion of the step function at projen (chebyspec.f90:398-470).
+// chebyord is rounded down to even first, as chebyshev_initialise does before
+// the projection runs.
+int orc_chebyshev_project(void* m, double* q0, const double* bounds, int chebyord, double projen) {
+  OrcMatrix* M = (OrcMatrix*)m;
+  const int64_t N = M->ndim;
+  const double pi = 3.1415926535897932;   // constants.f90:8
+  if (chebyord % 2 != 0) chebyord = chebyord - 1;
+  double escale = projen - (0.5 * (bounds[1] - bounds[0]) + bounds[0]);
+  escale = escale / (bounds[1] - bounds[0]);
+  escale = 2.0 * escale;
+  std::vector<double> gk(chebyord + 1), fk(chebyord + 1);
+  const double alpha = pi / (double)(chebyord + 2), cosa = std::cos(alpha), sina = std::sin(alpha);
+  for (int k = 0; k <= chebyord; ++k)
+    gk[k] = (1.0 - (double)k / ((double)(chebyord + 2))) * sina * std::cos(k * alpha) +
+            (1.0 / (double)(chebyord + 2)) * cosa * std::sin(k * alpha);
+  for (int k = 0; k <= chebyord; ++k) gk[k] = gk[k] / sina;
+  fk[0] = 1.0 - std::acos(escale) / pi;
+  for (int k = 1; k <= chebyord; ++k) fk[k] = -2.0 * std::sin(k * std::acos(escale)) / (k * pi);
+  std::vector<double> qk(N, 0.0), qkm1(q0, q0 + N), qkm2(N, 0.0), pq0(N), tmp;
+  for (int64_t i = 0; i < N; ++i) pq0[i] = fk[0] * gk[0] * q0[i];
+  for (int k = 1; k <= chebyord; ++k) {
+    chebyshev_recursion(k, *M, bounds, qk.data(), qkm1.data(), qkm2.data(), tmp);
+    for (int64_t i = 0; i < N; ++i) pq0[i] = pq0[i] + fk[k] * gk[k] * qk[i];
+    qkm2 = qkm1;
+    qkm1 = qk;
+    std::fill(qk.begin(), qk.end(), 0.0);
+  }
+  std::memcpy(q0, pq0.data(), sizeof(double) * N);
+  return chebyord;
+}
+
+}  // extern "C"

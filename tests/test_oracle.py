@@ -134,3 +134,81 @@ def test_heapsort_tie_order(built):
     idx = oracle.heapsort_index(np.array([2.0, 1.0, 2.0, 1.0, 2.0, 1.0]))
     assert sorted(idx[:3]) == [2, 4, 6]
     assert list(idx) == list(oracle.heapsort_index(np.array([2.0, 1.0, 2.0, 1.0, 2.0, 1.0])))
+
+
+def _cheb_exact(w, c, bounds, nk):
+    """sum_j c_j T_k(x_j), x = the eigenvalues mapped by matxvec_chebyshev."""
+    dE = bounds[1] - bounds[0]
+    x = (2.0 / dE) * w - (2.0 * (bounds[0] / dE) + 1.0)
+    T = np.zeros((nk, len(w)))
+    T[0] = 1.0
+    if nk > 1:
+        T[1] = x
+    for k in range(2, nk):
+        T[k] = 2.0 * x * T[k - 1] - T[k - 2]
+    return T @ c, T
+
+
+@pytest.mark.parametrize("chebyord", [40, 41])
+def test_chebyshev_auto_exact(cfg1, chebyord):
+    """C_k of chebyshev_auto (direct for k <= ord, doubling formulas above)
+    against sum_j <v_j|q0>^2 T_k(x_j) from a dense eigendecomposition; an odd
+    order is rounded down to even as chebyshev_initialise does."""
+    no, nv, e, eri, M = cfg1
+    w, V = np.linalg.eigh(M.dense())
+    bounds = np.array([w[0] - 0.2, 1.1 * w[-1]])
+    q0 = np.random.RandomState(3).uniform(size=M.ndim)
+    a, q1 = M.chebyshev_auto(q0, bounds, chebyord, n1=no * nv)
+    assert len(a) == 81 and q1.shape == (no * nv, 41)
+    ex, _ = _cheb_exact(w, (V.T @ q0) ** 2, bounds, len(a))
+    assert np.abs(a - ex).max() <= 1e-12 * a[0]
+    assert np.array_equal(q1[:, 0], q0[: no * nv])
+    # q_1 = H_norm q_0
+    dE = bounds[1] - bounds[0]
+    q1_ref = (2.0 / dE) * M.matvec(q0)[:, 0] - (2.0 * (bounds[0] / dE) + 1.0) * q0
+    assert np.abs(q1[:, 1] - q1_ref[: no * nv]).max() <= 1e-13 * np.abs(q1_ref).max()
+
+
+def test_chebyshev_project_exact(cfg1):
+    """project_psi0 equals V diag(sum_k f_k g_k T_k(x_j)) V^T q0."""
+    no, nv, e, eri, M = cfg1
+    w, V = np.linalg.eigh(M.dense())
+    bounds = np.array([w[0] - 0.2, 1.1 * w[-1]])
+    ord_, projen = 60, 0.5 * (w[0] + w[-1])
+    q0 = np.random.RandomState(4).uniform(size=M.ndim)
+    pq = M.chebyshev_project(q0, bounds, ord_, projen)
+    dE = bounds[1] - bounds[0]
+    es = 2.0 * ((projen - (0.5 * dE + bounds[0])) / dE)
+    al = np.pi / (ord_ + 2)
+    k = np.arange(ord_ + 1)
+    gk = ((1 - k / (ord_ + 2)) * np.sin(al) * np.cos(k * al) + np.cos(al) * np.sin(k * al) / (ord_ + 2)) / np.sin(al)
+    fk = np.empty(ord_ + 1)
+    fk[0] = 1 - np.arccos(es) / np.pi
+    fk[1:] = -2 * np.sin(k[1:] * np.arccos(es)) / (k[1:] * np.pi)
+    _, T = _cheb_exact(w, np.zeros(len(w)), bounds, ord_ + 1)
+    filt = (fk * gk) @ T
+    ref = V @ (filt * (V.T @ q0))
+    assert np.abs(pq - ref).max() <= 1e-11 * np.abs(ref).max()
+    # the filter passes the lower half of the spectrum (step at projen)
+    assert filt[w < projen - 3.0].min() > 0.95 and np.abs(filt[w > projen + 3.0]).max() < 0.05
+
+
+def test_spectral_bounds_match_dense(cfg1):
+    """spectral_bounds_davlanc: Davidson lowest and Lanczos highest eigenvalue."""
+    no, nv, e, eri, M = cfg1
+    w = np.linalg.eigvalsh(M.dense())
+    st, b = M.spectral_bounds()
+    assert st == 0
+    assert abs(b[0] - w[0]) <= 1e-10 and abs(b[1] - w[-1]) <= 1e-9
+
+
+def test_singlesubspace_block(cfg1):
+    """init_vec_singlesubspace: orthonormal columns supported on the 800
+    configurations of largest hii."""
+    no, nv, e, eri, M = cfg1
+    q = M.singlesubspace_block(2)
+    diag = M.coo()[0]
+    thr = np.sort(diag)[::-1][799]
+    support = np.flatnonzero(np.abs(q).sum(1))
+    assert 400 <= len(support) and np.all(diag[support] >= thr - 1e-4)
+    assert np.allclose(q.T @ q, np.eye(2), atol=1e-12)
