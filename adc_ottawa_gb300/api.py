@@ -285,14 +285,15 @@ class AdcGpu:
             q = q.reshape(-1, 1, order="F")
         nvec = q.shape[1]
         b = np.ascontiguousarray(bounds, np.float64)
-        ordmax = max(chebyord, 0)
-        out = np.zeros((nvec, 2 * ordmax + 1))
-        h1 = np.zeros((nvec, ordmax + 1, self.nocc * self.nvirt)) if save1h1p else None
+        ordr = max(chebyord, 0) - max(chebyord, 0) % 2     # the library's rounded order sets the strides
+        out = np.zeros((nvec, 2 * ordr + 1))
+        h1 = np.zeros((nvec, ordr + 1, self.nocc * self.nvirt)) if save1h1p else None
         o = C.c_int(0)
         self._check(lib().adcgpu_chebyshev_auto(self._h, nvec, ptr(q), ptr(b), chebyord, ptr(out), ptr(h1),
                                                 C.byref(o)), "chebyshev_auto")
-        o = o.value
-        return out[:, : 2 * o + 1], (h1[:, : o + 1] if save1h1p else None)
+        if o.value != ordr:
+            raise AdcGpuError(12, f"chebyshev_auto: order {o.value}, expected {ordr}")
+        return out, h1
 
     def project_psi0(self, q0: np.ndarray, bounds, chebyord: int, projen: float) -> np.ndarray:
         """project_psi0 (chebyspec.f90:398-470) on a copy of q0 (columns)."""
