@@ -84,8 +84,8 @@ SIGNATURES = {
                                  C.c_int, C.c_int, _dp, C.POINTER(C.c_int), C.POINTER(SilState)]),
     "adcgpu_autocorr": (C.c_int, [_vp, C.c_int, _dp, C.c_double, C.c_double, C.c_int, C.c_double, _dp,
                                   C.POINTER(C.c_int), _i64p]),
-    "adcgpu_chebyshev_auto": (C.c_int, [_vp, C.c_int, _dp, _dp, C.c_int, _dp, _dp, C.POINTER(C.c_int)]),
-    "adcgpu_chebyshev_project": (C.c_int, [_vp, C.c_int, _dp, _dp, C.c_int, C.c_double]),
+    "adcgpu_chebyshev_auto": (C.c_int, [_vp, C.c_int, _dp, _dp, C.c_int, C.c_int, _dp, _dp, C.POINTER(C.c_int)]),
+    "adcgpu_chebyshev_project": (C.c_int, [_vp, C.c_int, _dp, _dp, C.c_int, C.c_double, C.c_int]),
     "adcgpu_spectral_bounds": (C.c_int, [_vp, C.c_int, _dp]),
     "adcgpu_last_sigma_ms": (C.c_double, [_vp]),
     "adcgpu_device_bytes": (C.c_int64, [_vp]),

@@ -276,9 +276,10 @@ class AdcGpu:
         self._check(lib().adcgpu_spectral_bounds(self._h, precon, ptr(b)), "spectral_bounds")
         return b
 
-    def chebyshev_auto(self, q0: np.ndarray, bounds, chebyord: int, save1h1p: bool = False):
+    def chebyshev_auto(self, q0: np.ndarray, bounds, chebyord: int, save1h1p: bool = False, df: bool = False):
         """C_k, k = 0..2 ord, of chebyshev_auto (chebyspec.f90:246-330) for each
-        column of q0 (ord = chebyord rounded down to even).  Returns
+        column of q0 (ord = chebyord rounded down to even).  df: double-float
+        sigma arithmetic for blocks of >= 16 vectors.  Returns
         (auto[nvec, 2 ord + 1], q1h1p[nvec, ord + 1, n1] or None)."""
         q = np.asfortranarray(q0, np.float64)
         if q.ndim == 1:
@@ -289,21 +290,21 @@ class AdcGpu:
         out = np.zeros((nvec, 2 * ordr + 1))
         h1 = np.zeros((nvec, ordr + 1, self.nocc * self.nvirt)) if save1h1p else None
         o = C.c_int(0)
-        self._check(lib().adcgpu_chebyshev_auto(self._h, nvec, ptr(q), ptr(b), chebyord, ptr(out), ptr(h1),
-                                                C.byref(o)), "chebyshev_auto")
+        self._check(lib().adcgpu_chebyshev_auto(self._h, nvec, ptr(q), ptr(b), chebyord, int(df), ptr(out),
+                                                ptr(h1), C.byref(o)), "chebyshev_auto")
         if o.value != ordr:
             raise AdcGpuError(12, f"chebyshev_auto: order {o.value}, expected {ordr}")
         return out, h1
 
-    def project_psi0(self, q0: np.ndarray, bounds, chebyord: int, projen: float) -> np.ndarray:
+    def project_psi0(self, q0: np.ndarray, bounds, chebyord: int, projen: float, df: bool = False) -> np.ndarray:
         """project_psi0 (chebyspec.f90:398-470) on a copy of q0 (columns)."""
         q = np.array(q0, np.float64, order="F", copy=True)
         one = q.ndim == 1
         if one:
             q = q.reshape(-1, 1, order="F")
         b = np.ascontiguousarray(bounds, np.float64)
-        self._check(lib().adcgpu_chebyshev_project(self._h, q.shape[1], ptr(q), ptr(b), chebyord, projen),
-                    "project_psi0")
+        self._check(lib().adcgpu_chebyshev_project(self._h, q.shape[1], ptr(q), ptr(b), chebyord, projen,
+                                                   int(df)), "project_psi0")
         return q[:, 0] if one else q
 
 
@@ -343,7 +344,7 @@ def write_cheby1h1p(path: str, q1h1p) -> None:
 
 def chebyshev_auto_order_domain(g: "AdcGpu", q0: np.ndarray, chebyord: int, bounds=None, lprojpsi0: bool = False,
                                 projen: float = 0.0, save1h1p: bool = False, outdir: str | None = None,
-                                precon: int = PRECON_OLSEN):
+                                precon: int = PRECON_OLSEN, df: bool = False):
     """chebyshev_auto_order_domain (chebyspec.f90:25-116) for the columns of q0:
     spectral bounds (estimated by spectral_bounds when not given) widened to
     [0.9 Emin, 1.1 Emax] (:84-85), optional projection onto an energy window
@@ -356,8 +357,8 @@ def chebyshev_auto_order_domain(g: "AdcGpu", q0: np.ndarray, chebyord: int, boun
     b = np.array([0.9 * b[0], 1.1 * b[1]])
     q = np.asfortranarray(q0, np.float64)
     if lprojpsi0:
-        q = g.project_psi0(q, b, chebyord, projen)
-    auto, q1 = g.chebyshev_auto(q, b, chebyord, save1h1p)
+        q = g.project_psi0(q, b, chebyord, projen, df)
+    auto, q1 = g.chebyshev_auto(q, b, chebyord, save1h1p, df)
     if outdir is not None:
         write_chebyshev_auto(os.path.join(outdir, "chebyauto"), b, auto[0])
         if save1h1p:

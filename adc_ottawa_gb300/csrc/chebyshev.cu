@@ -194,8 +194,15 @@ struct ChebGPU {
   }
 
   // Orders 1..ord from q_0 = Q0.  a, b: the scaling of matxvec_chebyshev;
-  // coef (with acc): the projection coefficients f_k g_k.
-  int expand(double a, double b, const std::vector<double>* coef, int64_t n1) {
+  // coef (with acc): the projection coefficients f_k g_k.  df: the sigma
+  // product's tiled pass in double-float arithmetic (restored on return).
+  int expand(double a, double b, const std::vector<double>* coef, int64_t n1, int df) {
+    struct DfScope {
+      Ctx* c;
+      int old;
+      ~DfScope() { c->dense_df = old; }
+    } scope{c, c->dense_df};
+    c->dense_df = df ? 1 : 0;
     ADC_CUDA(c, cudaMemcpyAsync(R[1], Q0, blk_bytes, cudaMemcpyDeviceToDevice, c->stream));
     double *qkm2 = R[0], *qkm1 = R[1], *qk = R[2];
     for (int k = 1; k <= ord; ++k) {
@@ -295,7 +302,7 @@ static int singlesubspace_block(Ctx* c, int b, std::vector<double>& q0) {
 }  // namespace adcgpu
 
 extern "C" int adcgpu_chebyshev_auto(adcgpu_ctx* h, int nvec, const double* q0, const double* bounds, int chebyord,
-                                     double* auto_out, double* q1h1p, int* order_out) {
+                                     int df, double* auto_out, double* q1h1p, int* order_out) {
   using namespace adcgpu;
   Ctx* c = reinterpret_cast<Ctx*>(h);
   if (!c) return ADCGPU_BAD_INPUT;
@@ -314,7 +321,7 @@ extern "C" int adcgpu_chebyshev_auto(adcgpu_ctx* h, int nvec, const double* q0, 
   ST(G.save_h1(0, G.Q0, n1));
   double a, b;
   cheb_scaling(bounds, a, b);
-  ST(G.expand(a, b, nullptr, n1));
+  ST(G.expand(a, b, nullptr, n1, df));
   std::vector<double> sums((size_t)3 * nvec * (ord + 1));
   ADC_CUDA(c, cudaMemcpyAsync(sums.data(), G.sums, G.sums_bytes, cudaMemcpyDeviceToHost, c->stream));
   if (q1h1p) ADC_CUDA(c, cudaMemcpyAsync(q1h1p, G.h1, G.h1_bytes, cudaMemcpyDeviceToHost, c->stream));
@@ -338,7 +345,7 @@ extern "C" int adcgpu_chebyshev_auto(adcgpu_ctx* h, int nvec, const double* q0, 
 }
 
 extern "C" int adcgpu_chebyshev_project(adcgpu_ctx* h, int nvec, double* q0, const double* bounds, int chebyord,
-                                        double projen) {
+                                        double projen, int df) {
   using namespace adcgpu;
   Ctx* c = reinterpret_cast<Ctx*>(h);
   if (!c) return ADCGPU_BAD_INPUT;
@@ -370,7 +377,7 @@ extern "C" int adcgpu_chebyshev_project(adcgpu_ctx* h, int nvec, double* q0, con
   ADC_CUDA(c, cudaGetLastError());
   double a, b;
   cheb_scaling(bounds, a, b);
-  ST(G.expand(a, b, &coef, 0));
+  ST(G.expand(a, b, &coef, 0, df));
   ADC_CUDA(c, cudaMemcpyAsync(q0, G.acc, G.blk_bytes, cudaMemcpyDeviceToHost, c->stream));
   ADC_CUDA(c, cudaStreamSynchronize(c->stream));
   return ADCGPU_OK;

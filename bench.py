@@ -427,6 +427,11 @@ def run_cheb(args):
     launches = int(lib().adcgpu_kernel_launches()) - l0
     st = g.sigma_stats(reset=True)
     sig_gbs = st["alg_bytes"] / (st["ms"] * 1e-3) / 1e9 if st["ms"] > 0 else None
+    g.chebyshev_auto(q0, bounds, 4, df=True)
+    t = time.perf_counter()
+    auto_df, _ = g.chebyshev_auto(q0, bounds, K, df=True)
+    dt_df = time.perf_counter() - t
+    df_dev = float(np.abs(auto_df - auto).max() / auto[:, 0].max())
     extra = {}
     if not args.no_cpu:
         import oracle
@@ -444,7 +449,8 @@ def run_cheb(args):
                     {"workload": f"ADC(2)-s nocc={no} nvirt={nv} N={g.ndim} chebyshev vectors={nvec} order={K}"},
                     total_s=dt, spectral_bounds=[float(x) for x in raw], spectral_bounds_s=bounds_s,
                     sigma_ms_share=st["ms"] * 1e-3 / dt, sigma_alg_gbs=sig_gbs, gpu_launches=launches,
-                    c_last=[float(x) for x in auto[0, -3:]], **extra)
+                    c_last=[float(x) for x in auto[0, -3:]], df_seconds_per_order=dt_df / K,
+                    df_max_dev_over_c0=df_dev, **extra)
     g.close()
 
 

@@ -272,18 +272,23 @@ int adcgpu_autocorr(adcgpu_ctx* ctx, int nwp, const double* f, double tout,
    q0: ndim x nvec column-major.  auto_out: nvec x (2 ord + 1), layout
    [vector][k], C_k = <q_0|q_k> for k <= ord and the doubling formulas above.
    q1h1p (may be NULL, the save1h1p output): the first nocc*nvirt elements of
-   q_0..q_ord, layout [vector][k][n1]. */
+   q_0..q_ord, layout [vector][k][n1].
+   df != 0: for nvec >= 16 the sigma product's tiled pass runs in double-float
+   arithmetic on the FP32 pipe (a 48-bit significand, about 1e-14 relative
+   per product) instead of native FP64, whose pipe GB300 runs at 1/64 of the
+   FP32 rate; df = 0 is the plain FP64 path. */
 int adcgpu_chebyshev_auto(adcgpu_ctx* ctx, int nvec, const double* q0,
-                          const double* bounds, int chebyord, double* auto_out,
-                          double* q1h1p, int* order_out);
+                          const double* bounds, int chebyord, int df,
+                          double* auto_out, double* q1h1p, int* order_out);
 
 /* project_psi0 (chebyspec.f90:398-470): q0 <- sum_k f_k g_k T_k(H_norm) q0,
    the Jackson-damped Chebyshev expansion of the step function at projen, in
    place on the ndim x nvec block q0 (not normalised, as in the reference).
    ADCGPU_BAD_INPUT when projen lies outside bounds (the reference's acos
-   would return NaN). */
+   would return NaN).  df as for adcgpu_chebyshev_auto. */
 int adcgpu_chebyshev_project(adcgpu_ctx* ctx, int nvec, double* q0,
-                             const double* bounds, int chebyord, double projen);
+                             const double* bounds, int chebyord, double projen,
+                             int df);
 
 /* spectral_bounds_davlanc (specbounds.f90:121-205): bounds[0] from a one-root
    block Davidson (block 5, subspace 20, 100 iterations, tol 1e-8,

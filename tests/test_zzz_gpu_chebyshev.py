@@ -49,6 +49,22 @@ def test_chebyshev_auto_matches_oracle(cfg1, chebyord):
         assert np.abs(q1[p] - rq1.T).max() <= 1e-9 * np.abs(rq1).max()
 
 
+def test_chebyshev_df_matches_oracle(cfg1):
+    """16 vectors (the tiled sigma pass) with double-float arithmetic."""
+    g, M, w, n1 = cfg1
+    bounds = np.array([w[0] - 0.2, 1.1 * w[-1]])
+    Q = np.random.RandomState(11).uniform(size=(M.ndim, 16))
+    auto, _ = g.chebyshev_auto(Q, bounds, 40, df=True)
+    nat, _ = g.chebyshev_auto(Q, bounds, 40)
+    for p in (0, 7, 15):
+        ref, _ = M.chebyshev_auto(Q[:, p], bounds, 40)
+        assert np.abs(auto[p] - ref).max() <= 1e-7 * ref[0]
+    assert np.abs(auto - nat).max() <= 1e-10 * nat[:, 0].max()
+    pq = g.project_psi0(Q[:, :16], bounds, 40, 0.5 * (w[0] + w[-1]), df=True)
+    ref = M.chebyshev_project(Q[:, 3], bounds, 40, 0.5 * (w[0] + w[-1]))
+    assert np.abs(pq[:, 3] - ref).max() <= 1e-9 * np.abs(ref).max()
+
+
 def test_project_psi0_matches_oracle(cfg1):
     g, M, w, n1 = cfg1
     bounds = np.array([w[0] - 0.2, 1.1 * w[-1]])
