@@ -86,7 +86,7 @@ SIGNATURES = {
                                   C.POINTER(C.c_int), _i64p]),
     "adcgpu_chebyshev_auto": (C.c_int, [_vp, C.c_int, _dp, _dp, C.c_int, C.c_int, _dp, _dp, C.POINTER(C.c_int)]),
     "adcgpu_chebyshev_project": (C.c_int, [_vp, C.c_int, _dp, _dp, C.c_int, C.c_double, C.c_int]),
-    "adcgpu_spectral_bounds": (C.c_int, [_vp, C.c_int, _dp]),
+    "adcgpu_spectral_bounds": (C.c_int, [_vp, C.POINTER(DavParams), _dp]),
     "adcgpu_last_sigma_ms": (C.c_double, [_vp]),
     "adcgpu_device_bytes": (C.c_int64, [_vp]),
     "adcgpu_sigma_stats": (C.c_int, [_vp, _dp, C.c_int]),

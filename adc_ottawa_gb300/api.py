@@ -269,11 +269,15 @@ class AdcGpu:
         return a[:, : ntimes.value], int(nmult.value)
 
     # -- Chebyshev order-domain autocorrelation ------------------------------------
-    def spectral_bounds(self, precon: int = PRECON_OLSEN) -> np.ndarray:
+    def spectral_bounds(self, precon: int = PRECON_OLSEN, maxiter: int = 100, ldfl: bool = True,
+                        guessdim: int = 800) -> np.ndarray:
         """spectral_bounds(bounds,'c','davlanc',...) (specbounds.f90:121-205):
-        the unwidened [Emin, Emax] estimate."""
+        the unwidened [Emin, Emax] estimate.  precon, maxiter, ldfl and
+        guessdim are the final-space Davidson settings the reference leaves
+        to the user (precon_f, maxiter_f, ldfl_f, guessdim_f)."""
+        p = DavParams(maxiter=maxiter, precon=precon, ldfl=int(ldfl), guessdim=guessdim)
         b = np.zeros(2)
-        self._check(lib().adcgpu_spectral_bounds(self._h, precon, ptr(b)), "spectral_bounds")
+        self._check(lib().adcgpu_spectral_bounds(self._h, C.byref(p), ptr(b)), "spectral_bounds")
         return b
 
     def chebyshev_auto(self, q0: np.ndarray, bounds, chebyord: int, save1h1p: bool = False, df: bool = False):

@@ -383,7 +383,7 @@ extern "C" int adcgpu_chebyshev_project(adcgpu_ctx* h, int nvec, double* q0, con
   return ADCGPU_OK;
 }
 
-extern "C" int adcgpu_spectral_bounds(adcgpu_ctx* h, int precon, double* bounds) {
+extern "C" int adcgpu_spectral_bounds(adcgpu_ctx* h, const adcgpu_dav_params* fp, double* bounds) {
   using namespace adcgpu;
   Ctx* c = reinterpret_cast<Ctx*>(h);
   if (!c) return ADCGPU_BAD_INPUT;
@@ -391,18 +391,28 @@ extern "C" int adcgpu_spectral_bounds(adcgpu_ctx* h, int precon, double* bounds)
   if (!c->have_matrix) return set_err(c, ADCGPU_NO_MATRIX, "build the matrix first");
   if (!bounds) return set_err(c, ADCGPU_BAD_INPUT, "bounds required");
   if (c->geom.N < 200) return set_err(c, ADCGPU_BAD_INPUT, "the Lanczos estimate needs ndim >= 200 (2 x 100 vectors)");
-  // lower bound: one-root block Davidson (specbounds.f90:151-176)
+  // lower bound: one-root block Davidson (specbounds.f90:151-176).  The
+  // reference sets davstates_f, dmain_f, maxsubdim_f, davtol_f and
+  // lsubdiag_f; maxiter, precon, ldfl and guessdim stay the caller's
+  // final-space values (defaults.f90:84-94 when fp is NULL or a field is 0).
   adcgpu_dav_params p;
   std::memset(&p, 0, sizeof p);
+  if (fp) {
+    p.maxiter = fp->maxiter;
+    p.precon = fp->precon;
+    p.ldfl = fp->ldfl;
+    p.guessdim = fp->guessdim;
+  } else {
+    p.ldfl = 1;
+  }
+  if (p.maxiter <= 0) p.maxiter = 100;
+  if (p.precon == 0) p.precon = ADCGPU_PRECON_OLSEN;
+  if (p.guessdim <= 0) p.guessdim = 800;
   p.davstates = 1;
   p.dmain = 5;
   p.maxsubdim = 20;
-  p.maxiter = 100;
-  p.precon = precon ? precon : ADCGPU_PRECON_OLSEN;
-  p.ldfl = 1;
-  p.lsubdiag = 1;
-  p.guessdim = 800;
   p.davtol = 1e-8;
+  p.lsubdiag = 1;
   p.precision = ADCGPU_FP64;
   double lower = 0.0;
   adcgpu_dav_info info;

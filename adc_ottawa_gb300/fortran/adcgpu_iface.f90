@@ -10,6 +10,8 @@
 !   davdiag_block        -> davdiag_block_gpu         (block_davidson.f90:33)
 !   lancdiag_block       -> lancdiag_block_gpu        (block_lanczos.f90:28)
 !   propagate_fvec       -> propagate_fvec_gpu        (fvecprop.f90:27)
+!   chebyshev_auto_order_domain
+!                        -> chebyshev_auto_order_domain_gpu (chebyspec.f90:25)
 !
 ! A non-zero status from the library is turned into errmsg +
 ! error_control, as the reference does for its own failures.
@@ -115,6 +117,32 @@ module adcgpu_iface
        integer(c_int)        :: ntimes
        integer(c_int64_t)    :: nmult
      end function adcgpu_autocorr
+
+     integer(c_int) function adcgpu_spectral_bounds(ctx, p, bounds) bind(C, name="adcgpu_spectral_bounds")
+       import :: c_int, c_ptr, c_double, adcgpu_dav_params
+       type(c_ptr), value      :: ctx
+       type(adcgpu_dav_params) :: p
+       real(c_double)          :: bounds(2)
+     end function adcgpu_spectral_bounds
+
+     integer(c_int) function adcgpu_chebyshev_auto(ctx, nvec, q0, bounds, chebyord, df, auto, q1h1p, order) &
+          bind(C, name="adcgpu_chebyshev_auto")
+       import :: c_int, c_ptr, c_double
+       type(c_ptr), value    :: ctx
+       integer(c_int), value :: nvec, chebyord, df
+       real(c_double)        :: q0(*), bounds(2), auto(*)
+       type(c_ptr), value    :: q1h1p
+       integer(c_int)        :: order
+     end function adcgpu_chebyshev_auto
+
+     integer(c_int) function adcgpu_chebyshev_project(ctx, nvec, q0, bounds, chebyord, projen, df) &
+          bind(C, name="adcgpu_chebyshev_project")
+       import :: c_int, c_ptr, c_double
+       type(c_ptr), value    :: ctx
+       integer(c_int), value :: nvec, chebyord, df
+       real(c_double)        :: q0(*), bounds(2)
+       real(c_double), value :: projen
+     end function adcgpu_chebyshev_project
 
      type(c_ptr) function adcgpu_last_error(ctx) bind(C, name="adcgpu_last_error")
        import :: c_ptr
@@ -248,5 +276,68 @@ contains
     call adcgpu_check(st, 'propagate_fvec')
     ntimes = nt
   end subroutine propagate_fvec_gpu
+
+!#######################################################################
+! chebyshev_auto_order_domain (chebyspec.f90:25-116): the 'davlanc'
+! spectral bounds (specbounds.f90:121-205) widened to [0.9 Ea, 1.1 Eb],
+! the optional energy-window projection of q0 (lprojpsi0, projen), the
+! order-domain autocorrelation C_0..C_2*chebyord, and the files chebyauto
+! and (save1h1p) cheby1h1p in the layouts of write_chebyshev_auto and
+! write_1h1p (:334-394).  ndimsf is the 1h1p dimension, nocc*nvirt here.
+
+  subroutine chebyshev_auto_order_domain_gpu(q0, ndimf, noffdf, ndimsf)
+    use parameters
+    use iomod, only: freeunit
+    integer, intent(in)                       :: ndimf, ndimsf
+    integer*8, intent(in)                     :: noffdf
+    real(dp), dimension(ndimf), intent(inout) :: q0
+    type(adcgpu_dav_params)               :: p
+    real(dp)                              :: bounds(2)
+    real(dp), allocatable                 :: auto(:)
+    real(dp), allocatable, target         :: q1h1p(:,:)
+    integer(c_int)                        :: st, ord
+    integer                               :: unit, k
+    p%davstates=1; p%dmain=5; p%maxsubdim=20; p%maxiter=maxiter_f
+    p%precon=precon_f; p%ldfl=merge(1,0,ldfl_f); p%lsubdiag=1
+    p%guessdim=guessdim_f; p%davtol=1e-8_dp
+    p%precision=0; p%refine=0; p%tol_bf16=0.0_dp; p%tol_fp32=0.0_dp; p%refine_block=0
+    st = adcgpu_spectral_bounds(gpu_ctx, p, bounds)
+    call adcgpu_check(st, 'spectral_bounds')
+    bounds(1)=0.9d0*bounds(1)
+    bounds(2)=1.1d0*bounds(2)
+    if (mod(chebyord,2).ne.0) chebyord=chebyord-1
+    if (lprojpsi0) then
+       st = adcgpu_chebyshev_project(gpu_ctx, 1_c_int, q0, bounds, int(chebyord,c_int), projen, 0_c_int)
+       call adcgpu_check(st, 'project_psi0')
+    endif
+    allocate(auto(0:2*chebyord))
+    if (save1h1p) then
+       allocate(q1h1p(ndimsf,0:chebyord))
+       st = adcgpu_chebyshev_auto(gpu_ctx, 1_c_int, q0, bounds, int(chebyord,c_int), 0_c_int, auto, &
+            c_loc(q1h1p), ord)
+    else
+       st = adcgpu_chebyshev_auto(gpu_ctx, 1_c_int, q0, bounds, int(chebyord,c_int), 0_c_int, auto, &
+            c_null_ptr, ord)
+    endif
+    call adcgpu_check(st, 'chebyshev_auto')
+    call freeunit(unit)
+    open(unit,file='chebyauto',form='formatted',status='unknown')
+    write(unit,'(a,2(2x,E21.14),/)') '#    Spectral bounds:',bounds(1),bounds(2)
+    write(unit,'(a)') '#    Order [k]    C_k'
+    do k=0,chebyord*2
+       write(unit,'(i6,11x,E21.14)') k,auto(k)
+    enddo
+    close(unit)
+    if (save1h1p) then
+       call freeunit(unit)
+       open(unit=unit,file='cheby1h1p',status='unknown',access='sequential',form='unformatted')
+       do k=0,chebyord
+          write(unit) q1h1p(:,k)
+       enddo
+       close(unit)
+       deallocate(q1h1p)
+    endif
+    deallocate(auto)
+  end subroutine chebyshev_auto_order_domain_gpu
 
 end module adcgpu_iface

@@ -291,12 +291,17 @@ int adcgpu_chebyshev_project(adcgpu_ctx* ctx, int nvec, double* q0,
                              int df);
 
 /* spectral_bounds_davlanc (specbounds.f90:121-205): bounds[0] from a one-root
-   block Davidson (block 5, subspace 20, 100 iterations, tol 1e-8,
-   initvec_subdiag with 800 configurations, preconditioner precon, 0 = Olsen);
-   bounds[1] the highest Lanczos state energy of a block Lanczos (block 2,
+   block Davidson with block 5, subspace 20, tol 1e-8 and the initvec_subdiag
+   guess (the five settings specbounds makes), taking maxiter, precon, ldfl
+   and guessdim from fp, the caller's final-space parameters (may be NULL:
+   100, Olsen, deflation on, 800 -- the reference defaults, defaults.f90:84-94;
+   a zero field also takes its default); the other fields of fp are ignored.
+   bounds[1] is the highest Lanczos state energy of a block Lanczos (block 2,
    100 cycles, PRO) started from init_vec_singlesubspace
-   (block_lanczos.f90:748-923).  Needs ndim >= 200. */
-int adcgpu_spectral_bounds(adcgpu_ctx* ctx, int precon, double* bounds);
+   (block_lanczos.f90:748-923).  Returns the bounds unwidened.
+   Needs ndim >= 200. */
+int adcgpu_spectral_bounds(adcgpu_ctx* ctx, const adcgpu_dav_params* fp,
+                           double* bounds);
 
 /* ---------------------------------------------------------------------------
  * Learned preconditioner (ADCGPU_PRECON_MLP).  No counterpart routine in the
