@@ -43,13 +43,19 @@ int dmalloc(Ctx* c, void** p, size_t bytes) {
     return set_err(c, e == cudaErrorMemoryAllocation ? ADCGPU_OUT_OF_MEMORY : ADCGPU_CUDA_ERROR, buf);
   }
   c->dev_bytes += (int64_t)bytes;
+  c->dev_allocs[*p] = bytes;
   return ADCGPU_OK;
 }
 
-void dfree(Ctx* c, void* p, size_t bytes) {
+void dfree(Ctx* c, void* p, size_t) {
   if (!p) return;
   cudaFree(p);
-  if (bytes) c->dev_bytes -= (int64_t)bytes;
+  if (!c) return;
+  auto it = c->dev_allocs.find(p);
+  if (it != c->dev_allocs.end()) {
+    c->dev_bytes -= (int64_t)it->second;
+    c->dev_allocs.erase(it);
+  }
 }
 
 static void join_diag_order(Ctx* c) {
@@ -67,7 +73,7 @@ static void free_matrix(Ctx* c) {
   void** ps[] = {(void**)&c->d_diag, (void**)&c->d_A, (void**)&c->d_Bt, (void**)&c->d_A32, (void**)&c->d_Bt16,
                  (void**)&c->d_Bt32, (void**)&c->d_diag32, (void**)&c->d_rowcount, &c->d_ws};
   for (void** p : ps) {
-    if (*p) cudaFree(*p);
+    dfree(c, *p);
     *p = nullptr;
   }
   c->ws_bytes = 0;
@@ -78,7 +84,7 @@ static void free_matrix(Ctx* c) {
 static void free_eri(Ctx* c) {
   double** ps[] = {&c->d_vovo, &c->d_vvoo, &c->d_ooov, &c->d_vvov};
   for (double** p : ps) {
-    if (*p) cudaFree(*p);
+    dfree(c, *p);
     *p = nullptr;
   }
   c->have_eri = false;
@@ -125,8 +131,8 @@ int adcgpu_ctx_destroy(adcgpu_ctx* h) {
   free_matrix(c);
   free_eri(c);
   free_mlp(c);
-  if (c->d_e) cudaFree(c->d_e);
-  if (c->d_sil) cudaFree(c->d_sil);
+  dfree(c, c->d_e);
+  dfree(c, c->d_sil);
   cudaEventDestroy(c->ev0);
   cudaEventDestroy(c->ev1);
   if (c->st_ev0) cudaEventDestroy(c->st_ev0);
@@ -153,7 +159,7 @@ int adcgpu_set_orbitals(adcgpu_ctx* h, int nocc, int nvirt, const double* e) {
   free_eri(c);
   c->geom = g;
   c->e.assign(e, e + nocc + nvirt);
-  if (c->d_e) cudaFree(c->d_e);
+  dfree(c, c->d_e);
   c->d_e = nullptr;
   int st = dmalloc(c, (void**)&c->d_e, sizeof(double) * (nocc + nvirt));
   if (st) return st;

@@ -117,10 +117,10 @@ struct DavidsonGPU {
   }
   void release() {
     T* ps[] = {V, W, X, R, WY, Tn, Tmp, Cv};
-    for (T* p : ps) if (p) cudaFree(p);
-    if (d_lam) cudaFree(d_lam);
-    if (d_small) cudaFree(d_small);
-    if (d_small2) cudaFree(d_small2);
+    for (T* p : ps) dfree(c, p);
+    dfree(c, d_lam);
+    dfree(c, d_small);
+    dfree(c, d_small2);
     V = W = X = R = WY = Tn = Tmp = Cv = nullptr;
     d_lam = d_small = d_small2 = nullptr;
     ws.release();

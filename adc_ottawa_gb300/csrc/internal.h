@@ -43,6 +43,7 @@
 #include <atomic>
 #include <thread>
 #include <string>
+#include <unordered_map>
 #include <vector>
 
 #include "../../include/adcgpu.h"
@@ -248,7 +249,8 @@ struct Ctx {
   bool st_pending = false;
   double st_pending_bytes = 0.0;
   int st_pending_cols = 0;
-  int64_t dev_bytes = 0;
+  int64_t dev_bytes = 0;          // sum of the live dmalloc sizes
+  std::unordered_map<void*, size_t> dev_allocs;   // dmalloc pointer -> size
   // learned preconditioner (MlpState, mlp.cu); DPR is used when absent
   void* mlp = nullptr;
   // SIL persistent state for adcgpu_silstep (device Krylov vectors)
@@ -283,8 +285,12 @@ const std::vector<int64_t>& diag_order(Ctx* c);
                                std::string(#call) + ": " + cudaGetErrorString(_e)); \
   } while (0)
 
+// Device allocations of a context: dmalloc records each size, dfree (null is
+// a no-op) releases the pointer and subtracts the recorded size, so
+// adcgpu_device_bytes reports what the context holds.  dfree's third
+// argument is not needed and is ignored.
 int dmalloc(Ctx* c, void** p, size_t bytes);
-void dfree(Ctx* c, void* p, size_t bytes);
+void dfree(Ctx* c, void* p, size_t bytes = 0);
 
 // ---------------------------------------------------------------------------
 // Kernels launched from other translation units.

@@ -62,7 +62,7 @@ struct LanczosGPU {
 
   ~LanczosGPU() {
     double* ps[] = {Qall, Q1, Q2, U, Tmp, d_s, d_s2, d_part};
-    for (double* p : ps) if (p) cudaFree(p);
+    for (double* p : ps) dfree(c, p);
   }
 
   int colnorms(double* X, int ncol, std::vector<double>& out) {

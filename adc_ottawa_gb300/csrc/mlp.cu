@@ -531,9 +531,9 @@ void free_mlp(Ctx* c) {
   MlpState* s = state(c);
   if (!s) return;
   float* ps[] = {s->p, s->m1, s->m2, s->grad, s->scratch};
-  for (float* p : ps) if (p) cudaFree(p);
-  if (s->W1b) cudaFree(s->W1b);
-  if (s->W2b) cudaFree(s->W2b);
+  for (float* p : ps) dfree(c, p);
+  dfree(c, s->W1b);
+  dfree(c, s->W2b);
   delete s;
   c->mlp = nullptr;
 }

@@ -1247,7 +1247,7 @@ int sigma_impl(Ctx* c, int m, const T* dV, int64_t ldv, T* dW, int64_t ldw, cons
   if (sizeof(T) == 4) {
     const size_t need = sizeof(double) * (size_t)n1 * m;
     if (plan->acc_bytes < need) {
-      if (plan->d_acc) cudaFree(plan->d_acc);
+      dfree(c, plan->d_acc);
       plan->d_acc = nullptr; plan->acc_bytes = 0;
       int st2 = dmalloc(c, (void**)&plan->d_acc, need);
       if (st2) return st2;
@@ -1391,9 +1391,9 @@ int build_chunks(Ctx* c, int chunk) {
   }
   SigmaPlan* plan = reinterpret_cast<SigmaPlan*>(c->sigma_plan);
   if (!plan) { plan = new SigmaPlan; c->sigma_plan = plan; }
-  if (plan->d_chunks) cudaFree(plan->d_chunks);
-  if (plan->d_items) cudaFree(plan->d_items);
-  if (plan->d_titems) cudaFree(plan->d_titems);
+  dfree(c, plan->d_chunks);
+  dfree(c, plan->d_items);
+  dfree(c, plan->d_titems);
   plan->d_chunks = plan->d_items = plan->d_titems = nullptr;
   int st;
   if ((st = dmalloc(c, (void**)&plan->d_titems, sizeof(int2) * titems.size()))) return st;
@@ -1418,10 +1418,10 @@ int prepare_desc(Ctx* c) {
 void free_sigma_plan(Ctx* c) {
   SigmaPlan* plan = reinterpret_cast<SigmaPlan*>(c->sigma_plan);
   if (!plan) return;
-  if (plan->d_chunks) cudaFree(plan->d_chunks);
-  if (plan->d_items) cudaFree(plan->d_items);
-  if (plan->d_titems) cudaFree(plan->d_titems);
-  if (plan->d_acc) cudaFree(plan->d_acc);
+  dfree(c, plan->d_chunks);
+  dfree(c, plan->d_items);
+  dfree(c, plan->d_titems);
+  dfree(c, plan->d_acc);
   delete plan;
   c->sigma_plan = nullptr;
 }

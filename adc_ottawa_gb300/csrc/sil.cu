@@ -190,13 +190,13 @@ struct SilEngine {
   int64_t nmult = 0;
 
   ~SilEngine() {
-    if (Psi) cudaFree(Psi);
-    if (Kbase) cudaFree(Kbase);
-    if (d_part) cudaFree(d_part);
-    if (d_coef) cudaFree(d_coef);
-    if (d_mask) cudaFree(d_mask);
-    if (d_order) cudaFree(d_order);
-    if (d_kptr) cudaFree(d_kptr);
+    dfree(c, Psi);
+    dfree(c, Kbase);
+    dfree(c, d_part);
+    dfree(c, d_coef);
+    dfree(c, d_mask);
+    dfree(c, d_order);
+    dfree(c, d_kptr);
   }
   double* K(int q) { return Kbase + (size_t)(q - 1) * N * 2 * P; }   // q = 1..kdim (K_1 = DtPsi)
 

@@ -131,3 +131,16 @@ def test_rejects_bad_bounds(cfg1):
     with pytest.raises(AdcGpuError) as ei:
         g.project_psi0(q0, [w[0] - 0.2, 1.1 * w[-1]], 10, 10.0 * w[-1])
     assert ei.value.code == 12
+
+
+def test_device_bytes_released_after_solvers(cfg1):
+    """adcgpu_device_bytes counts what the context holds: the FP64 solvers'
+    work spaces are released when they return."""
+    g, M, w, n1 = cfg1
+    b0 = g.device_bytes()
+    assert b0 > 8 * M.ndim
+    g.davdiag_block(4, 1e-8, want_vectors=False)
+    g.lancdiag_block(np.random.RandomState(1).uniform(size=(M.ndim, 2)), 10, orthotype=1)
+    g.chebyshev_auto(np.ones(M.ndim), [w[0] - 0.2, 1.1 * w[-1]], 10)
+    g.spectral_bounds()
+    assert g.device_bytes() == b0
