@@ -11,6 +11,8 @@
  *             lancdiag_block             source/eigen/block_lanczos.f90:28-81
  *   SIL       SILStep                    source/propagation/sillib.f90:108-393
  *             propagate_sillib           source/propagation/fvecprop.f90:365-564
+ *   Chebyshev chebyshev_auto_order_domain source/propagation/chebyspec.f90:25-116
+ *             spectral_bounds            source/propagation/specbounds.f90:24-205
  *
  * Conventions
  *   - Plain C types only.  Host arrays are owned by the caller; the library
