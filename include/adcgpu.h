@@ -1,7 +1,7 @@
 /*
  * adcgpu.h -- C ABI of the GB300 (sm_103a) ADC(2)-s hot path.
  *
- * One shared library, libadcgpu.so, replaces three Fortran subsystems of
+ * One shared library, libadcgpu.so, replaces four Fortran subsystems of
  * mschuurman/ADC_ottawa beneath the unchanged Fortran driver:
  *
  *   builder   write_fspace_adc2_1        source/adclib/fspacetrial.f90:533-564
