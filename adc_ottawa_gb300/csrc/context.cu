@@ -163,7 +163,7 @@ int adcgpu_set_orbitals(adcgpu_ctx* h, int nocc, int nvirt, const double* e) {
   c->d_e = nullptr;
   int st = dmalloc(c, (void**)&c->d_e, sizeof(double) * (nocc + nvirt));
   if (st) return st;
-  ADC_CUDA(c, cudaMemcpy(c->d_e, e, sizeof(double) * (nocc + nvirt), cudaMemcpyHostToDevice));
+  ADC_CUDA(c, h2d(c, c->d_e, e, sizeof(double) * (nocc + nvirt)));
   c->have_orb = true;
   return ADCGPU_OK;
 }
@@ -222,7 +222,7 @@ int adcgpu_set_eri_mo_complex(adcgpu_ctx* h, const double* buf) {
     }
     int st = dmalloc(c, (void**)dst[k], sizeof(double) * sz[k]);
     if (st) return st;
-    ADC_CUDA(c, cudaMemcpy(*dst[k], hb.data(), sizeof(double) * sz[k], cudaMemcpyHostToDevice));
+    ADC_CUDA(c, h2d(c, *dst[k], hb.data(), sizeof(double) * sz[k]));
   }
   c->have_eri = true;
   return ADCGPU_OK;
@@ -257,7 +257,7 @@ int adcgpu_build_adc2s(adcgpu_ctx* h, int ndim, const int32_t* kpq, int64_t* nof
     // the guess selection order of |hii| (initvec_ondiag), sorted on a host
     // thread while the caller goes on (it depends only on the diagonal)
     std::vector<double> ah((size_t)c->geom.N);
-    ADC_CUDA(c, cudaMemcpy(ah.data(), c->d_diag, sizeof(double) * ah.size(), cudaMemcpyDeviceToHost));
+    ADC_CUDA(c, d2h(c, ah.data(), c->d_diag, sizeof(double) * ah.size()));
     c->diag_order_thread = std::thread([c, ah = std::move(ah)]() mutable {
       for (double& x : ah) x = std::fabs(x);
       host_heapsort_index((int64_t)ah.size(), ah.data(), c->diag_order);
@@ -273,7 +273,7 @@ int adcgpu_get_diag(adcgpu_ctx* h, double* hii) {
   Ctx* c = reinterpret_cast<Ctx*>(h);
   CTX_CHECK(c);
   if (!c->have_matrix) return set_err(c, ADCGPU_NO_MATRIX, "no matrix");
-  ADC_CUDA(c, cudaMemcpy(hii, c->d_diag, sizeof(double) * c->geom.N, cudaMemcpyDeviceToHost));
+  ADC_CUDA(c, d2h(c, hii, c->d_diag, sizeof(double) * c->geom.N));
   return ADCGPU_OK;
 }
 
@@ -293,9 +293,9 @@ int adcgpu_export_coo(adcgpu_ctx* h, int64_t cap, double* hv, int32_t* oi, int32
   }
   st = export_coo_device(c, d_h, d_i, d_j);
   if (!st) {
-    cudaMemcpy(hv, d_h, sizeof(double) * n, cudaMemcpyDeviceToHost);
-    cudaMemcpy(oi, d_i, sizeof(int32_t) * n, cudaMemcpyDeviceToHost);
-    cudaError_t e = cudaMemcpy(oj, d_j, sizeof(int32_t) * n, cudaMemcpyDeviceToHost);
+    d2h(c, hv, d_h, sizeof(double) * n);
+    d2h(c, oi, d_i, sizeof(int32_t) * n);
+    cudaError_t e = d2h(c, oj, d_j, sizeof(int32_t) * n);
     if (e != cudaSuccess) st = set_err(c, ADCGPU_CUDA_ERROR, cudaGetErrorString(e));
   }
   dfree(c, d_h, sizeof(double) * n);
@@ -399,7 +399,7 @@ int adcgpu_sigma(adcgpu_ctx* h, int m, const double* v, double* w) {
     if ((st = dmalloc(c, (void**)&dw, sizeof(double) * n))) { dfree(c, dv, sizeof(double) * n); return st; }
     ADC_CUDA(c, cudaMemcpyAsync(dv, v, sizeof(double) * n, cudaMemcpyHostToDevice, c->stream));
     st = adcgpu_sigma_device(h, m, dv, dw, N);
-    if (!st) ADC_CUDA(c, cudaMemcpy(w, dw, sizeof(double) * n, cudaMemcpyDeviceToHost));
+    if (!st) ADC_CUDA(c, d2h(c, w, dw, sizeof(double) * n));
     dfree(c, dv, sizeof(double) * n);
     dfree(c, dw, sizeof(double) * n);
     return st;
@@ -410,10 +410,10 @@ int adcgpu_sigma(adcgpu_ctx* h, int m, const double* v, double* w) {
   float *dv = nullptr, *dw = nullptr;
   if ((st = dmalloc(c, (void**)&dv, sizeof(float) * n))) return st;
   if ((st = dmalloc(c, (void**)&dw, sizeof(float) * n))) { dfree(c, dv, sizeof(float) * n); return st; }
-  ADC_CUDA(c, cudaMemcpy(dv, hv.data(), sizeof(float) * n, cudaMemcpyHostToDevice));
+  ADC_CUDA(c, h2d(c, dv, hv.data(), sizeof(float) * n));
   st = adcgpu_sigma_device(h, m, dv, dw, N);
   if (!st) {
-    ADC_CUDA(c, cudaMemcpy(hv.data(), dw, sizeof(float) * n, cudaMemcpyDeviceToHost));
+    ADC_CUDA(c, d2h(c, hv.data(), dw, sizeof(float) * n));
     for (size_t i = 0; i < n; ++i) w[i] = hv[i];
   }
   dfree(c, dv, sizeof(float) * n);

@@ -476,7 +476,7 @@ int DavidsonGPU<T>::guess_subdiag(const std::vector<double>& hdiag, int subdim) 
   for (int i = 0; i < blocksize; ++i) {
     std::fill(colbuf.begin(), colbuf.end(), T(0));
     for (int j = 0; j < subdim; ++j) colbuf[sub[j]] = (T)Vs[(size_t)i * subdim + j];
-    ADC_CUDA(c, cudaMemcpy(V + (size_t)i * N, colbuf.data(), bytes_v, cudaMemcpyHostToDevice));
+    ADC_CUDA(c, h2d(c, V + (size_t)i * N, colbuf.data(), bytes_v));
   }
   return ADCGPU_OK;
 }
@@ -510,7 +510,7 @@ int davidson_solve(Ctx* c, const adcgpu_dav_params* p, double* evals, double* ev
   if (blocksize > N || maxvec < 2 * blocksize || maxvec > N)
     return set_err(c, ADCGPU_BAD_INPUT, "blocksize/maxvec incompatible with the matrix dimension");
   std::vector<double> hdiag(N);
-  ADC_CUDA(c, cudaMemcpy(hdiag.data(), c->d_diag, sizeof(double) * N, cudaMemcpyDeviceToHost));
+  ADC_CUDA(c, d2h(c, hdiag.data(), c->d_diag, sizeof(double) * N));
   const int guess_kind = p->lsubdiag ? 1 : 0;
   const int precon64 = p->precon;
   int st = ADCGPU_OK;
@@ -584,7 +584,7 @@ int davidson_solve(Ctx* c, const adcgpu_dav_params* p, double* evals, double* ev
     D.release();
   }
   if (evecs && (st == ADCGPU_OK || st == ADCGPU_NOT_CONVERGED))
-    cudaMemcpy(evecs, out64, sizeof(double) * (size_t)N * nstates, cudaMemcpyDeviceToHost);
+    d2h(c, evecs, out64, sizeof(double) * (size_t)N * nstates);
   dfree(c, out64, 0);
   if (st && st != ADCGPU_NOT_CONVERGED) return st;
   for (int i = 0; i < nstates; ++i) evals[i] = ev[i];
@@ -620,7 +620,7 @@ extern "C" int adcgpu_davidson_trace(adcgpu_ctx* h, const adcgpu_dav_params* p, 
   int maxvec = p->maxsubdim >= 0 ? p->maxsubdim : 4 * blocksize;
   maxvec = (maxvec / blocksize) * blocksize;
   std::vector<double> hdiag(N), ev;
-  ADC_CUDA(c, cudaMemcpy(hdiag.data(), c->d_diag, sizeof(double) * N, cudaMemcpyDeviceToHost));
+  ADC_CUDA(c, d2h(c, hdiag.data(), c->d_diag, sizeof(double) * N));
   DavidsonGPU<double> D;
   D.c = c; D.N = N; D.nstates = nstates; D.blocksize = blocksize; D.maxvec = maxvec;
   D.niter = p->maxiter; D.ipre = p->precon; D.ldeflate = false; D.tol = p->davtol; D.hii = c->d_diag;
@@ -631,7 +631,7 @@ extern "C" int adcgpu_davidson_trace(adcgpu_ctx* h, const adcgpu_dav_params* p, 
   int it = 0, nc = 0, nout = 0;
   st = D.run(hdiag, p->lsubdiag ? 1 : 0, p->guessdim, nullptr, 0, ev, out, blocksize, &nout, &it, &nc);
   if (st == ADCGPU_OK || st == ADCGPU_NOT_CONVERGED) {
-    cudaMemcpy(evecs, out, sizeof(double) * (size_t)N * nstates, cudaMemcpyDeviceToHost);
+    d2h(c, evecs, out, sizeof(double) * (size_t)N * nstates);
     for (int i = 0; i < nstates; ++i) evals[i] = ev[i];
   }
   if (nrec) *nrec = D.tr_n;

@@ -289,6 +289,21 @@ const std::vector<int64_t>& diag_order(Ctx* c);
 // a no-op) releases the pointer and subtracts the recorded size, so
 // adcgpu_device_bytes reports what the context holds.  dfree's third
 // argument is not needed and is ignored.
+// Host<->device copies on the context's stream.  The stream is created
+// non-blocking, so it is not ordered with the legacy default stream that a
+// plain cudaMemcpy uses: a copy there could overtake kernels still queued on
+// the context's stream, or be overtaken by them.  h2d returns once the host
+// buffer may be reused (pageable sources are staged before the call returns)
+// and is ordered before later work on the stream; d2h returns when the data
+// has arrived.
+inline cudaError_t h2d(Ctx* c, void* dst, const void* src, size_t bytes) {
+  return cudaMemcpyAsync(dst, src, bytes, cudaMemcpyHostToDevice, c->stream);
+}
+inline cudaError_t d2h(Ctx* c, void* dst, const void* src, size_t bytes) {
+  cudaError_t e = cudaMemcpyAsync(dst, src, bytes, cudaMemcpyDeviceToHost, c->stream);
+  return e != cudaSuccess ? e : cudaStreamSynchronize(c->stream);
+}
+
 int dmalloc(Ctx* c, void** p, size_t bytes);
 void dfree(Ctx* c, void* p, size_t bytes = 0);
 

@@ -424,8 +424,8 @@ int ensure_state(Ctx* c) {
   if ((st = dmalloc(c, (void**)&s->grad, sizeof(float) * NPARAM))) return st;
   if ((st = dmalloc(c, (void**)&s->W1b, sizeof(__nv_bfloat16) * MLP_H * MLP_NIN))) return st;
   if ((st = dmalloc(c, (void**)&s->W2b, sizeof(__nv_bfloat16) * MLP_H * MLP_H))) return st;
-  ADC_CUDA(c, cudaMemset(s->m1, 0, sizeof(float) * NPARAM));
-  ADC_CUDA(c, cudaMemset(s->m2, 0, sizeof(float) * NPARAM));
+  ADC_CUDA(c, cudaMemsetAsync(s->m1, 0, sizeof(float) * NPARAM, c->stream));
+  ADC_CUDA(c, cudaMemsetAsync(s->m2, 0, sizeof(float) * NPARAM, c->stream));
   return ADCGPU_OK;
 }
 
@@ -549,9 +549,9 @@ extern "C" int adcgpu_mlp_set_params(adcgpu_ctx* h, const float* params, int64_t
   int st = ensure_state(c);
   if (st) return st;
   MlpState* s = state(c);
-  ADC_CUDA(c, cudaMemcpy(s->p, params, sizeof(float) * NPARAM, cudaMemcpyHostToDevice));
-  ADC_CUDA(c, cudaMemset(s->m1, 0, sizeof(float) * NPARAM));
-  ADC_CUDA(c, cudaMemset(s->m2, 0, sizeof(float) * NPARAM));
+  ADC_CUDA(c, h2d(c, s->p, params, sizeof(float) * NPARAM));
+  ADC_CUDA(c, cudaMemsetAsync(s->m1, 0, sizeof(float) * NPARAM, c->stream));
+  ADC_CUDA(c, cudaMemsetAsync(s->m2, 0, sizeof(float) * NPARAM, c->stream));
   s->step = 0;
   st = refresh_bf16(c);
   if (st) return st;
@@ -564,7 +564,7 @@ extern "C" int adcgpu_mlp_get_params(adcgpu_ctx* h, float* params, int64_t n) {
   if (!c || !params || n != NPARAM || !c->mlp) return ADCGPU_BAD_INPUT;
   cudaSetDevice(c->device);
   ADC_CUDA(c, cudaStreamSynchronize(c->stream));
-  ADC_CUDA(c, cudaMemcpy(params, state(c)->p, sizeof(float) * NPARAM, cudaMemcpyDeviceToHost));
+  ADC_CUDA(c, d2h(c, params, state(c)->p, sizeof(float) * NPARAM));
   return ADCGPU_OK;
 }
 

@@ -1397,13 +1397,13 @@ int build_chunks(Ctx* c, int chunk) {
   plan->d_chunks = plan->d_items = plan->d_titems = nullptr;
   int st;
   if ((st = dmalloc(c, (void**)&plan->d_titems, sizeof(int2) * titems.size()))) return st;
-  ADC_CUDA(c, cudaMemcpy(plan->d_titems, titems.data(), sizeof(int2) * titems.size(), cudaMemcpyHostToDevice));
+  ADC_CUDA(c, h2d(c, plan->d_titems, titems.data(), sizeof(int2) * titems.size()));
   plan->ntitems = (int)titems.size();
   if ((st = dmalloc(c, (void**)&plan->d_chunks, sizeof(int2) * chunks.size()))) return st;
   if ((st = dmalloc(c, (void**)&plan->d_items, sizeof(int2) * std::max<size_t>(items.size(), 1)))) return st;
-  ADC_CUDA(c, cudaMemcpy(plan->d_chunks, chunks.data(), sizeof(int2) * chunks.size(), cudaMemcpyHostToDevice));
+  ADC_CUDA(c, h2d(c, plan->d_chunks, chunks.data(), sizeof(int2) * chunks.size()));
   if (!items.empty())
-    ADC_CUDA(c, cudaMemcpy(plan->d_items, items.data(), sizeof(int2) * items.size(), cudaMemcpyHostToDevice));
+    ADC_CUDA(c, h2d(c, plan->d_items, items.data(), sizeof(int2) * items.size()));
   plan->nchunks = (int)chunks.size();
   plan->nitems = (int)items.size();
   plan->chunk = chunk;

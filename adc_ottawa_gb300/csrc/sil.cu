@@ -210,7 +210,7 @@ struct SilEngine {
     ST(dmalloc(c, (void**)&d_kptr, sizeof(double*) * (kdim + 2)));
     std::vector<double*> kp(kdim + 2, nullptr);
     for (int q = 1; q <= kdim; ++q) kp[q] = K(q);
-    ADC_CUDA(c, cudaMemcpy(d_kptr, kp.data(), sizeof(double*) * (kdim + 2), cudaMemcpyHostToDevice));
+    ADC_CUDA(c, h2d(c, d_kptr, kp.data(), sizeof(double*) * (kdim + 2)));
     return ADCGPU_OK;
   }
 
@@ -436,7 +436,7 @@ extern "C" int adcgpu_autocorr(adcgpu_ctx* h, int nwp, const double* f, double t
       norm0[p] = std::sqrt(s);
       for (int64_t i = 0; i < N; ++i) blk[(size_t)p * N + i] = f[(size_t)p * N + i] / norm0[p];
     }
-    ADC_CUDA(c, cudaMemcpy(E.Psi, blk.data(), sizeof(double) * blk.size(), cudaMemcpyHostToDevice));
+    ADC_CUDA(c, h2d(c, E.Psi, blk.data(), sizeof(double) * blk.size()));
   }
   const double intperiod = 0.5 * tout, tiny = 1e-9;
   const int nsteps = (int)(tfinal / intperiod);
@@ -501,18 +501,18 @@ extern "C" int adcgpu_silstep(adcgpu_ctx* h, double* psi, double* dtpsi, int psi
   ST(E.alloc());
   std::vector<double> blk((size_t)N * 2);
   for (int64_t i = 0; i < N; ++i) { blk[i] = psi[2 * i]; blk[N + i] = psi[2 * i + 1]; }
-  ADC_CUDA(c, cudaMemcpy(E.Psi, blk.data(), sizeof(double) * 2 * N, cudaMemcpyHostToDevice));
+  ADC_CUDA(c, h2d(c, E.Psi, blk.data(), sizeof(double) * 2 * N));
   for (int64_t i = 0; i < N; ++i) { blk[i] = dtpsi[2 * i]; blk[N + i] = dtpsi[2 * i + 1]; }
-  ADC_CUDA(c, cudaMemcpy(E.K(1), blk.data(), sizeof(double) * 2 * N, cudaMemcpyHostToDevice));
+  ADC_CUDA(c, h2d(c, E.K(1), blk.data(), sizeof(double) * 2 * N));
   std::vector<SilPacket> pk(1);
   std::vector<int> mask(1, 1);
   std::vector<double> period(1, intperiod);
   ST(E.silstep(mask, pk, period, tol, relax != 0));
   ADC_CUDA(c, cudaStreamSynchronize(c->stream));
   if (pk[0].err) return pk[0].err;
-  ADC_CUDA(c, cudaMemcpy(blk.data(), E.Psi, sizeof(double) * 2 * N, cudaMemcpyDeviceToHost));
+  ADC_CUDA(c, d2h(c, blk.data(), E.Psi, sizeof(double) * 2 * N));
   for (int64_t i = 0; i < N; ++i) { psi[2 * i] = blk[i]; psi[2 * i + 1] = blk[N + i]; }
-  ADC_CUDA(c, cudaMemcpy(blk.data(), E.K(1), sizeof(double) * 2 * N, cudaMemcpyDeviceToHost));
+  ADC_CUDA(c, d2h(c, blk.data(), E.K(1), sizeof(double) * 2 * N));
   for (int64_t i = 0; i < N; ++i) { dtpsi[2 * i] = blk[i]; dtpsi[2 * i + 1] = blk[N + i]; }
   if (stepsize_out) *stepsize_out = pk[0].Stepsize;
   if (trueorder_out) *trueorder_out = pk[0].TrueOrder;
