@@ -292,12 +292,12 @@ const std::vector<int64_t>& diag_order(Ctx* c);
 // Host<->device copies on the context's stream.  The stream is created
 // non-blocking, so it is not ordered with the legacy default stream that a
 // plain cudaMemcpy uses: a copy there could overtake kernels still queued on
-// the context's stream, or be overtaken by them.  h2d returns once the host
-// buffer may be reused (pageable sources are staged before the call returns)
-// and is ordered before later work on the stream; d2h returns when the data
-// has arrived.
+// the context's stream, or be overtaken by them.  Both return when the copy
+// has completed (so a caller's buffer, pinned or not, may be reused at once)
+// and are ordered after earlier and before later work on the stream.
 inline cudaError_t h2d(Ctx* c, void* dst, const void* src, size_t bytes) {
-  return cudaMemcpyAsync(dst, src, bytes, cudaMemcpyHostToDevice, c->stream);
+  cudaError_t e = cudaMemcpyAsync(dst, src, bytes, cudaMemcpyHostToDevice, c->stream);
+  return e != cudaSuccess ? e : cudaStreamSynchronize(c->stream);
 }
 inline cudaError_t d2h(Ctx* c, void* dst, const void* src, size_t bytes) {
   cudaError_t e = cudaMemcpyAsync(dst, src, bytes, cudaMemcpyDeviceToHost, c->stream);
