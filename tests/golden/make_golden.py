@@ -1,12 +1,14 @@
 """Generate the golden fixtures in tests/golden/ from the oracle.
 
 Run on a CPU host:  python tests/golden/make_golden.py [--config2]
+                    python tests/golden/make_golden.py --chebyshev
 
 The fixtures pin (i) the seeded synthetic generator bit for bit across
 hosts (SHA-256 of the orbital energies and packed ERIs), (ii) the oracle's
 kept structure (count and an order-independent hash), diagonal and values,
 and (iii) the oracle's eigenvalues, Lanczos spectra and SIL autocorrelation
-on small systems.  --config2 adds the nocc=10, nvirt=110 system (about
+on small systems.  --chebyshev writes chebyshev.json alone (the
+order-domain autocorrelation and spectral bounds).  --config2 adds the nocc=10, nvirt=110 system (about
 137 M kept elements; the oracle Davidson takes tens of minutes there).
 """
 from __future__ import annotations
@@ -69,7 +71,28 @@ def small_case(no, nv, seed, dav=None, lanczos=None, sil=None) -> dict:
     return out
 
 
+def chebyshev_case() -> dict:
+    """Chebyshev order-domain autocorrelation on nocc=5 nvirt=19 (seed 1234):
+    the oracle's 'davlanc' bounds, and C_0..C_80 of a seeded uniform start
+    vector with bounds [Emin - 0.2, 1.1 Emax] (which contain the spectrum)."""
+    no, nv, seed = 5, 19, 1234
+    e, eri = synth_system(no, nv, seed)
+    M = oracle.Matrix.build(no, nv, e, eri)
+    st, raw = M.spectral_bounds()
+    assert st == 0
+    bounds = [float(raw[0]) - 0.2, 1.1 * float(raw[1])]
+    q0 = synth_uniform_block(M.ndim, 1, 79)[:, 0]
+    auto, _ = M.chebyshev_auto(q0, np.array(bounds), 40)
+    return {"nocc": no, "nvirt": nv, "seed": seed, "vector_seed": 79, "spectral_bounds": raw.tolist(),
+            "bounds": bounds, "chebyord": 40, "auto": auto.tolist()}
+
+
 def main():
+    if "--chebyshev" in sys.argv:
+        with open(os.path.join(HERE, "chebyshev.json"), "w") as f:
+            json.dump(chebyshev_case(), f, indent=1)
+        print("wrote chebyshev.json")
+        return
     cases = [
         small_case(2, 3, 5),
         small_case(4, 9, 7, dav={"nstates": 4, "tol": 1e-8}),

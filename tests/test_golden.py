@@ -61,3 +61,18 @@ def test_oracle_solvers_reproduce(built):
     st, a, _ = M.autocorr(f, S["tout"], S["tfinal"], S["kdim"], S["tol"])
     ref = np.array(S["auto_re"]) + 1j * np.array(S["auto_im"])
     assert np.abs(a - ref).max() <= 1e-9 * np.abs(ref).max()
+
+
+def test_oracle_chebyshev_reproduces(built):
+    """chebyshev.json: the oracle's 'davlanc' bounds and C_0..C_80."""
+    from adc_ottawa_gb300 import synth_uniform_block
+
+    c = load("chebyshev.json")
+    e, eri = system(c["nocc"], c["nvirt"], c["seed"])
+    M = oracle.Matrix.build(c["nocc"], c["nvirt"], e, eri)
+    st, raw = M.spectral_bounds()
+    assert st == 0 and np.abs(raw - np.array(c["spectral_bounds"])).max() <= 1e-9
+    q0 = synth_uniform_block(M.ndim, 1, c["vector_seed"])[:, 0]
+    a, _ = M.chebyshev_auto(q0, np.array(c["bounds"]), c["chebyord"])
+    ref = np.array(c["auto"])
+    assert np.abs(a - ref).max() <= 1e-12 * ref[0]

@@ -144,3 +144,22 @@ def test_device_bytes_released_after_solvers(cfg1):
     g.chebyshev_auto(np.ones(M.ndim), [w[0] - 0.2, 1.1 * w[-1]], 10)
     g.spectral_bounds()
     assert g.device_bytes() == b0
+
+
+def test_matches_golden_fixture(cfg1):
+    """tests/golden/chebyshev.json (written by the oracle): bounds within
+    1e-8 Ha, C_k within 1e-7 C_0."""
+    import json
+    import os
+
+    from adc_ottawa_gb300 import synth_uniform_block
+    from tests.conftest import ROOT
+
+    g, M, w, n1 = cfg1
+    c = json.load(open(os.path.join(ROOT, "tests", "golden", "chebyshev.json")))
+    assert (c["nocc"], c["nvirt"], c["seed"]) == (5, 19, 1234)
+    assert np.abs(g.spectral_bounds() - np.array(c["spectral_bounds"])).max() <= 1e-8
+    q0 = synth_uniform_block(g.ndim, 1, c["vector_seed"])[:, 0]
+    auto, _ = g.chebyshev_auto(q0, c["bounds"], c["chebyord"])
+    ref = np.array(c["auto"])
+    assert np.abs(auto[0] - ref).max() <= 1e-7 * ref[0]
