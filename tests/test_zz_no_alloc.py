@@ -5,7 +5,8 @@ such as a host application working inside a device-memory budget fixed in
 advance, or a host thread that must not stall on cudaFree.  It must
 give the same product as the regular entry point (adcgpu_sigma_device) on
 the same device buffers, on consecutive calls that reuse its static scratch,
-and it must refuse sizes beyond that scratch.  This file is collected last.
+and it must refuse sizes beyond that scratch.  This file is collected after
+the builder, learned-preconditioner and solver tests.
 """
 import ctypes as C
 
