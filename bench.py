@@ -17,6 +17,9 @@ e2e    = the same solve through the C ABI from host buffers: orbital energies
 
 Multi-GPU: the path does not shard (one matrix per device); --gpus N runs N
 independent replicas (torchrun, one rank per GPU), no collective.
+
+Secondary workloads (--suite lanczos | sil | batch | learned | cheb) print one
+JSON line each; see --help.
 """
 from __future__ import annotations
 
