@@ -57,6 +57,7 @@ def lib():
         L.orc_matvec.argtypes = [C.c_void_p, C.c_int, _dp, _dp, C.c_int]
         L.orc_eigh.argtypes = [C.c_int, _dp, _dp, _dp]
         L.orc_heapsort_index.argtypes = [C.c_int, _dp, _ip]
+        L.orc_heapsort_index_desc.argtypes = [C.c_int, _dp, _ip]
         L.orc_davidson.argtypes = [C.c_void_p, _ip, C.c_double, C.c_int, _dp, _dp, _ip]
         L.orc_davidson.restype = C.c_int
         L.orc_block_lanczos.argtypes = [C.c_void_p, C.c_int, C.c_int, C.c_int, _dp, C.c_int, _dp, _dp]
@@ -242,6 +243,14 @@ def heapsort_index(arr):
     arr = np.ascontiguousarray(arr, np.float64)
     out = np.empty(len(arr), np.int32)
     lib().orc_heapsort_index(len(arr), _p(arr), _p(out, _ip))
+    return out
+
+
+def heapsort_index_desc(arr):
+    """dsortindxa1('D', ...): descending, ties in heap order (1-based)."""
+    arr = np.ascontiguousarray(arr, np.float64)
+    out = np.empty(len(arr), np.int32)
+    lib().orc_heapsort_index_desc(len(arr), _p(arr), _p(out, _ip))
     return out
 
 

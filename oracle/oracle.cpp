@@ -540,6 +540,38 @@ void dsortindxa1_A(int n, const double* arrin, std::vector<int>& indx) {
   }
 }
 
+// dsortindxa1 with order 'D' (misc.f90:515-551): the same heapsort with
+// both comparisons reversed; init_vec_singlesubspace sorts hii with it.
+void dsortindxa1_D(int n, const double* arrin, std::vector<int>& indx) {
+  indx.resize(n);
+  for (int i = 0; i < n; ++i) indx[i] = i + 1;
+  if (n == 1) return;
+  auto arr = [&](int k) { return arrin[k - 1]; };
+  auto ix = [&](int pos) -> int& { return indx[pos - 1]; };
+  int l = n / 2 + 1, ir = n, indxt, i, j;
+  double q;
+  for (;;) {
+    if (l > 1) {
+      l = l - 1;
+      indxt = ix(l);
+      q = arr(indxt);
+    } else {
+      indxt = ix(ir);
+      q = arr(indxt);
+      ix(ir) = ix(1);
+      ir = ir - 1;
+      if (ir == 1) { ix(1) = indxt; return; }
+    }
+    i = l; j = l + l;
+    while (j <= ir) {
+      if (j < ir) { if (arr(ix(j)) > arr(ix(j + 1))) j = j + 1; }
+      if (q > arr(ix(j))) { ix(i) = ix(j); i = j; j = j + j; }
+      else j = ir + 1;
+    }
+    ix(i) = indxt;
+  }
+}
+
 // hxvec_incore (block_davidson.f90:844-883): W(:,n) = hii.V(:,n) + sum_k ...
 void hxvec(const OrcMatrix& M, int ncol, const double* V, int64_t ldv, double* W, int64_t ldw,
            int nthreads) {
@@ -580,6 +612,12 @@ int orc_eigh(int n, const double* A, double* w, double* V) {
 void orc_heapsort_index(int n, const double* arr, int32_t* indx_out) {
   std::vector<int> ix;
   dsortindxa1_A(n, arr, ix);
+  for (int i = 0; i < n; ++i) indx_out[i] = ix[i];
+}
+
+void orc_heapsort_index_desc(int n, const double* arr, int32_t* indx_out) {
+  std::vector<int> ix;
+  dsortindxa1_D(n, arr, ix);
   for (int i = 0; i < n; ++i) indx_out[i] = ix[i];
 }
 

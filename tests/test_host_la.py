@@ -73,3 +73,15 @@ def test_heapsort_matches_reference_order(built, driver, tmp_path, n):
     arr = np.round(rs.uniform(0.0, 3.0, n) * 4) / 4          # many ties
     idx = run(driver, "heap", [n], arr, tmp_path, np.int64, n)
     assert np.array_equal(idx, oracle.heapsort_index(arr).astype(np.int64))
+
+
+@pytest.mark.parametrize("n", [2, 9, 800, 5000])
+def test_descending_heapsort_is_ascending_on_negated_keys(built, driver, tmp_path, n):
+    """init_vec_singlesubspace sorts hii with dsortindxa1('D'); the library
+    runs its ascending heapsort on -hii.  Both comparisons flip, so the
+    permutation, ties included, is the reference's."""
+    rs = np.random.RandomState(n + 1)
+    arr = np.round(rs.uniform(-1.0, 3.0, n) * 4) / 4          # many ties, both signs
+    idx = run(driver, "heap", [n], -arr, tmp_path, np.int64, n)
+    assert np.array_equal(idx, oracle.heapsort_index_desc(arr).astype(np.int64))
+    assert np.array_equal(oracle.heapsort_index(-arr), oracle.heapsort_index_desc(arr))
