@@ -130,6 +130,19 @@ class AdcGpu:
             msg = lib().adcgpu_last_error(self._h)
             raise AdcGpuError(st, f"{what}: {msg.decode() if msg else ''}")
 
+    def _rows(self, a: np.ndarray, what: str) -> None:
+        """Host arrays cross the C ABI as bare pointers, so their shape is
+        checked here: ndim rows and at least one column."""
+        if a.ndim != 2 or a.shape[0] != self.ndim or a.shape[1] < 1:
+            raise AdcGpuError(12, f"{what}: expected {self.ndim} rows, got shape {a.shape}")
+
+    @staticmethod
+    def _bounds(bounds) -> np.ndarray:
+        b = np.ascontiguousarray(bounds, np.float64).reshape(-1)
+        if b.shape != (2,):
+            raise AdcGpuError(12, f"bounds must be [Emin, Emax], got {b.shape[0]} values")
+        return b
+
     def close(self):
         if getattr(self, "_h", None):
             lib().adcgpu_ctx_destroy(self._h)
@@ -190,6 +203,7 @@ class AdcGpu:
         one = V.ndim == 1
         if one:
             V = V.reshape(-1, 1, order="F")
+        self._rows(V, "sigma")
         W = np.empty_like(V, order="F")
         self._check(lib().adcgpu_sigma(self._h, V.shape[1], ptr(V), ptr(W)), "sigma")
         return W[:, 0] if one else W
@@ -231,6 +245,7 @@ class AdcGpu:
     def lancdiag_block(self, q0: np.ndarray, ncycles: int, orthotype: int = 0, want_tmat: bool = True,
                        want_evals: bool = True, want_ritz: bool = False):
         q0 = np.asfortranarray(q0, np.float64)
+        self._rows(q0, "lancdiag_block")
         b = q0.shape[1]
         nvec = b * ncycles
         T = np.empty((nvec, nvec), order="F") if want_tmat else None
@@ -244,6 +259,8 @@ class AdcGpu:
                 relax: bool = False, restart: bool = True, stdform: bool = True):
         psi = np.ascontiguousarray(psi, np.complex128)
         dtpsi = np.ascontiguousarray(dtpsi, np.complex128)
+        if psi.shape != (self.ndim,) or dtpsi.shape != (self.ndim,):
+            raise AdcGpuError(12, f"silstep: psi and dtpsi must hold {self.ndim} values")
         step = C.c_double(0.0)
         order = C.c_int(0)
         state = SilState()
@@ -258,6 +275,7 @@ class AdcGpu:
         f = np.asfortranarray(fvecs, np.float64)
         if f.ndim == 1:
             f = f.reshape(-1, 1, order="F")
+        self._rows(f, "propagate_fvec")
         nwp = f.shape[1]
         nt = int(tfinal / (0.5 * tout)) + 1
         out = np.zeros((nwp, nt, 2))
@@ -288,8 +306,9 @@ class AdcGpu:
         q = np.asfortranarray(q0, np.float64)
         if q.ndim == 1:
             q = q.reshape(-1, 1, order="F")
+        self._rows(q, "chebyshev_auto")
         nvec = q.shape[1]
-        b = np.ascontiguousarray(bounds, np.float64)
+        b = self._bounds(bounds)
         ordr = max(chebyord, 0) - max(chebyord, 0) % 2     # the library's rounded order sets the strides
         out = np.zeros((nvec, 2 * ordr + 1))
         h1 = np.zeros((nvec, ordr + 1, self.nocc * self.nvirt)) if save1h1p else None
@@ -306,7 +325,8 @@ class AdcGpu:
         one = q.ndim == 1
         if one:
             q = q.reshape(-1, 1, order="F")
-        b = np.ascontiguousarray(bounds, np.float64)
+        self._rows(q, "project_psi0")
+        b = self._bounds(bounds)
         self._check(lib().adcgpu_chebyshev_project(self._h, q.shape[1], ptr(q), ptr(b), chebyord, projen,
                                                    int(df)), "project_psi0")
         return q[:, 0] if one else q
