@@ -3,7 +3,7 @@
 ! and drop-in wrappers for the ADC(2)-s hot path of ADC_ottawa.
 !
 ! The wrappers keep the reference's argument lists and read the same
-! module globals (parameters.f90), so the drivers change only the name
+! module globals (parameters.f90), so the calling routines change only the name
 ! they call:
 !
 !   write_fspace_adc2_1  -> write_fspace_adc2_1_gpu   (fspacetrial.f90:533)

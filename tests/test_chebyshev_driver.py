@@ -1,5 +1,5 @@
 """Host logic of chebyshev_auto_order_domain (chebyspec.f90:25-116) on the
-CPU: the driver is run against a stand-in for the device context whose three
+CPU: chebyshev_auto_order_domain runs against a stand-in for the device context whose three
 calls are answered by the oracle, so the widening of the bounds (:84-85), the
 optional projection (:90), the even-order rounding and the output files are
 checked without a GPU."""
@@ -11,7 +11,7 @@ from tests.conftest import system
 
 
 class OracleContext:
-    """The three AdcGpu calls the driver makes, answered by the oracle."""
+    """The three AdcGpu calls chebyshev_auto_order_domain makes, answered by the oracle."""
 
     def __init__(self, M, n1):
         self.M, self.n1, self.calls = M, n1, []
