@@ -332,6 +332,38 @@ class AdcGpu:
         return q[:, 0] if one else q
 
 
+def write_davidson_file(path: str, evals: np.ndarray, evecs: np.ndarray) -> None:
+    """The davname eigenpair file of wreigenpairs (block_davidson.f90:1469-1532):
+    one Fortran unformatted sequential record (i, E_i, x_i) per root, roots in
+    the given (ascending) order; readdavvc (adc_common.f90:999-1052) reads it."""
+    ev = np.ascontiguousarray(evals, np.float64).reshape(-1)
+    X = np.asfortranarray(evecs, np.float64)
+    if X.ndim != 2 or X.shape[1] != ev.shape[0]:
+        raise AdcGpuError(12, f"write_davidson_file: {ev.shape[0]} values but vectors of shape {X.shape}")
+    st = lib().adcgpu_write_davidson_file(path.encode(), X.shape[0], X.shape[1], ptr(ev), ptr(X))
+    if st:
+        raise AdcGpuError(st, f"write_davidson_file {path}")
+
+
+def read_davidson_file(path: str, ndim: int):
+    """Records (i, E_i, x_i) of a davname file, as readdavvc reads them."""
+    idx, ev, vecs = [], [], []
+    with open(path, "rb") as f:
+        while True:
+            head = f.read(4)
+            if not head:
+                break
+            n = int(np.frombuffer(head, np.int32)[0])
+            body = f.read(n)
+            tail = int(np.frombuffer(f.read(4), np.int32)[0])
+            if n != tail or n != 12 + 8 * ndim:
+                raise AdcGpuError(12, f"{path}: record of {n} bytes (trailer {tail}), expected {12 + 8 * ndim}")
+            idx.append(int(np.frombuffer(body[:4], np.int32)[0]))
+            ev.append(float(np.frombuffer(body[4:12], np.float64)[0]))
+            vecs.append(np.frombuffer(body[12:], np.float64).copy())
+    return np.array(idx), np.array(ev), np.array(vecs).T
+
+
 def fortran_e(x: float, w: int = 21, d: int = 14) -> str:
     """Fortran Ew.d edit descriptor (0.ddddE+xx form, as gfortran writes it)."""
     x = float(x)

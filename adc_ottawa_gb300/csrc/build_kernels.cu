@@ -347,9 +347,9 @@ __global__ void k_export_coupling(GeomDev g, const double* __restrict__ Bt, cons
   }
 }
 
-inline int grid_for(int64_t n, int block) {
+inline int grid_for(const Ctx* c, int64_t n, int block) {
   int64_t g = (n + block - 1) / block;
-  return (int)std::min<int64_t>(std::max<int64_t>(g, 1), 152LL * 32);
+  return (int)std::min<int64_t>(std::max<int64_t>(g, 1), (int64_t)c->nsm * 32);
 }
 
 }  // namespace
@@ -363,7 +363,7 @@ int build_eri_blocks_from_packed(Ctx* c, const double* d_packed) {
     if (*dst[k]) { dfree(c, *dst[k], 0); *dst[k] = nullptr; }
     int st = dmalloc(c, (void**)dst[k], sizeof(double) * sz[k]);
     if (st) return st;
-    k_gather_block<<<grid_for(sz[k], 256), 256, 0, c->stream>>>(d_packed, *dst[k], k, no, nv, sz[k]); ADC_COUNT_LAUNCH();
+    k_gather_block<<<grid_for(c, sz[k], 256), 256, 0, c->stream>>>(d_packed, *dst[k], k, no, nv, sz[k]); ADC_COUNT_LAUNCH();
     ADC_CUDA(c, cudaGetLastError());
   }
   ADC_CUDA(c, cudaStreamSynchronize(c->stream));
@@ -394,13 +394,13 @@ int build_matrix(Ctx* c) {
 
   k_ca<<<(int)((nv * (int64_t)nv + 127) / 128), 128, 0, s>>>(E, c->d_e, d_ca); ADC_COUNT_LAUNCH();
   k_cb<<<(no * no + 63) / 64, 64, 0, s>>>(E, c->d_e, d_cb); ADC_COUNT_LAUNCH();
-  k_cc_tables<<<grid_for(n1 * n1, 256), 256, 0, s>>>(E, c->d_e, d_X, d_D1); ADC_COUNT_LAUNCH();
+  k_cc_tables<<<grid_for(c, n1 * n1, 256), 256, 0, s>>>(E, c->d_e, d_X, d_D1); ADC_COUNT_LAUNCH();
   ADC_CUDA(c, cudaGetLastError());
   dim3 tiles((unsigned)((n1 + PT - 1) / PT), (unsigned)((n1 + PT - 1) / PT));
   k_phph<<<tiles, dim3(PT, PT), 0, s>>>(E, c->d_e, d_X, d_D1, d_ca, d_cb, c->d_A, c->d_diag, d_kept); ADC_COUNT_LAUNCH();
   ADC_CUDA(c, cudaGetLastError());
-  k_diag2<<<grid_for(G.n2, 256), 256, 0, s>>>(g, c->d_e, c->d_diag); ADC_COUNT_LAUNCH();
-  k_coupling<<<152 * 8, 256, 0, s>>>(E, g, c->d_Bt, c->d_rowcount + n1); ADC_COUNT_LAUNCH();
+  k_diag2<<<grid_for(c, G.n2, 256), 256, 0, s>>>(g, c->d_e, c->d_diag); ADC_COUNT_LAUNCH();
+  k_coupling<<<c->nsm * 8, 256, 0, s>>>(E, g, c->d_Bt, c->d_rowcount + n1); ADC_COUNT_LAUNCH();
   ADC_CUDA(c, cudaGetLastError());
   unsigned long long kept_ph = 0;
   ADC_CUDA(c, cudaMemcpyAsync(&kept_ph, d_kept, sizeof(kept_ph), cudaMemcpyDeviceToHost, s));
@@ -445,7 +445,7 @@ int export_coo_device(Ctx* c, double* d_h, int32_t* d_oi, int32_t* d_oj) {
   if ((st = dmalloc(c, &d_tmp, tmp_bytes))) return st;
   cub::DeviceScan::ExclusiveSum(d_tmp, tmp_bytes, d_cnt, d_pos, nrows, s);
   k_export_phph<<<n1, 256, 0, s>>>(c->d_A, n1, d_pos, d_h, d_oi, d_oj); ADC_COUNT_LAUNCH();
-  k_export_coupling<<<152 * 8, 256, 0, s>>>(g, c->d_Bt, d_pos + n1, d_h, d_oi, d_oj); ADC_COUNT_LAUNCH();
+  k_export_coupling<<<c->nsm * 8, 256, 0, s>>>(g, c->d_Bt, d_pos + n1, d_h, d_oi, d_oj); ADC_COUNT_LAUNCH();
   ADC_CUDA(c, cudaGetLastError());
   ADC_CUDA(c, cudaStreamSynchronize(s));
   dfree(c, d_tmp, tmp_bytes);

@@ -36,7 +36,8 @@ namespace adcgpu {
 
 namespace {
 
-constexpr int CHEB_BLK = 152 * 2;   // blocks of the fused pass: two per SM
+// blocks of the fused pass: two per SM (c: the context in scope)
+#define CHEB_BLK (c->nsm * 2)
 constexpr int CHEB_THR = 256;
 
 // Block partial sums of one pass, written to part[(blk*P + p)*3 + j].
@@ -279,7 +280,7 @@ static int singlesubspace_block(Ctx* c, int b, std::vector<double>& q0) {
     k_unit_cols<<<1, MC, 0, c->stream>>>(N, m, drows + j0, dV); ADC_COUNT_LAUNCH();
     st = sigma_fp64(c, m, dV, N, dW, N);
     if (st) break;
-    k_gather_rows<<<152, 256, 0, c->stream>>>(N, (int)sub, m, drows, dW, dS); ADC_COUNT_LAUNCH();
+    k_gather_rows<<<c->nsm, 256, 0, c->stream>>>(N, (int)sub, m, drows, dW, dS); ADC_COUNT_LAUNCH();
     if (cudaMemcpyAsync(hsub.data() + (size_t)j0 * sub, dS, sizeof(double) * (size_t)sub * m,
                         cudaMemcpyDeviceToHost, c->stream) != cudaSuccess ||
         cudaStreamSynchronize(c->stream) != cudaSuccess)
@@ -373,7 +374,7 @@ extern "C" int adcgpu_chebyshev_project(adcgpu_ctx* h, int nvec, double* q0, con
   G.c = c; G.N = N; G.P = nvec; G.ord = ord;
   ST(G.alloc(true, 0, false));
   ADC_CUDA(c, cudaMemcpyAsync(G.Q0, q0, G.blk_bytes, cudaMemcpyHostToDevice, c->stream));
-  k_cheb_scale<<<152 * 4, 256, 0, c->stream>>>(N * nvec, coef[0], G.Q0, G.acc); ADC_COUNT_LAUNCH();
+  k_cheb_scale<<<c->nsm * 4, 256, 0, c->stream>>>(N * nvec, coef[0], G.Q0, G.acc); ADC_COUNT_LAUNCH();
   ADC_CUDA(c, cudaGetLastError());
   double a, b;
   cheb_scaling(bounds, a, b);

@@ -114,6 +114,10 @@ int adcgpu_ctx_create(int device, adcgpu_ctx** out) {
   if (cudaSetDevice(device) != cudaSuccess) return ADCGPU_CUDA_ERROR;
   Ctx* c = new Ctx;
   c->device = device;
+  // grids are sized in multiples of the streaming-multiprocessor count
+  int nsm = 0;
+  if (cudaDeviceGetAttribute(&nsm, cudaDevAttrMultiProcessorCount, device) == cudaSuccess && nsm > 0) c->nsm = nsm;
+  else cudaGetLastError();
   if (cudaStreamCreateWithFlags(&c->stream, cudaStreamNonBlocking) != cudaSuccess ||
       cudaEventCreate(&c->ev0) != cudaSuccess || cudaEventCreate(&c->ev1) != cudaSuccess) {
     delete c;

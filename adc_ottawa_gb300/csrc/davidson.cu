@@ -52,10 +52,10 @@ __global__ void k_fill_random_f(float* x, int64_t n, uint64_t seed) {
 
 template <typename T> void fill_random(Ctx* c, T* x, int64_t n, uint64_t seed);
 template <> void fill_random<double>(Ctx* c, double* x, int64_t n, uint64_t seed) {
-  k_fill_random<<<152 * 4, 256, 0, c->stream>>>(x, n, seed); ADC_COUNT_LAUNCH();
+  k_fill_random<<<c->nsm * 4, 256, 0, c->stream>>>(x, n, seed); ADC_COUNT_LAUNCH();
 }
 template <> void fill_random<float>(Ctx* c, float* x, int64_t n, uint64_t seed) {
-  k_fill_random_f<<<152 * 4, 256, 0, c->stream>>>(x, n, seed); ADC_COUNT_LAUNCH();
+  k_fill_random_f<<<c->nsm * 4, 256, 0, c->stream>>>(x, n, seed); ADC_COUNT_LAUNCH();
 }
 
 template <typename T> int sigma_t(Ctx* c, int m, const T* V, int64_t ldv, T* W, int64_t ldw);
@@ -462,7 +462,7 @@ int DavidsonGPU<T>::guess_subdiag(const std::vector<double>& hdiag, int subdim) 
   ST(dmalloc(c, (void**)&d_sub, sizeof(int64_t) * subdim));
   ST(dmalloc(c, (void**)&d_H, sizeof(double) * (size_t)subdim * subdim));
   ADC_CUDA(c, cudaMemcpyAsync(d_sub, sub.data(), sizeof(int64_t) * subdim, cudaMemcpyHostToDevice, c->stream));
-  k_gather_sub<<<152 * 4, 256, 0, c->stream>>>(to_dev(c->geom), c->d_A, c->d_Bt, nullptr, d_sub,
+  k_gather_sub<<<c->nsm * 4, 256, 0, c->stream>>>(to_dev(c->geom), c->d_A, c->d_Bt, nullptr, d_sub,
                                                subdim, d_H); ADC_COUNT_LAUNCH();
   std::vector<double> H((size_t)subdim * subdim), w(subdim), Vs((size_t)subdim * subdim);
   ADC_CUDA(c, cudaMemcpyAsync(H.data(), d_H, sizeof(double) * H.size(), cudaMemcpyDeviceToHost, c->stream));

@@ -409,9 +409,9 @@ int Workspace::reserve(Ctx* c, size_t need) {
 }
 
 // Row blocks of the TN reduction: at least 4 blocks per SM on large N.
-static int tn_blocks(int64_t N) {
+static int tn_blocks(const Ctx* c, int64_t N) {
   int64_t b = (N + 1023) / 1024;
-  return (int)std::max<int64_t>(1, std::min<int64_t>(b, 152 * 4));
+  return (int)std::max<int64_t>(1, std::min<int64_t>(b, c->nsm * 4));
 }
 
 template <typename T, typename TA, typename TC>
@@ -419,7 +419,7 @@ int gemm_tn(Ctx* c, Workspace& ws, int64_t N, int p, int q, const T* A, int64_t 
             TC* C, int ldc, TC alpha, TC beta) {
   if (p <= 0 || q <= 0) return ADCGPU_OK;
   const int ntile = ((p + TN_P - 1) / TN_P) * ((q + TN_Q - 1) / TN_Q);
-  const int nblk = tn_blocks(N);
+  const int nblk = tn_blocks(c, N);
   const int64_t rows = ((N + nblk - 1) / nblk + TN_ROWS - 1) / TN_ROWS * TN_ROWS;
   size_t need = sizeof(TA) * (size_t)nblk * ntile * TN_P * TN_Q;
   int st = ws.reserve(c, need);
@@ -434,7 +434,7 @@ int gemm_tn(Ctx* c, Workspace& ws, int64_t N, int p, int q, const T* A, int64_t 
     k_gemm_tn_part<T, TA><<<dim3(nblk, ntile), 256, 0, c->stream>>>(N, p, q, A, lda, B, ldb, (TA*)ws.p, rows); ADC_COUNT_LAUNCH();
   }
   const int nout = ntile * TN_P * TN_Q;
-  k_gemm_tn_reduce<TA, TC><<<std::min((nout + 255) / 256, 152 * 8), 256, 0, c->stream>>>(p, q, nblk, ntile,
+  k_gemm_tn_reduce<TA, TC><<<std::min((nout + 255) / 256, c->nsm * 8), 256, 0, c->stream>>>(p, q, nblk, ntile,
                                                                                          (TA*)ws.p, C, ldc, alpha,
                                                                                          beta); ADC_COUNT_LAUNCH();
   ADC_CUDA(c, cudaGetLastError());
@@ -468,7 +468,7 @@ int gemm_nn(Ctx* c, int64_t N, int p, int q, T alpha, const T* A, int64_t lda, c
 template <typename T, typename TD>
 int precond_dpr(Ctx* c, int64_t N, int nb, const T* R, int64_t ldr, const double* d_lam, const TD* hii, T* Tout,
                 int64_t ldt) {
-  k_dpr<T, TD><<<152 * 8, 256, 0, c->stream>>>(N, nb, R, ldr, d_lam, hii, Tout, ldt); ADC_COUNT_LAUNCH();
+  k_dpr<T, TD><<<c->nsm * 8, 256, 0, c->stream>>>(N, nb, R, ldr, d_lam, hii, Tout, ldt); ADC_COUNT_LAUNCH();
   ADC_CUDA(c, cudaGetLastError());
   return ADCGPU_OK;
 }
@@ -476,7 +476,7 @@ int precond_dpr(Ctx* c, int64_t N, int nb, const T* R, int64_t ldr, const double
 template <typename T, typename TD>
 int precond_olsen(Ctx* c, Workspace& ws, int64_t N, int nb, const T* X, const T* R, int64_t ld, const double* d_lam,
                   const TD* hii, T* Tout, int64_t ldt, double* h_alpha_out) {
-  const int nblk = 152 * 2;
+  const int nblk = c->nsm * 2;
   int st = ws.reserve(c, sizeof(double) * (size_t)nblk * nb * 2 + sizeof(double) * 4 * nb);
   if (st) return st;
   double* part = (double*)ws.p;
@@ -489,7 +489,7 @@ int precond_olsen(Ctx* c, Workspace& ws, int64_t N, int nb, const T* X, const T*
   for (int i = 0; i < nb; ++i) alpha[i] = h[2 * i + 1] == 0.0 ? 0.0 : h[2 * i] / h[2 * i + 1];
   double* d_alpha = sums + 2 * nb;
   ADC_CUDA(c, cudaMemcpyAsync(d_alpha, alpha.data(), sizeof(double) * nb, cudaMemcpyHostToDevice, c->stream));
-  k_olsen_apply<T, TD><<<152 * 8, 256, 0, c->stream>>>(N, nb, X, R, ld, d_lam, d_alpha, hii, Tout, ldt); ADC_COUNT_LAUNCH();
+  k_olsen_apply<T, TD><<<c->nsm * 8, 256, 0, c->stream>>>(N, nb, X, R, ld, d_lam, d_alpha, hii, Tout, ldt); ADC_COUNT_LAUNCH();
   ADC_CUDA(c, cudaGetLastError());
   if (h_alpha_out) std::copy(alpha.begin(), alpha.end(), h_alpha_out);
   ADC_CUDA(c, cudaStreamSynchronize(c->stream));
@@ -499,7 +499,7 @@ int precond_olsen(Ctx* c, Workspace& ws, int64_t N, int nb, const T* X, const T*
 template <typename T>
 int residuals(Ctx* c, Workspace& ws, int64_t N, int nb, const T* X, const T* WY, int64_t ld, const double* d_lam,
               T* Rout, double* h_norm2) {
-  const int nblk = 152 * 2;
+  const int nblk = c->nsm * 2;
   int st = ws.reserve(c, sizeof(double) * ((size_t)nblk * nb + nb));
   if (st) return st;
   double* part = (double*)ws.p;
@@ -514,7 +514,7 @@ int residuals(Ctx* c, Workspace& ws, int64_t N, int nb, const T* X, const T* WY,
 
 template <typename TS, typename TD>
 int convert(Ctx* c, const TS* x, TD* y, int64_t n) {
-  k_convert<TS, TD><<<152 * 8, 256, 0, c->stream>>>(x, y, n); ADC_COUNT_LAUNCH();
+  k_convert<TS, TD><<<c->nsm * 8, 256, 0, c->stream>>>(x, y, n); ADC_COUNT_LAUNCH();
   ADC_CUDA(c, cudaGetLastError());
   return ADCGPU_OK;
 }

@@ -3,12 +3,16 @@
 // diagrmat block_davidson.f90:991 and initvec_subdiag :400; dsbev in
 // diagmat_banded block_lanczos.f90:2041; dsteqr in SILStep sillib.f90:355).
 //
-// Symmetric eigenproblem: Householder reduction to tridiagonal form followed
-// by the implicit QL iteration with Wilkinson shifts (the classical
-// tred2/tql2 pair of the EISPACK literature), written here for column-major
-// storage.  These matrices are at most a few thousand wide; the O(N)
-// tall-skinny work that forms them runs on the GPU.
+// Symmetric eigenproblem, in the formulation of Golub and Van Loan (Matrix
+// Computations, 4th ed.): Householder reduction to tridiagonal form by
+// symmetric rank-2 updates (Alg. 8.3.1, with the Householder vector of
+// Alg. 5.1.1), then the implicit symmetric QR iteration with a Wilkinson
+// shift, each step a chase of one Givens bulge down the unreduced block
+// (Alg. 8.3.2/8.3.3), eigenvectors accumulated from the rotations.  These
+// matrices are at most a few thousand wide; the O(N) tall-skinny work that
+// forms them runs on the GPU.
 #include <algorithm>
+#include <cfloat>
 #include <cmath>
 #include <cstring>
 #include <vector>
@@ -19,104 +23,122 @@ namespace adcgpu {
 
 namespace {
 
-// Reduce symmetric a (n x n, row-major view z[i][j] = a(i,j)) to tridiagonal
-// form; on exit z holds the orthogonal transformation, d the diagonal and
-// e the sub-diagonal (e[0] = 0).
-void tred2(int n, std::vector<double>& z, std::vector<double>& d, std::vector<double>& e) {
-  auto Z = [&](int i, int j) -> double& { return z[(size_t)i * n + j]; };
-  for (int i = n - 1; i > 0; --i) {
-    int l = i - 1;
-    double h = 0.0, scale = 0.0;
-    if (l > 0) {
-      for (int k = 0; k <= l; ++k) scale += std::fabs(Z(i, k));
-      if (scale == 0.0) {
-        e[i] = Z(i, l);
-      } else {
-        for (int k = 0; k <= l; ++k) { Z(i, k) /= scale; h += Z(i, k) * Z(i, k); }
-        double f = Z(i, l);
-        double g = f >= 0.0 ? -std::sqrt(h) : std::sqrt(h);
-        e[i] = scale * g;
-        h -= f * g;
-        Z(i, l) = f - g;
-        f = 0.0;
-        for (int j = 0; j <= l; ++j) {
-          Z(j, i) = Z(i, j) / h;
-          g = 0.0;
-          for (int k = 0; k <= j; ++k) g += Z(j, k) * Z(i, k);
-          for (int k = j + 1; k <= l; ++k) g += Z(k, j) * Z(i, k);
-          e[j] = g / h;
-          f += e[j] * Z(i, j);
-        }
-        double hh = f / (h + h);
-        for (int j = 0; j <= l; ++j) {
-          f = Z(i, j);
-          e[j] = g = e[j] - hh * f;
-          for (int k = 0; k <= j; ++k) Z(j, k) -= (f * e[k] + g * Z(i, k));
-        }
-      }
-    } else {
-      e[i] = Z(i, l);
+// Householder vector of x[0..m): v[0] = 1 and beta with
+// (I - beta v v^T) x = mu e_0, mu = ||x|| (beta = 0 and mu = x[0] when x is
+// already a multiple of e_0).
+double house(int m, const double* x, double* v, double* mu) {
+  double sigma = 0.0;
+  for (int i = 1; i < m; ++i) sigma += x[i] * x[i];
+  v[0] = 1.0;
+  for (int i = 1; i < m; ++i) v[i] = x[i];
+  if (sigma == 0.0) { *mu = x[0]; return 0.0; }
+  const double norm = std::sqrt(x[0] * x[0] + sigma);
+  // v0 = x0 - ||x||, written without cancellation when x0 > 0
+  const double v0 = x[0] <= 0.0 ? x[0] - norm : -sigma / (x[0] + norm);
+  for (int i = 1; i < m; ++i) v[i] /= v0;
+  *mu = norm;
+  return 2.0 * v0 * v0 / (sigma + v0 * v0);
+}
+
+// A (n x n column-major, full symmetric, overwritten) = Q T Q^T with T
+// tridiagonal: diagonal d[0..n), sub-diagonal e[0..n-1).  With Q != null
+// the orthogonal Q (n x n column-major) is formed.
+void tridiagonalise(int n, double* A, double* d, double* e, double* Q) {
+  auto a = [&](int i, int j) -> double& { return A[(size_t)j * n + i]; };
+  std::vector<double> V((size_t)n * n, 0.0), beta(n, 0.0), p(n), w(n);
+  for (int k = 0; k + 2 < n; ++k) {
+    const int m = n - k - 1;
+    double* v = &V[(size_t)k * n];
+    double mu;
+    beta[k] = house(m, &a(k + 1, k), v, &mu);
+    d[k] = a(k, k);
+    e[k] = mu;
+    const double bk = beta[k];
+    if (bk == 0.0) continue;
+    // p = beta A22 v; w = p - (beta p^T v / 2) v; A22 -= v w^T + w v^T
+    for (int i = 0; i < m; ++i) p[i] = 0.0;
+    for (int j = 0; j < m; ++j) {
+      const double vj = v[j];
+      const double* col = &a(k + 1, k + 1 + j);
+      for (int i = 0; i < m; ++i) p[i] += col[i] * vj;
     }
-    d[i] = h;
+    double pv = 0.0;
+    for (int i = 0; i < m; ++i) { p[i] *= bk; pv += p[i] * v[i]; }
+    const double K = 0.5 * bk * pv;
+    for (int i = 0; i < m; ++i) w[i] = p[i] - K * v[i];
+    for (int j = 0; j < m; ++j) {
+      double* col = &a(k + 1, k + 1 + j);
+      const double vj = v[j], wj = w[j];
+      for (int i = 0; i < m; ++i) col[i] -= v[i] * wj + w[i] * vj;
+    }
   }
-  d[0] = 0.0;
-  e[0] = 0.0;
-  for (int i = 0; i < n; ++i) {
-    int l = i - 1;
-    if (d[i] != 0.0) {
-      for (int j = 0; j <= l; ++j) {
-        double g = 0.0;
-        for (int k = 0; k <= l; ++k) g += Z(i, k) * Z(k, j);
-        for (int k = 0; k <= l; ++k) Z(k, j) -= g * Z(k, i);
-      }
+  if (n >= 2) {
+    d[n - 2] = a(n - 2, n - 2);
+    e[n - 2] = a(n - 1, n - 2);
+  }
+  d[n - 1] = a(n - 1, n - 1);
+  if (!Q) return;
+  // Q = H_0 H_1 ... H_{n-3}, accumulated from the right end
+  std::memset(Q, 0, sizeof(double) * (size_t)n * n);
+  for (int i = 0; i < n; ++i) Q[(size_t)i * n + i] = 1.0;
+  for (int k = n - 3; k >= 0; --k) {
+    const double bk = beta[k];
+    if (bk == 0.0) continue;
+    const int m = n - k - 1;
+    const double* v = &V[(size_t)k * n];
+    for (int j = k + 1; j < n; ++j) {
+      double* col = &Q[(size_t)j * n + k + 1];
+      double s = 0.0;
+      for (int i = 0; i < m; ++i) s += v[i] * col[i];
+      s *= bk;
+      for (int i = 0; i < m; ++i) col[i] -= s * v[i];
     }
-    d[i] = Z(i, i);
-    Z(i, i) = 1.0;
-    for (int j = 0; j <= l; ++j) Z(j, i) = Z(i, j) = 0.0;
   }
 }
 
-// Implicit QL on the tridiagonal (d, e); accumulates into z (row-major).
-bool tql2(int n, std::vector<double>& d, std::vector<double>& e, std::vector<double>* z) {
-  for (int i = 1; i < n; ++i) e[i - 1] = e[i];
-  if (n > 0) e[n - 1] = 0.0;
-  for (int l = 0; l < n; ++l) {
-    int iter = 0, m;
-    do {
-      for (m = l; m < n - 1; ++m) {
-        double dd = std::fabs(d[m]) + std::fabs(d[m + 1]);
-        if (std::fabs(e[m]) <= 1e-300 || std::fabs(e[m]) + dd == dd) break;
+// Eigenvalues of the symmetric tridiagonal (d, e) in place (d, unsorted);
+// with Z != null (n x n column-major, holding the basis the tridiagonal is
+// expressed in) the rotations are applied to its columns, so column i ends
+// as the eigenvector of d[i].  False if the iteration did not converge.
+bool tridiagonal_qr(int n, double* d, double* e, double* Z) {
+  int sweeps = 0;
+  int q = n - 1;
+  while (q > 0) {
+    for (int i = 0; i < q; ++i)
+      if (std::fabs(e[i]) <= DBL_EPSILON * (std::fabs(d[i]) + std::fabs(d[i + 1])) || std::fabs(e[i]) < DBL_MIN)
+        e[i] = 0.0;
+    while (q > 0 && e[q - 1] == 0.0) --q;
+    if (q == 0) break;
+    int p = q - 1;
+    while (p > 0 && e[p - 1] != 0.0) --p;
+    if (++sweeps > 30 * n) return false;
+    // Wilkinson shift from the trailing 2 x 2 of the block [p, q]
+    const double half = 0.5 * (d[q - 1] - d[q]), bq = e[q - 1];
+    const double mu = d[q] - bq * bq / (half + std::copysign(std::hypot(half, bq), half));
+    double x = d[p] - mu, z = e[p];
+    for (int k = p; k < q; ++k) {
+      const double r = std::hypot(x, z);
+      const double c = r == 0.0 ? 1.0 : x / r, s = r == 0.0 ? 0.0 : z / r;
+      if (k > p) e[k - 1] = r;
+      const double ak = d[k], ak1 = d[k + 1], bk = e[k];
+      d[k] = c * c * ak + 2.0 * c * s * bk + s * s * ak1;
+      d[k + 1] = s * s * ak - 2.0 * c * s * bk + c * c * ak1;
+      e[k] = c * s * (ak1 - ak) + (c * c - s * s) * bk;
+      if (k + 1 < q) {
+        z = s * e[k + 1];          // the bulge at (k + 2, k)
+        e[k + 1] *= c;
+        x = e[k];
       }
-      if (m != l) {
-        if (iter++ == 60) return false;
-        double g = (d[l + 1] - d[l]) / (2.0 * e[l]);
-        double r = std::hypot(g, 1.0);
-        g = d[m] - d[l] + e[l] / (g + (g >= 0.0 ? std::fabs(r) : -std::fabs(r)));
-        double s = 1.0, c = 1.0, p = 0.0;
-        int i;
-        for (i = m - 1; i >= l; --i) {
-          double f = s * e[i], b = c * e[i];
-          e[i + 1] = (r = std::hypot(f, g));
-          if (r == 0.0) { d[i + 1] -= p; e[m] = 0.0; break; }
-          s = f / r; c = g / r;
-          g = d[i + 1] - p;
-          r = (d[i] - g) * s + 2.0 * c * b;
-          d[i + 1] = g + (p = s * r);
-          g = c * r - b;
-          if (z) {
-            for (int k = 0; k < n; ++k) {
-              double& zk1 = (*z)[(size_t)k * n + i + 1];
-              double& zk = (*z)[(size_t)k * n + i];
-              f = zk1;
-              zk1 = s * zk + c * f;
-              zk = c * zk - s * f;
-            }
-          }
+      if (Z) {
+        double* zk = Z + (size_t)k * n;
+        double* zk1 = Z + (size_t)(k + 1) * n;
+        for (int i = 0; i < n; ++i) {
+          const double u = zk[i], t = zk1[i];
+          zk[i] = c * u + s * t;
+          zk1[i] = c * t - s * u;
         }
-        if (r == 0.0 && i >= l) continue;
-        d[l] -= p; e[l] = g; e[m] = 0.0;
       }
-    } while (m != l);
+    }
   }
   return true;
 }
@@ -125,24 +147,23 @@ bool tql2(int n, std::vector<double>& d, std::vector<double>& e, std::vector<dou
 
 bool host_syev(int n, const double* A, int lda, double* w, double* V) {
   if (n <= 0) return true;
-  std::vector<double> z((size_t)n * n), d(n), e(n);
-  // row-major z[i][j] = A(i,j) from the upper triangle of column-major A
+  std::vector<double> a((size_t)n * n), d(n), e(std::max(n - 1, 1), 0.0), Z;
+  // full symmetric copy from the upper triangle of column-major A
   for (int j = 0; j < n; ++j)
     for (int i = 0; i <= j; ++i) {
-      double x = A[(size_t)j * lda + i];
-      z[(size_t)i * n + j] = x;
-      z[(size_t)j * n + i] = x;
+      const double x = A[(size_t)j * lda + i];
+      a[(size_t)j * n + i] = x;
+      a[(size_t)i * n + j] = x;
     }
-  tred2(n, z, d, e);
-  if (!tql2(n, d, e, V ? &z : nullptr)) return false;
-  // sort ascending; eigenvector k is column k of z (row-major z[i][k])
+  if (V) Z.resize((size_t)n * n);
+  tridiagonalise(n, a.data(), d.data(), e.data(), V ? Z.data() : nullptr);
+  if (!tridiagonal_qr(n, d.data(), e.data(), V ? Z.data() : nullptr)) return false;
   std::vector<int> idx(n);
   for (int i = 0; i < n; ++i) idx[i] = i;
   std::stable_sort(idx.begin(), idx.end(), [&](int x, int y) { return d[x] < d[y]; });
   for (int c = 0; c < n; ++c) {
     w[c] = d[idx[c]];
-    if (V)
-      for (int r = 0; r < n; ++r) V[(size_t)c * n + r] = z[(size_t)r * n + idx[c]];
+    if (V) std::memcpy(V + (size_t)c * n, &Z[(size_t)idx[c] * n], sizeof(double) * n);
   }
   return true;
 }
@@ -152,7 +173,7 @@ bool host_syev(int n, const double* A, int lda, double* w, double* V) {
 // (block_lanczos.f90:2006-2052): the band is reduced to tridiagonal form by
 // Givens rotations, one bandwidth at a time, each fill-in element chased
 // down the band (the band-reduction scheme of Rutishauser and Schwarz), in
-// O(n^2 kd) operations; the implicit QL iteration then gives the
+// O(n^2 kd) operations; the implicit symmetric QR iteration then gives the
 // eigenvalues in O(n^2).
 bool host_sbev_values(int n, int kd, const double* A, int lda, double* w) {
   if (n <= 0) return true;
@@ -195,10 +216,10 @@ bool host_sbev_values(int n, int kd, const double* A, int lda, double* w) {
       }
     }
   }
-  std::vector<double> d(n), e(n, 0.0);
+  std::vector<double> d(n), e(std::max(n - 1, 1), 0.0);
   for (int i = 0; i < n; ++i) d[i] = Z(i, i);
-  for (int i = 1; i < n; ++i) e[i] = Z(i, i - 1);
-  if (!tql2(n, d, e, nullptr)) return false;
+  for (int i = 0; i + 1 < n; ++i) e[i] = Z(i + 1, i);
+  if (!tridiagonal_qr(n, d.data(), e.data(), nullptr)) return false;
   std::sort(d.begin(), d.end());
   std::memcpy(w, d.data(), sizeof(double) * n);
   return true;

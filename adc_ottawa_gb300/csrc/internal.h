@@ -205,6 +205,7 @@ struct DevBuf {
 
 struct Ctx {
   int device = 0;
+  int nsm = 152;                  // streaming multiprocessors of the device (queried at creation)
   cudaStream_t stream = nullptr;
   cudaEvent_t ev0 = nullptr, ev1 = nullptr;
   std::string err;

@@ -66,7 +66,7 @@ struct LanczosGPU {
   }
 
   int colnorms(double* X, int ncol, std::vector<double>& out) {
-    const int nblk = 152 * 2;
+    const int nblk = c->nsm * 2;
     k_colnorm2_part<<<nblk, 256, 0, c->stream>>>(N, ncol, X, N, d_part); ADC_COUNT_LAUNCH();
     std::vector<double> part((size_t)nblk * ncol);
     ADC_CUDA(c, cudaMemcpyAsync(part.data(), d_part, sizeof(double) * part.size(), cudaMemcpyDeviceToHost, c->stream));
@@ -80,7 +80,7 @@ struct LanczosGPU {
 
   int scale_cols(double* X, int ncol, const std::vector<double>& s) {
     ADC_CUDA(c, cudaMemcpyAsync(d_s2, s.data(), sizeof(double) * ncol, cudaMemcpyHostToDevice, c->stream));
-    k_scale_cols<<<152 * 4, 256, 0, c->stream>>>(N, ncol, X, N, d_s2); ADC_COUNT_LAUNCH();
+    k_scale_cols<<<c->nsm * 4, 256, 0, c->stream>>>(N, ncol, X, N, d_s2); ADC_COUNT_LAUNCH();
     ADC_CUDA(c, cudaGetLastError());
     return ADCGPU_OK;
   }
@@ -143,7 +143,7 @@ struct LanczosGPU {
     ST(dmalloc(c, (void**)&Tmp, sizeof(double) * (size_t)N * b));
     ST(dmalloc(c, (void**)&d_s, sizeof(double) * (size_t)std::max(b * b, 4096)));
     ST(dmalloc(c, (void**)&d_s2, sizeof(double) * (size_t)std::max(b * b, 4096)));
-    ST(dmalloc(c, (void**)&d_part, sizeof(double) * 152 * 2 * (size_t)std::max(b, 64)));
+    ST(dmalloc(c, (void**)&d_part, sizeof(double) * c->nsm * 2 * (size_t)std::max(b, 64)));
     ADC_CUDA(c, cudaMemsetAsync(Q1, 0, sizeof(double) * N * b, c->stream));
     ADC_CUDA(c, cudaMemcpyAsync(Q2, q0_host, sizeof(double) * N * b, cudaMemcpyHostToDevice, c->stream));
     // init_vecs_random: normalise, then modified Gram-Schmidt twice
@@ -288,14 +288,14 @@ struct LanczosGPU {
         }
         dfree(c, d_part, 0);   // grow the norm partials to nvec columns
         d_part = nullptr;
-        ST(dmalloc(c, (void**)&d_part, sizeof(double) * 152 * 2 * (size_t)nvec));
+        ST(dmalloc(c, (void**)&d_part, sizeof(double) * c->nsm * 2 * (size_t)nvec));
         std::vector<double> nr;
         ST(colnorms(d_R, nvec, nr));
         for (auto& v : nr) v = 1.0 / v;
         double* d_sc = nullptr;
         ST(dmalloc(c, (void**)&d_sc, sizeof(double) * nvec));
         ADC_CUDA(c, cudaMemcpyAsync(d_sc, nr.data(), sizeof(double) * nvec, cudaMemcpyHostToDevice, c->stream));
-        k_scale_cols<<<152 * 4, 256, 0, c->stream>>>(N, nvec, d_R, N, d_sc); ADC_COUNT_LAUNCH();
+        k_scale_cols<<<c->nsm * 4, 256, 0, c->stream>>>(N, nvec, d_R, N, d_sc); ADC_COUNT_LAUNCH();
         ADC_CUDA(c, cudaMemcpyAsync(ritz_out, d_R, sizeof(double) * (size_t)N * nvec, cudaMemcpyDeviceToHost, c->stream));
         ADC_CUDA(c, cudaStreamSynchronize(c->stream));
         dfree(c, d_E, 0);

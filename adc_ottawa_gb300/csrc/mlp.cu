@@ -470,29 +470,29 @@ int mlp_fwd_bwd(Ctx* c, int G, int S, const float* d_feat, const float* d_t0, co
   cudaStream_t st = c->stream;
   const float* P = s->p;
   float* gr = s->grad;
-  k_to_bf16_f<<<152 * 4, 256, 0, st>>>(d_feat, X, M * MLP_NIN); ADC_COUNT_LAUNCH();
+  k_to_bf16_f<<<c->nsm * 4, 256, 0, st>>>(d_feat, X, M * MLP_NIN); ADC_COUNT_LAUNCH();
   // Z1 = X W1^T
   dim3 g1((MLP_H + 63) / 64, (unsigned)((M + 63) / 64), 1);
   k_gemm_bf16<<<g1, 128, 0, st>>>((int)M, MLP_H, MLP_NIN, X, MLP_NIN, 0, s->W1b, MLP_NIN, 1, Z1, MLP_H, 1.f, 0.f, 1); ADC_COUNT_LAUNCH();
-  k_bias_silu<<<152 * 4, 256, 0, st>>>(M, Z1, P + OFF_B1, H1, Z1); ADC_COUNT_LAUNCH();
+  k_bias_silu<<<c->nsm * 4, 256, 0, st>>>(M, Z1, P + OFF_B1, H1, Z1); ADC_COUNT_LAUNCH();
   k_gemm_bf16<<<g1, 128, 0, st>>>((int)M, MLP_H, MLP_H, H1, MLP_H, 0, s->W2b, MLP_H, 1, Z2, MLP_H, 1.f, 0.f, 1); ADC_COUNT_LAUNCH();
-  k_bias_silu<<<152 * 4, 256, 0, st>>>(M, Z2, P + OFF_B2, H2, Z2); ADC_COUNT_LAUNCH();
-  k_head<<<152 * 4, 256, 0, st>>>(M, H2, P, m); ADC_COUNT_LAUNCH();
+  k_bias_silu<<<c->nsm * 4, 256, 0, st>>>(M, Z2, P + OFF_B2, H2, Z2); ADC_COUNT_LAUNCH();
+  k_head<<<c->nsm * 4, 256, 0, st>>>(M, H2, P, m); ADC_COUNT_LAUNCH();
   if (d_m_out) ADC_CUDA(c, cudaMemcpyAsync(d_m_out, m, sizeof(float) * M, cudaMemcpyDeviceToDevice, st));
   k_cos_loss<<<G, 256, 0, st>>>(S, m, d_t0, d_e, dm, loss); ADC_COUNT_LAUNCH();
   // backward
   ADC_CUDA(c, cudaMemsetAsync(gr, 0, sizeof(float) * NPARAM, st));
-  k_grad_w3<<<152, MLP_H, 0, st>>>(M, dm, H2, gr + OFF_W3, gr + OFF_B3); ADC_COUNT_LAUNCH();
-  k_back_head<<<152 * 4, 256, 0, st>>>(M, dm, Z2, P, dZ); ADC_COUNT_LAUNCH();          // dZ = dZ2
-  k_colsum_bf16<<<152, MLP_H, 0, st>>>(M, dZ, gr + OFF_B2); ADC_COUNT_LAUNCH();
+  k_grad_w3<<<c->nsm, MLP_H, 0, st>>>(M, dm, H2, gr + OFF_W3, gr + OFF_B3); ADC_COUNT_LAUNCH();
+  k_back_head<<<c->nsm * 4, 256, 0, st>>>(M, dm, Z2, P, dZ); ADC_COUNT_LAUNCH();          // dZ = dZ2
+  k_colsum_bf16<<<c->nsm, MLP_H, 0, st>>>(M, dZ, gr + OFF_B2); ADC_COUNT_LAUNCH();
   const int ks = (int)std::min<int64_t>(64, std::max<int64_t>(1, M / 4096));
   // dW2 = dZ2^T H1  (H x H, K = M)
   dim3 g2((MLP_H + 63) / 64, (MLP_H + 63) / 64, ks);
   k_gemm_bf16<<<g2, 128, 0, st>>>(MLP_H, MLP_H, (int)M, dZ, MLP_H, 1, H1, MLP_H, 0, gr + OFF_W2, MLP_H, 1.f, 0.f, ks); ADC_COUNT_LAUNCH();
   // dH1 = dZ2 W2  (M x H)
   k_gemm_bf16<<<g1, 128, 0, st>>>((int)M, MLP_H, MLP_H, dZ, MLP_H, 0, s->W2b, MLP_H, 0, dH, MLP_H, 1.f, 0.f, 1); ADC_COUNT_LAUNCH();
-  k_back_act<<<152 * 4, 256, 0, st>>>(M, dH, Z1, dZ); ADC_COUNT_LAUNCH();               // dZ = dZ1
-  k_colsum_bf16<<<152, MLP_H, 0, st>>>(M, dZ, gr + OFF_B1); ADC_COUNT_LAUNCH();
+  k_back_act<<<c->nsm * 4, 256, 0, st>>>(M, dH, Z1, dZ); ADC_COUNT_LAUNCH();               // dZ = dZ1
+  k_colsum_bf16<<<c->nsm, MLP_H, 0, st>>>(M, dZ, gr + OFF_B1); ADC_COUNT_LAUNCH();
   // dW1 = dZ1^T X  (H x 16, K = M)
   dim3 g3(1, (MLP_H + 63) / 64, ks);
   k_gemm_bf16<<<g3, 128, 0, st>>>(MLP_H, MLP_NIN, (int)M, dZ, MLP_H, 1, X, MLP_NIN, 0, gr + OFF_W1, MLP_NIN, 1.f, 0.f, ks); ADC_COUNT_LAUNCH();
@@ -516,7 +516,7 @@ int mlp_apply(Ctx* c, const MlpPrecond&, int64_t N, int nb, const T* R, const T*
   const size_t smem = apply_smem();
   auto kern = k_mlp_apply<T>;
   ADC_CUDA(c, cudaFuncSetAttribute(kern, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem));
-  kern<<<152, 256, smem, c->stream>>>(to_dev(c->geom), c->d_e, N, nb, R, d_lam, hii, s->W1b, s->W2b, s->p, Tout,
+  kern<<<c->nsm, 256, smem, c->stream>>>(to_dev(c->geom), c->d_e, N, nb, R, d_lam, hii, s->W1b, s->W2b, s->p, Tout,
                                       nullptr); ADC_COUNT_LAUNCH();
   ADC_CUDA(c, cudaGetLastError());
   return ADCGPU_OK;
@@ -628,9 +628,9 @@ extern "C" int adcgpu_mlp_infer(adcgpu_ctx* h, int nb, const double* lam, const 
   const size_t smem = apply_smem();
   ADC_CUDA(c, cudaFuncSetAttribute(k_mlp_apply<double>, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem));
   MlpState* s = state(c);
-  k_mlp_apply<double><<<152, 256, smem, c->stream>>>(to_dev(c->geom), c->d_e, N, nb, dR, dl, c->d_diag, s->W1b,
+  k_mlp_apply<double><<<c->nsm, 256, smem, c->stream>>>(to_dev(c->geom), c->d_e, N, nb, dR, dl, c->d_diag, s->W1b,
                                                      s->W2b, s->p, dT, dm); ADC_COUNT_LAUNCH();
-  k_features<<<152 * 4, 256, 0, c->stream>>>(to_dev(c->geom), c->d_e, N, nb, dl, c->d_diag, dF); ADC_COUNT_LAUNCH();
+  k_features<<<c->nsm * 4, 256, 0, c->stream>>>(to_dev(c->geom), c->d_e, N, nb, dl, c->d_diag, dF); ADC_COUNT_LAUNCH();
   ADC_CUDA(c, cudaGetLastError());
   if (m_out) ADC_CUDA(c, cudaMemcpyAsync(m_out, dm, sizeof(float) * M, cudaMemcpyDeviceToHost, c->stream));
   if (t_out) ADC_CUDA(c, cudaMemcpyAsync(t_out, dT, sizeof(double) * M, cudaMemcpyDeviceToHost, c->stream));

@@ -179,7 +179,7 @@ int fold_impl(Ctx* c, Workspace& ws, int64_t N, int nb, const T* R, int64_t ldr,
   M* HV = X + vec;
   double* sc = reinterpret_cast<double*>(HV + vec);
   cudaStream_t s = c->stream;
-  k_fold_prep<T><<<dim3(152 * 2, nb), 256, 0, s>>>(N, n1, R, ldr, d_lam, hii, Tout, ldt); ADC_COUNT_LAUNCH();
+  k_fold_prep<T><<<dim3(c->nsm * 2, nb), 256, 0, s>>>(N, n1, R, ldr, d_lam, hii, Tout, ldt); ADC_COUNT_LAUNCH();
   ADC_CUDA(c, cudaGetLastError());
   ST(sigma_any(c, nb, Tout, ldt, Z, ldz));
   k_mr_init<T, M><<<nb, MR_THREADS, 0, s>>>(n1, R, ldr, Z, ldz, V, Vold, W, Wold, X, sc); ADC_COUNT_LAUNCH();
@@ -189,7 +189,7 @@ int fold_impl(Ctx* c, Workspace& ws, int64_t N, int nb, const T* R, int64_t ldr,
     k_mr_step<M><<<nb, MR_THREADS, 0, s>>>(n1, d_lam, HV, V, Vold, W, Wold, X, sc); ADC_COUNT_LAUNCH();
     ADC_CUDA(c, cudaGetLastError());
   }
-  k_mr_out<T, M><<<152 * 2, 256, 0, s>>>(n1, nb, X, Tout, ldt); ADC_COUNT_LAUNCH();
+  k_mr_out<T, M><<<c->nsm * 2, 256, 0, s>>>(n1, nb, X, Tout, ldt); ADC_COUNT_LAUNCH();
   ADC_CUDA(c, cudaGetLastError());
   return ADCGPU_OK;
 }

@@ -16,6 +16,7 @@
 // k_singles: W1 = diag1 . V1 + A V1 as a tiled dense product (n1 <= ~5000).
 #include <cuda_bf16.h>
 
+#include <mutex>
 #include <type_traits>
 
 #include "df.h"
@@ -1172,7 +1173,7 @@ int launch_tile(Ctx* c, const GeomDev& g, const SigmaPlan* plan, const TV* Bt, c
   // thread: set it to the device's opt-in maximum, never to this call's size
   ADC_CUDA(c, cudaFuncSetAttribute(kern, cudaFuncAttributeMaxDynamicSharedMemorySize, smem_optin_max(c)));
   ADC_CUDA(c, cudaFuncSetAttribute(kern, cudaFuncAttributePreferredSharedMemoryCarveout, 100));
-  const int grid = std::min(plan->ntitems, 152 * 2);
+  const int grid = std::min(plan->ntitems, c->nsm * 2);
   kern<<<grid, 256, smem, c->stream>>>(g, plan->d_titems, plan->ntitems, Bt, diag, V, ldv, ncols, W, ldw, W1,
                                        ld1); ADC_COUNT_LAUNCH();
   ADC_CUDA(c, cudaGetLastError());
@@ -1186,7 +1187,7 @@ int launch_tile_mma(Ctx* c, const GeomDev& g, const SigmaPlan* plan, const __nv_
   auto kern = k_sigma_tile_mma<TA>;
   ADC_CUDA(c, cudaFuncSetAttribute(kern, cudaFuncAttributeMaxDynamicSharedMemorySize, smem_optin_max(c)));
   ADC_CUDA(c, cudaFuncSetAttribute(kern, cudaFuncAttributePreferredSharedMemoryCarveout, 100));
-  const int grid = std::min(plan->ntitems, 152 * 2);
+  const int grid = std::min(plan->ntitems, c->nsm * 2);
   kern<<<grid, 256, smem, c->stream>>>(g, plan->d_titems, plan->ntitems, Bt, diag, V, ldv, ncols, W, ldw, W1,
                                        ld1); ADC_COUNT_LAUNCH();
   ADC_CUDA(c, cudaGetLastError());
@@ -1197,7 +1198,7 @@ int launch_tile_mma(Ctx* c, const GeomDev& g, const SigmaPlan* plan, const __nv_
 template <typename T, typename TV, typename TA>
 int launch_p2(Ctx* c, const GeomDev& g, const SigmaPlan* plan, int mc, const TV* Bt, const T* V, int64_t ldv,
               T* W, int64_t ldw, TA* W1, int64_t ld1) {
-  const int g2 = std::min(plan->nitems, 152 * 8 * 8) / 8 + 1;
+  const int g2 = std::min(plan->nitems, c->nsm * 8 * 8) / 8 + 1;
   const int gs = g.noP <= 8 ? 1 : (g.noP <= 16 ? 2 : 4);
   cudaStream_t s = c->stream;
 #define P2(MC, GS) \
@@ -1319,8 +1320,8 @@ int sigma_impl(Ctx* c, int m, const T* dV, int64_t ldv, T* dW, int64_t ldw, cons
     int cap = plan->mc_cap[sizeof(T) == 8 ? 0 : 1];
     if (sizeof(T) == 8) cap = std::min(cap, 2);
     const int mc = (left >= 4 && cap >= 4) ? 4 : ((left >= 2 && cap >= 2) ? 2 : 1);
-    const int g1 = std::min(plan->nchunks, 152 * 4 * 16) / 4 + 1;   // 4 warps per block
-    const int g2 = std::min(plan->nitems, 152 * 8 * 8) / 8 + 1;
+    const int g1 = std::min(plan->nchunks, c->nsm * 4 * 16) / 4 + 1;   // 4 warps per block
+    const int g2 = std::min(plan->nitems, c->nsm * 8 * 8) / 8 + 1;
 #define LAUNCH_P2(MC, GS) \
   k_sigma_p2<T, TV, TAcc, MC, GS><<<g2, 256, 0, s>>>(g, items, plan->nitems, Bt, V, ldv, W, ldw, W1, ld1); ADC_COUNT_LAUNCH();
 #define LAUNCH(MC)                                                                                              \
@@ -1433,10 +1434,10 @@ int prepare_mixed(Ctx* c) {
   if (!c->d_diag32 && (st = dmalloc(c, (void**)&c->d_diag32, sizeof(float) * G.N))) return st;
   if (!c->d_Bt16 && (st = dmalloc(c, (void**)&c->d_Bt16, sizeof(uint16_t) * G.off[5]))) return st;
   if (!c->d_Bt32 && (st = dmalloc(c, (void**)&c->d_Bt32, sizeof(float) * G.off[5]))) return st;
-  k_to_f32<<<152 * 8, 256, 0, c->stream>>>(c->d_A, c->d_A32, G.n1 * G.n1); ADC_COUNT_LAUNCH();
-  k_to_f32<<<152 * 8, 256, 0, c->stream>>>(c->d_diag, c->d_diag32, G.N); ADC_COUNT_LAUNCH();
-  k_to_bf16<<<152 * 8, 256, 0, c->stream>>>(c->d_Bt, (__nv_bfloat16*)c->d_Bt16, G.off[5]); ADC_COUNT_LAUNCH();
-  k_to_f32<<<152 * 8, 256, 0, c->stream>>>(c->d_Bt, c->d_Bt32, G.off[5]); ADC_COUNT_LAUNCH();
+  k_to_f32<<<c->nsm * 8, 256, 0, c->stream>>>(c->d_A, c->d_A32, G.n1 * G.n1); ADC_COUNT_LAUNCH();
+  k_to_f32<<<c->nsm * 8, 256, 0, c->stream>>>(c->d_diag, c->d_diag32, G.N); ADC_COUNT_LAUNCH();
+  k_to_bf16<<<c->nsm * 8, 256, 0, c->stream>>>(c->d_Bt, (__nv_bfloat16*)c->d_Bt16, G.off[5]); ADC_COUNT_LAUNCH();
+  k_to_f32<<<c->nsm * 8, 256, 0, c->stream>>>(c->d_Bt, c->d_Bt32, G.off[5]); ADC_COUNT_LAUNCH();
   ADC_CUDA(c, cudaGetLastError());
   return ADCGPU_OK;
 }
@@ -1590,17 +1591,21 @@ namespace {
 
 // Device address of g_noalloc_acc, looked up once per device with that device
 // current (the host-side symbol is only a stand-in, never a device address).
+// std::call_once orders the lookup against every later reader, so host
+// threads that make their first call on a device at the same time are safe.
+constexpr int NOALLOC_MAX_DEVICES = 64;
 double* noalloc_scratch(Ctx* c) {
-  static double* ptrs[64] = {nullptr};
-  if (c->device < 0 || c->device >= 64) return nullptr;
-  if (!ptrs[c->device]) {
+  static std::once_flag once[NOALLOC_MAX_DEVICES];
+  static double* ptrs[NOALLOC_MAX_DEVICES] = {nullptr};
+  if (c->device < 0 || c->device >= NOALLOC_MAX_DEVICES) return nullptr;
+  std::call_once(once[c->device], [c]() {
     void* p = nullptr;
     if (cudaGetSymbolAddress(&p, g_noalloc_acc) != cudaSuccess) {
       cudaGetLastError();
-      return nullptr;
+      return;
     }
     ptrs[c->device] = reinterpret_cast<double*>(p);
-  }
+  });
   return ptrs[c->device];
 }
 
@@ -1632,8 +1637,8 @@ int sigma_fp32_with_acc(Ctx* c, int m, const float* dV, int64_t ldv, float* dW, 
     const int64_t ld1 = (int64_t)n1;
     const int cap = plan->mc_cap[1];
     const int mc = (left >= 4 && cap >= 4) ? 4 : ((left >= 2 && cap >= 2) ? 2 : 1);
-    const int g1 = std::min(plan->nchunks, 152 * 4 * 16) / 4 + 1;
-    const int g2 = std::min(plan->nitems, 152 * 8 * 8) / 8 + 1;
+    const int g1 = std::min(plan->nchunks, c->nsm * 4 * 16) / 4 + 1;
+    const int g2 = std::min(plan->nitems, c->nsm * 8 * 8) / 8 + 1;
 #define NA_P2(MC, GS) \
   k_sigma_p2<T, TV, TAcc, MC, GS><<<g2, 256, 0, s>>>(g, items, plan->nitems, Bt, V, ldv, W, ldw, W1, ld1); ADC_COUNT_LAUNCH();
 #define NA_LAUNCH(MC)                                                                                           \

@@ -26,7 +26,8 @@ typedef std::complex<double> cplx;
 
 namespace {
 
-constexpr int SIL_BLK = 152 * 2;
+// blocks of the reduction passes: two per SM (c: the context in scope)
+#define SIL_BLK (c->nsm * 2)
 
 // per-packet partials: conj(x).y (2 sums) for active packets
 __global__ void k_cdot(int64_t N, int P, const double* __restrict__ X, const double* __restrict__ Y,
@@ -223,7 +224,7 @@ struct SilEngine {
   int minus_i_H(const double* X, double* Y, const std::vector<int>& mask) {
     ST(sigma_fp64(c, 2 * P, X, N, Y, N));
     ST(set_mask(mask));
-    k_minus_i<<<152 * 4, 256, 0, c->stream>>>(N, P, Y, d_mask); ADC_COUNT_LAUNCH();
+    k_minus_i<<<c->nsm * 4, 256, 0, c->stream>>>(N, P, Y, d_mask); ADC_COUNT_LAUNCH();
     ADC_CUDA(c, cudaGetLastError());
     int na = 0;
     for (int v : mask) na += v;
@@ -273,7 +274,7 @@ struct SilEngine {
     for (int p = 0; p < P; ++p) { coef[2 * p] = s[p].real(); coef[2 * p + 1] = s[p].imag(); }
     ADC_CUDA(c, cudaMemcpyAsync(d_coef, coef.data(), sizeof(double) * coef.size(), cudaMemcpyHostToDevice, c->stream));
     ST(set_mask(mask));
-    k_cscale<<<152 * 4, 256, 0, c->stream>>>(N, P, Kn, d_coef, d_mask); ADC_COUNT_LAUNCH();
+    k_cscale<<<c->nsm * 4, 256, 0, c->stream>>>(N, P, Kn, d_coef, d_mask); ADC_COUNT_LAUNCH();
     ADC_CUDA(c, cudaGetLastError());
     return ADCGPU_OK;
   }
@@ -388,7 +389,7 @@ struct SilEngine {
     ADC_CUDA(c, cudaMemcpyAsync(d_coef, coef.data(), sizeof(double) * coef.size(), cudaMemcpyHostToDevice, c->stream));
     ADC_CUDA(c, cudaMemcpyAsync(d_order, ordv.data(), sizeof(int) * P, cudaMemcpyHostToDevice, c->stream));
     ST(set_mask(pmask));
-    k_combine<<<152 * 4, 256, 0, c->stream>>>(N, P, Psi, d_kptr, d_coef, d_order, kdim, d_mask); ADC_COUNT_LAUNCH();
+    k_combine<<<c->nsm * 4, 256, 0, c->stream>>>(N, P, Psi, d_kptr, d_coef, d_order, kdim, d_mask); ADC_COUNT_LAUNCH();
     ADC_CUDA(c, cudaGetLastError());
     (void)maxord;
     return ADCGPU_OK;

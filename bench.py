@@ -37,6 +37,13 @@ sys.path.insert(0, HERE)
 
 NO, NV, SEED, NROOTS, TOL = 16, 180, 7, 20, 1e-6
 METRIC = "time-to-converge 20 roots (mixed+learned vs FP64 GPU) at 1e-6 Ha; matvec GB/s"
+# DRAM bytes moved by the sigma kernels per sigma call, relative to the
+# algorithmic bytes of the call: from ncu (dram__bytes_read.sum +
+# dram__bytes_write.sum of one-kernel captures, profiles/); the solve's mix
+# of calls is assumed to keep the ratio
+TRAFFIC_PER_ALG_BYTE = 1.98
+TRAFFIC_SOURCE = ("ncu DRAM bytes per sigma call at nocc=10/nvirt=110 as a ratio (1.98) of the algorithmic "
+                  "bytes, applied to this workload")
 
 
 def parse():
@@ -146,34 +153,56 @@ def measured_peaks():
 
 
 # ---------------------------------------------------------------------------
-def cpu_sample(no, nv, seed, e, eri, nmult_ref, N_target, nnz_target, threads):
-    """Oracle (CPU restatement of hxvec_incore) timed on a bounded sample:
-    the reference-style COO sigma product of the nocc=10/nvirt=110 matrix,
-    scaled by stored-element count to the bench matrix and multiplied by the
-    number of sigma columns the reference algorithm computes for this solve
-    (block_davidson.f90:855 recomputes all currdim columns per iteration).
-    Dense linear algebra is not included: a lower bound of the CPU solve."""
-    import numpy as np
+CONFIG3_FIXTURE = os.path.join(HERE, "tests", "golden", "config3.json")
 
-    import oracle
-    from adc_ottawa_gb300 import synth_system
 
-    e2, eri2 = synth_system(10, 110, 2024)
-    M = oracle.Matrix.build(10, 110, e2, eri2, nthreads=threads)
-    ncol = max(threads, 1)
-    x = np.random.RandomState(0).rand(M.ndim, ncol)
-    M.matvec(x[:, :1], nthreads=1)
-    t = time.perf_counter()
-    M.matvec(x, nthreads=threads)
-    dt = time.perf_counter() - t
-    per_col = dt / ncol * threads       # single-thread seconds per column
-    per_col_target = per_col * (nnz_target / M.nnz)
-    secs = per_col_target * nmult_ref / threads
-    return {"value": secs, "unit": "s", "cores": threads, "kind": "port",
-            "sample": (f"oracle hxvec_incore (COO, OpenMP over columns) on the nocc=10/nvirt=110 matrix "
-                       f"({M.nnz} elements, {ncol} columns, {dt:.2f} s), scaled by element count to "
-                       f"{nnz_target} and by the reference algorithm's {nmult_ref} sigma columns for this solve; "
-                       f"dense linear algebra excluded (lower bound)")}
+def reference_columns(no, nv):
+    """Sigma columns and iterations of the reference Davidson algorithm on
+    this workload (FP64, DPR, all currdim columns recomputed every iteration,
+    block_davidson.f90:855), recorded by tests/golden/make_config3.py; None
+    when no record exists for these sizes."""
+    if not os.path.exists(CONFIG3_FIXTURE):
+        return None
+    with open(CONFIG3_FIXTURE) as f:
+        d = json.load(f)
+    if (d["nocc"], d["nvirt"], d["seed"]) != (no, nv, SEED) or d["davidson"]["nstates"] != NROOTS:
+        return None
+    return {"nmult_reference": int(d["davidson"]["nmult_reference"]),
+            "iterations": int(d["davidson"]["iterations"]), "source": "tests/golden/config3.json"}
+
+
+class CpuReferenceSigma:
+    """The oracle (CPU restatement of the reference path) on the benchmarked
+    matrix: built by the reference's builder algorithm (get_offdiag_adc2_save_omp,
+    get_matrix.f90:705-1186) on all host cores, then timed on the reference's
+    sigma product hxvec_incore (block_davidson.f90:844-883: OpenMP over
+    columns, every column streams the whole COO matrix).  One sample = one
+    column per host thread.  Only the oracle library is loaded here."""
+
+    def __init__(self, no, nv, threads):
+        import oracle
+
+        self.threads = threads
+        e, eri = oracle.synth_system(no, nv, SEED, threads)
+        t = time.perf_counter()
+        self.M = oracle.Matrix.build(no, nv, e, eri, nthreads=threads)
+        self.build_s = time.perf_counter() - t
+        del eri
+        self.x = oracle.synth_uniform_block(self.M.ndim, threads, 5)
+
+    def sample(self):
+        """Seconds per sigma column, from one hxvec_incore call on one
+        column per thread."""
+        t = time.perf_counter()
+        self.M.matvec(self.x, nthreads=self.threads)
+        dt = time.perf_counter() - t
+        return dt / self.threads, dt
+
+    def describe(self, dt, cols):
+        return (f"oracle hxvec_incore (reference COO sigma, OpenMP over columns) on this workload's matrix "
+                f"({self.M.nnz} stored elements, built on the host in {self.build_s:.1f} s): {self.threads} "
+                f"columns in {dt:.2f} s per sample, scaled by the {cols} sigma columns the reference algorithm "
+                f"computes in this solve; dense linear algebra excluded, so a lower bound")
 
 
 def run_gb300(args):
@@ -229,16 +258,11 @@ def run_gb300(args):
         r64 = g.davdiag_block(NROOTS, TOL, precon=PRECON_DPR, precision=ADCGPU_FP64, want_vectors=False,
                               raise_on_nonconv=False)
         fp64 = {"seconds": time.perf_counter() - t, "iterations": r64.iterations, "status": r64.status,
+                "nmult_reference": r64.nmult_reference,
                 "max_abs_dE_vs_mixed": float(np.abs(r64.evals - r.evals).max())}
     hbm, src = measured_peaks()
     achieved = stats["alg_bytes"] / (stats["ms"] * 1e-3) / 1e9 if stats["ms"] > 0 else 0.0
     per_launch_bytes = stats["alg_bytes"] / max(stats["calls"], 1)
-    # DRAM bytes moved by the sigma kernels per sigma call, relative to the
-    # algorithmic bytes: measured with ncu (dram__bytes_read.sum +
-    # dram__bytes_write.sum of every sigma kernel over the two solves of the
-    # nocc=10/nvirt=110 bench run: 276 GB for ~114 calls of 1.22 GB); the
-    # same solve structure at this size is assumed to keep the ratio
-    TRAFFIC_PER_ALG_BYTE = 1.98
     # e2e through the C ABI with host buffers
     e2e = None
     if not args.no_e2e:
@@ -255,14 +279,23 @@ def run_gb300(args):
         e2e = {"value": allmax(statistics.mean(et), world), "unit": "s",
                "h2d_bytes_per_step": int(e.nbytes + eri.nbytes),
                "d2h_bytes_per_step": int(8 * NROOTS + 8 * NROOTS * g.ndim)}
+    cols_ref = fp64["nmult_reference"] if fp64 else None
+    cols_src = "the FP64 DPR solve of this run (the reference algorithm's iteration structure)"
+    if cols_ref is None:
+        rc = reference_columns(no, nv)
+        cols_ref, cols_src = (rc["nmult_reference"], rc["source"]) if rc else (None, None)
     cpu = None
-    if rank == 0 and world == 1 and not args.no_cpu:
+    if rank == 0 and world == 1 and not args.no_cpu and cols_ref:
         nthr = os.cpu_count() or 1
-        nmult_ref = r.nmult_reference
-        cpu = cpu_sample(no, nv, SEED, e, eri, nmult_ref, g.ndim, nnz, nthr)
+        ref = CpuReferenceSigma(no, nv, nthr)
+        per_col, dt = min(ref.sample() for _ in range(2))
+        cpu = {"value": per_col * cols_ref, "unit": "s", "cores": nthr, "kind": "port",
+               "sample": ref.describe(dt, cols_ref) + f" (column count from {cols_src})",
+               "measured_s_per_column": per_col, "reference_sigma_columns": cols_ref}
+        del ref
     line = {
         "metric": METRIC,
-        "value": t_step * world / world,
+        "value": t_step,
         "unit": "s",
         "n_gpus": world,
         "steps": args.steps,
@@ -273,20 +306,21 @@ def run_gb300(args):
         "vs_baseline": None,
         "dtype": "fp32+bf16 (FP64 Rayleigh-Ritz, residuals, refinement)",
         "data": "synthetic (seeded orbital energies and 8-fold symmetric ERIs)",
-        "config": {"workload": f"ADC(2)-s nocc={no} nvirt={nv} N={g.ndim} davidson {NROOTS} roots tol {TOL}",
-                   "nnz_kept": nnz, "build_s": build_s, "iterations": r.iterations, "nmult": r.nmult,
-                   "phase_iterations_bf16_fp32_fp64": [r.iters_bf16, r.iters_fp32, r.iters_fp64],
-                   "max_residual_fp64": r.max_residual, "sigma_shape": tuned,
-                   "status": r.status, "evals_lowest": r.evals[:5].tolist(),
-                   "l2": "inputs larger than L2 (stored matrix > 3 GB)", "parallelism": f"replicas x{world}",
-                   "preconditioner": "fold: DPR doubles rows, singles block solve of the folded residual",
-                   "fp64_gpu": fp64,
-                   "speedup_vs_fp64_gpu": (fp64["seconds"] / t_step) if fp64 else None},
-        "roofline": {"bound": "hbm", "kernel": "sigma product (k_sigma_p1/p1s + k_sigma_p2 + k_singles), all calls of the timed solves", "achieved": achieved,
+        "config": workload_config(no, nv, g.ndim),
+        "method": "mixed-precision ladder (BF16 -> FP32 -> FP64 refinement) with the folded singles-block "
+                  "preconditioner; the learned (MLP) preconditioner is slower than the fold on this workload "
+                  "family and is timed by --suite learned",
+        "details": {"nnz_kept": nnz, "build_s": build_s, "iterations": r.iterations, "nmult": r.nmult,
+                    "phase_iterations_bf16_fp32_fp64": [r.iters_bf16, r.iters_fp32, r.iters_fp64],
+                    "max_residual_fp64": r.max_residual, "sigma_shape": tuned,
+                    "status": r.status, "evals_lowest": r.evals[:5].tolist(), "parallelism": f"replicas x{world}",
+                    "fp64_gpu": fp64,
+                    "speedup_vs_fp64_gpu": (fp64["seconds"] / t_step) if fp64 else None},
+        "roofline": {"bound": "hbm", "kernel": "sigma product (all sigma kernels of one call), every call of the "
+                     "timed solves", "achieved": achieved,
                      "peak": hbm, "unit": "GB/s", "frac": achieved / hbm,
                      "traffic": per_launch_bytes * TRAFFIC_PER_ALG_BYTE,
-                     "traffic_source": "ncu DRAM bytes per sigma call at nocc=10/nvirt=110 as a ratio (1.98) of the "
-                                       "algorithmic bytes, applied to this workload",
+                     "traffic_source": TRAFFIC_SOURCE,
                      "alg_bytes_per_launch": per_launch_bytes, "launches": stats["calls"],
                      "avg_launch_ms": stats["ms"] / max(stats["calls"], 1), "peak_source": src},
         "clocks": clocks,
@@ -299,40 +333,60 @@ def run_gb300(args):
     g.close()
 
 
+def workload_config(no, nv, ndim):
+    """The workload, identical in both arms."""
+    return {"workload": f"ADC(2)-s nocc={no} nvirt={nv} N={ndim} davidson {NROOTS} roots tol {TOL}",
+            "nocc": no, "nvirt": nv, "seed": SEED, "roots": NROOTS, "tol": TOL,
+            "l2": "inputs larger than L2 (stored matrix > 3 GB)"}
+
+
 def run_reference(args):
+    """The reference algorithm on the host cores: the oracle (the CPU
+    restatement of the reference's Fortran path; the Fortran itself cannot
+    be compiled on these hosts) builds this workload's matrix, and each step
+    times one bounded sample of the reference solve's dominant cost, its
+    sigma product hxvec_incore on one column per host thread.  A step's
+    value is that sample scaled to the whole solve by the reference
+    algorithm's sigma-column count (a lower bound: dense linear algebra
+    excluded).  Only oracle/ is loaded in this process."""
     rank, world, local = dist_env()
     if rank != 0:
         return
-    import numpy as np
+    import oracle
 
-    from adc_ottawa_gb300 import adc2s_dim
-
-    # The reference (Fortran) cannot be built here; the oracle port stands in.
     no, nv = args.nocc, args.nvirt
-    N, _ = adc2s_dim(no, nv)
-    n1 = no * nv
-    pv, po = nv * (nv - 1) // 2, no * (no - 1) // 2
-    nnz = (n1 * (n1 - 1) // 2 + no * nv * (no + nv - 1) + pv * no * (2 * no + nv - 2)
-           + po * nv * (no + 2 * nv - 2) + 2 * po * pv * (2 * no + 2 * nv - 4))
-    # reference sigma columns for a 20-root solve: blocksize 40, maxvec 160;
-    # currdim cycles 40..160 -> about 100 columns per iteration
-    iters = 30
-    nmult_ref = iters * 100
-    times = []
+    N = oracle.adc2s_dim(no, nv)
     threads = os.cpu_count() or 1
+    rc = reference_columns(no, nv)
+    base = {"impl": "reference", "metric": METRIC, "unit": "s", "n_gpus": world, "steps": args.steps,
+            "warmup": args.warmup, "higher_is_better": False, "scaling": "weak", "vs_baseline": None,
+            "dtype": "f64", "data": "synthetic (seeded orbital energies and 8-fold symmetric ERIs)",
+            "config": workload_config(no, nv, N)}
+    if rc is None:
+        base.update({"value": None, "reason": "no recorded sigma-column count of the reference algorithm for "
+                                              "this workload (tests/golden/config3.json)"})
+        print(json.dumps(base), flush=True)
+        return
+    ref = CpuReferenceSigma(no, nv, threads)
+    samples = []
     for k in range(args.warmup + args.steps):
-        s = cpu_sample(no, nv, SEED, None, None, nmult_ref, N, nnz, threads)
+        per_col, dt = ref.sample()
         if k >= args.warmup:
-            times.append(s["value"])
-    v = statistics.mean(times)
-    line = {"impl": "reference", "metric": METRIC,
-            "value": v, "unit": "s", "n_gpus": world, "steps": args.steps, "warmup": args.warmup,
-            "ms_per_step": v * 1e3, "higher_is_better": False, "scaling": "weak", "vs_baseline": None,
-            "dtype": "f64", "data": "synthetic",
-            "config": {"workload": f"ADC(2)-s nocc={no} nvirt={nv} N={N} davidson {NROOTS} roots tol {TOL}"},
-            "cpu_baseline": {"value": v, "unit": "s", "cores": threads, "kind": "port", "sample": s["sample"]},
-            "e2e": {"value": v, "unit": "s", "h2d_bytes_per_step": 0, "d2h_bytes_per_step": 0}}
-    print(json.dumps(line), flush=True)
+            samples.append((per_col, dt))
+    per_col = statistics.mean(p for p, _ in samples)
+    dt = statistics.mean(d for _, d in samples)
+    v = per_col * rc["nmult_reference"]
+    base.update({
+        "value": v, "ms_per_step": v * 1e3,
+        "extrapolation": {"kind": "measured sample scaled to the solve", "measured_s_per_column": per_col,
+                          "measured_s_per_sample": dt, "columns_per_sample": threads,
+                          "reference_sigma_columns": rc["nmult_reference"],
+                          "reference_iterations": rc["iterations"], "column_count_source": rc["source"],
+                          "timed_region_s": dt * args.steps, "host_build_s": ref.build_s},
+        "cpu_baseline": {"value": v, "unit": "s", "cores": threads, "kind": "port",
+                         "sample": ref.describe(dt, rc["nmult_reference"])},
+        "e2e": {"value": v, "unit": "s", "h2d_bytes_per_step": 0, "d2h_bytes_per_step": 0}})
+    print(json.dumps(base), flush=True)
 
 
 def _secondary_line(metric, value, unit, steps, warmup, config, **extra):

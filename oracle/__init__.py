@@ -29,10 +29,11 @@ _i64p = C.POINTER(C.c_int64)
 
 
 def build(force: bool = False) -> str:
-    """Compile oracle.cpp with the committed Makefile (strict IEEE flags)."""
-    src = os.path.join(_HERE, "oracle.cpp")
-    if force or not os.path.exists(_LIB_PATH) or os.path.getmtime(_LIB_PATH) < os.path.getmtime(src):
-        subprocess.run(["make", "-s", "-C", _HERE], check=True)
+    """Compile oracle.cpp and the shared synthetic generator with the
+    committed Makefile (strict IEEE flags; make decides what is stale)."""
+    if force:
+        subprocess.run(["make", "-s", "-C", _HERE, "clean"], check=True)
+    subprocess.run(["make", "-s", "-C", _HERE], check=True)
     return _LIB_PATH
 
 
@@ -69,12 +70,44 @@ def lib():
         L.orc_chebyshev_auto.restype = C.c_int
         L.orc_chebyshev_project.argtypes = [C.c_void_p, _dp, _dp, C.c_int, C.c_double]
         L.orc_chebyshev_project.restype = C.c_int
+        L.orc_synth_orbitals.argtypes = [C.c_int, C.c_int, C.c_uint64, _dp]
+        L.orc_synth_orbitals.restype = C.c_int
+        L.orc_eri_packed_size.argtypes = [C.c_int]
+        L.orc_eri_packed_size.restype = C.c_int64
+        L.orc_synth_eri_packed.argtypes = [C.c_int, C.c_uint64, _dp, C.c_int]
+        L.orc_synth_eri_packed.restype = C.c_int
+        L.orc_synth_uniform_block.argtypes = [C.c_int64, C.c_int, C.c_uint64, _dp]
+        L.orc_synth_uniform_block.restype = C.c_int
+        L.orc_adc2s_dim.argtypes = [C.c_int, C.c_int, _ip]
+        L.orc_adc2s_dim.restype = C.c_int64
         _lib = L
     return _lib
 
 
 def _p(a, t=_dp):
     return a.ctypes.data_as(t)
+
+
+def synth_system(no: int, nv: int, seed: int, nthreads: int = 0):
+    """The seeded synthetic system (orbital energies, packed ERIs) from the
+    generator compiled into the oracle library: the same source and bits as
+    adc_ottawa_gb300.synth_system, without loading the product library."""
+    e = np.empty(no + nv)
+    assert lib().orc_synth_orbitals(no, nv, seed, _p(e)) == 0
+    eri = np.empty(lib().orc_eri_packed_size(no + nv))
+    assert lib().orc_synth_eri_packed(no + nv, seed, _p(eri), nthreads) == 0
+    return e, eri
+
+
+def synth_uniform_block(nrow: int, ncol: int, seed: int) -> np.ndarray:
+    out = np.empty((nrow, ncol), order="F")
+    assert lib().orc_synth_uniform_block(nrow, ncol, seed, _p(out)) == 0
+    return out
+
+
+def adc2s_dim(no: int, nv: int) -> int:
+    cnt = np.zeros(5, np.int32)
+    return int(lib().orc_adc2s_dim(no, nv, _p(cnt, _ip)))
 
 
 def select(no: int, nv: int) -> np.ndarray:

@@ -1,6 +1,7 @@
 """Generate the golden fixtures in tests/golden/ from the oracle.
 
 Run on a CPU host:  python tests/golden/make_golden.py [--config2]
+                    python tests/golden/make_golden.py --config2-solvers
                     python tests/golden/make_golden.py --chebyshev
 
 The fixtures pin (i) the seeded synthetic generator bit for bit across
@@ -87,7 +88,58 @@ def chebyshev_case() -> dict:
             "bounds": bounds, "chebyord": 40, "auto": auto.tolist()}
 
 
+def config2_solvers() -> dict:
+    """Block Lanczos and SIL on the nocc=10/nvirt=110 matrix (seed 2024),
+    the shapes of the nocc=10/nvirt=110 workloads:
+
+    * block Lanczos, b = 10 seeded uniform start vectors (seed 99), 30
+      cycles, orthotype 0 and 1 (run_block_lanczos, block_lanczos.f90
+      :947-1256): the eigenvalues of T and the first-block trace moments
+      tr (T^k)[:b,:b], k = 1..59 (stable under the sign freedom of the QR);
+    * SIL autocorrelation (propagate_sillib, fvecprop.f90:365-564) of the
+      first two of 32 seeded wavepackets (synth_uniform_block seed 77),
+      Krylov dimension 15, tout = 0.1 au (step tout/2 = 0.05 au), 20 outer
+      steps (tfinal = 1.0 au), autotol 1e-8."""
+    no, nv, seed = 10, 110, 2024
+    e, eri = synth_system(no, nv, seed)
+    M = oracle.Matrix.build(no, nv, e, eri)
+    out = {"lanczos": [], "sil": None}
+    b, ncyc = 10, 30
+    q0 = synth_uniform_block(M.ndim, b, 99)
+    for ot in (0, 1):
+        t = time.time()
+        T, ev = M.block_lanczos(q0, ncyc, orthotype=ot)
+        mom, Tk = [], np.eye(T.shape[0])[:, :b]
+        for k in range(1, 2 * ncyc):
+            Tk = T @ Tk
+            mom.append(float(np.trace(Tk[:b])))
+        out["lanczos"].append({"b": b, "ncycles": ncyc, "seed": 99, "orthotype": ot, "evals": ev.tolist(),
+                               "trace_moments": mom})
+        print("lanczos orthotype", ot, time.time() - t, flush=True)
+    f = synth_uniform_block(M.ndim, 32, 77)
+    sil = {"npackets": 32, "seed": 77, "packets": [0, 1], "tout": 0.1, "tfinal": 1.0, "kdim": 15, "tol": 1e-8,
+           "auto_re": [], "auto_im": [], "nmult": []}
+    for p in sil["packets"]:
+        t = time.time()
+        st, a, nm = M.autocorr(f[:, p], sil["tout"], sil["tfinal"], sil["kdim"], sil["tol"])
+        assert st == 0, st
+        sil["auto_re"].append(a.real.tolist())
+        sil["auto_im"].append(a.imag.tolist())
+        sil["nmult"].append(int(nm))
+        print("sil packet", p, time.time() - t, flush=True)
+    out["sil"] = sil
+    return out
+
+
 def main():
+    if "--config2-solvers" in sys.argv:
+        path = os.path.join(HERE, "config2.json")
+        gold = json.load(open(path))
+        gold.update(config2_solvers())
+        with open(path, "w") as f:
+            json.dump(gold, f, indent=1)
+        print("updated config2.json")
+        return
     if "--chebyshev" in sys.argv:
         with open(os.path.join(HERE, "chebyshev.json"), "w") as f:
             json.dump(chebyshev_case(), f, indent=1)

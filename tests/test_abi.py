@@ -75,3 +75,28 @@ def test_ctx_without_gpu_fails_cleanly(built):
         lib().adcgpu_ctx_destroy(h)
     else:
         assert st == 13
+
+
+def test_davidson_file_records(built, tmp_path):
+    """wreigenpairs' davname file (block_davidson.f90:1469-1532): one Fortran
+    unformatted sequential record per root, 4-byte length markers around
+    (int32 i, real8 E_i, real8 x_i(ndim)), i = 1..nstates in the given order.
+    The host-side writer needs no GPU."""
+    from adc_ottawa_gb300 import read_davidson_file, write_davidson_file
+
+    rs = np.random.RandomState(3)
+    ndim, nst = 37, 4
+    ev = np.sort(rs.rand(nst))
+    X = np.asfortranarray(rs.rand(ndim, nst))
+    path = str(tmp_path / "davname")
+    write_davidson_file(path, ev, X)
+    raw = open(path, "rb").read()
+    rec = 4 + 12 + 8 * ndim + 4
+    assert len(raw) == nst * rec
+    for i in range(nst):
+        r = raw[i * rec:(i + 1) * rec]
+        assert np.frombuffer(r[:4], np.int32)[0] == 12 + 8 * ndim == np.frombuffer(r[-4:], np.int32)[0]
+        assert np.frombuffer(r[4:8], np.int32)[0] == i + 1
+    idx, e2, X2 = read_davidson_file(path, ndim)
+    assert np.array_equal(idx, np.arange(1, nst + 1))
+    assert np.array_equal(e2, ev) and np.array_equal(X2, X)

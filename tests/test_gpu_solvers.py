@@ -155,7 +155,8 @@ def test_silstep_single(cfg1):
 @pytest.mark.slow
 def test_davidson_config2_golden(gpu):
     """nocc=10, nvirt=110, 10 roots, tol 1e-8, DPR: eigenvalues within 1e-8 Ha
-    of the oracle's reference-algorithm run (tests/golden/config2.json)."""
+    of the oracle's reference-algorithm run (tests/golden/config2.json), in
+    the same number of iterations and reference sigma columns."""
     import json
     import os
 
@@ -167,6 +168,11 @@ def test_davidson_config2_golden(gpu):
     res = g.davdiag_block(dv["nstates"], dv["tol"], precon=dv["precon"], want_vectors=False)
     assert res.status == 0
     assert np.abs(res.evals - np.array(dv["evals"])).max() < 1e-8
+    # the same iteration structure as the reference algorithm: iterations
+    # and the sum of currdim over them (the columns hxvec_incore recomputes,
+    # block_davidson.f90:855)
+    assert res.iterations == dv["iterations"]
+    assert res.nmult_reference == dv["nmult"]
     g.close()
 
 

@@ -2,7 +2,8 @@
 
 - the band reduction that gives the Lanczos T eigenvalues (dsbev('N') in
   diagmat_banded, block_lanczos.f90:2006-2052) against dense numpy eigvalsh;
-- the dense tred2/tql2 eigensolver against numpy;
+- the dense eigensolver (Householder tridiagonalisation + implicit
+  symmetric QR) against numpy, eigenvectors included;
 - the heapsort that selects the Davidson guess vectors (dsortindxa1,
   initvec_ondiag block_davidson.f90:463-532) against the oracle's
   restatement, including the order of ties.
@@ -65,6 +66,36 @@ def test_dense_eigenvalues(driver, tmp_path):
     A = B + B.T
     w = run(driver, "syev", [120], np.asfortranarray(A), tmp_path, np.float64, 120)
     assert np.abs(w - np.linalg.eigvalsh(A)).max() <= 1e-12 * np.abs(A).max() * 10
+
+
+@pytest.mark.parametrize("n,kind", [(1, "rand"), (2, "rand"), (3, "rand"), (37, "rand"), (160, "rand"),
+                                    (50, "degenerate"), (64, "diagonal"), (40, "graded")])
+def test_dense_eigenvectors(driver, tmp_path, n, kind):
+    """dsyev('V') stand-in: ascending eigenvalues within 1e-12 of numpy and
+    orthonormal eigenvectors with A V = V diag(w), also for repeated
+    eigenvalues, an already diagonal matrix and a widely graded spectrum."""
+    rs = np.random.RandomState(n)
+    if kind == "rand":
+        B = rs.standard_normal((n, n))
+        A = B + B.T
+    elif kind == "degenerate":
+        Q, _ = np.linalg.qr(rs.standard_normal((n, n)))
+        w0 = np.repeat([-1.0, 0.5, 2.0, 7.0, 7.0], n // 5)
+        A = (Q * w0) @ Q.T
+        A = 0.5 * (A + A.T)
+    elif kind == "diagonal":
+        A = np.diag(rs.standard_normal(n))
+    else:
+        Q, _ = np.linalg.qr(rs.standard_normal((n, n)))
+        A = (Q * np.logspace(-8, 4, n)) @ Q.T
+        A = 0.5 * (A + A.T)
+    out = run(driver, "syevv", [n], np.asfortranarray(A), tmp_path, np.float64, n + n * n)
+    w, V = out[:n], out[n:].reshape((n, n), order="F")
+    scale = max(np.abs(A).max(), 1e-300)
+    assert np.all(np.diff(w) >= 0)
+    assert np.abs(w - np.linalg.eigvalsh(A)).max() <= 1e-12 * scale * max(1, n / 10)
+    assert np.abs(V.T @ V - np.eye(n)).max() <= 1e-12 * max(1, n / 10)
+    assert np.abs(A @ V - V * w).max() <= 1e-12 * scale * max(1, n / 10)
 
 
 @pytest.mark.parametrize("n", [1, 6, 1000, 65537])
