@@ -31,6 +31,7 @@ SOURCES = [
     ("context.cu", []),
     ("build_kernels.cu", ["--fmad=false"]),
     ("sigma.cu", []),
+    ("sigma_umma.cu", []),
     ("dense.cu", []),
     ("precond_fold.cu", []),
     ("davidson.cu", []),

@@ -330,6 +330,9 @@ struct SigmaPlan {
   int ntitems = 0;
   void* d_acc = nullptr;      // FP64 accumulator of the singles rows (FP32 path)
   size_t acc_bytes = 0;
+  void* umma = nullptr;       // tensor-core pass plan (sigma_umma.cu), built on first use
+  int umma_item_rows = 4096;  // rows per tensor-core work item (autotuned)
+  int umma_off = 0;           // 1: the tensor-core pass is not used
 };
 int prepare_desc(Ctx* c);
 int build_chunks(Ctx* c, int chunk);
@@ -338,6 +341,15 @@ int sigma_fp64(Ctx* c, int m, const double* dV, int64_t ldv, double* dW, int64_t
 int sigma_fp32(Ctx* c, int m, const float* dV, int64_t ldv, float* dW, int64_t ldw);
 int prepare_mixed(Ctx* c);
 void free_mlp(Ctx* c);
+
+// sigma_umma.cu : the tensor-core (tcgen05) pass of the BF16 sigma product
+bool umma_supported(const Ctx* c);
+int umma_prepare(Ctx* c, void*& handle, int item_rows);
+void umma_free(Ctx* c, void*& handle);
+int umma_launch(Ctx* c, void* handle, const float* V, int64_t ldv, int m, float* W, int64_t ldw, double* W1,
+                int64_t ld1);
+int umma_runs(void* handle, const int2** runs, int* nruns);
+int umma_check(Ctx* c, void* handle);
 
 // hostla.cpp : dense host linear algebra (FP64)
 // Symmetric eigen-decomposition (Householder tridiagonalisation + implicit QL).

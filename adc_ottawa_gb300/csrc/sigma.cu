@@ -500,6 +500,76 @@ __global__ void __launch_bounds__(256) k_sigma_p2(GeomDev g, const int2* __restr
   }
 }
 
+// Pass 3: the W1 part of segment A, W1[(a', k), c] += sum over the rows of
+// (a', b') of A[row, k] V2[row, c], for the tensor-core pass (which does the
+// W2 part of segment A itself).  One warp per run of rows with equal a' in
+// one slab (contiguous in storage: item = (first row, row count)).  Lanes
+// form groups of GS (>= noP/8 chunks of segment A); 32/GS rows per step; the
+// sums reduce across groups at the end, one atomic per (single, column).
+template <typename TV, int MC, int GS>
+__global__ void __launch_bounds__(256) k_sigma_p3(GeomDev g, const int2* __restrict__ runs, int nruns,
+                                                  const TV* __restrict__ Bt, const float* __restrict__ V,
+                                                  int64_t ldv, double* __restrict__ W1, int64_t ld1) {
+  const int lane = threadIdx.x & 31;
+  const int warp = (blockIdx.x * blockDim.x + threadIdx.x) >> 5;
+  const int nwarps = (gridDim.x * blockDim.x) >> 5;
+  const int no = g.no;
+  const int64_t n1 = g.n1;
+  const int nA = g.noP / 8;
+  const int slot = lane / GS, h = lane % GS;
+  constexpr int RPS = 32 / GS;
+  for (int it = warp; it < nruns; it += nwarps) {
+    const int2 run = runs[it];
+    const Double r0 = decode_row(g, run.x);
+    const int cls = r0.cls, ap = r0.ap;
+    const bool twoa = (cls == 1 || cls >= 3);
+    const int64_t L = g.len[cls];
+    const bool act = h < nA;
+    float ya[8][MC];
+#pragma unroll
+    for (int u = 0; u < 8; ++u)
+#pragma unroll
+      for (int c = 0; c < MC; ++c) ya[u][c] = 0.f;
+    for (int r = slot; r < run.y; r += RPS) {
+      const int64_t row = run.x + r;
+      // rows of one run: (a', a' + 1 + r) for a' < b' classes, (a', a') otherwise
+      const Double rr{ap, twoa ? ap + 1 + r : ap, r0.kp, r0.lp, cls};
+      const int64_t d = row_to_d(g, rr, row);
+      float v[8];
+      if (act) Load8<float, TV>::go(Bt + g.off[cls] + (row - g.start[cls]) * L + 8 * h, v);
+      else {
+#pragma unroll
+        for (int u = 0; u < 8; ++u) v[u] = 0.f;
+      }
+#pragma unroll
+      for (int c = 0; c < MC; ++c) {
+        const float x2 = V[(int64_t)c * ldv + n1 + d];
+#pragma unroll
+        for (int u = 0; u < 8; ++u) ya[u][c] += v[u] * x2;
+      }
+    }
+#pragma unroll
+    for (int u = 0; u < 8; ++u)
+#pragma unroll
+      for (int c = 0; c < MC; ++c) {
+        float y = ya[u][c];
+#pragma unroll
+        for (int o = GS; o < 32; o <<= 1) y += __shfl_xor_sync(0xffffffffu, y, o);
+        ya[u][c] = y;
+      }
+    if (slot == 0 && act) {
+#pragma unroll
+      for (int u = 0; u < 8; ++u) {
+        const int kk = 8 * h + u;
+        if (kk >= no) continue;
+#pragma unroll
+        for (int c = 0; c < MC; ++c)
+          if (ya[u][c] != 0.f) atomicAdd(&W1[(int64_t)c * ld1 + (int64_t)ap * no + kk], (double)ya[u][c]);
+      }
+    }
+  }
+}
+
 // Arithmetic of the tiled pass 1.  Native: values, vectors and sums in T.
 // DF (FP64 inputs only): the C|D values and the vectors are held in shared
 // memory as double-float pairs and multiplied on the FP32 pipe (df.h), and so
@@ -1220,6 +1290,24 @@ int launch_p2(Ctx* c, const GeomDev& g, const SigmaPlan* plan, int mc, const TV*
   return ADCGPU_OK;
 }
 
+// pass 3 (segment A's W1 part, after the tensor-core pass) for mc <= 8 columns
+template <typename TV>
+int launch_p3(Ctx* c, const GeomDev& g, const int2* runs, int nruns, int mc, const TV* Bt, const float* V,
+              int64_t ldv, double* W1, int64_t ld1) {
+  const int g3 = std::min(nruns, c->nsm * 8 * 8) / 8 + 1;
+  const int gs = g.noP <= 8 ? 1 : (g.noP <= 16 ? 2 : 4);
+  cudaStream_t s = c->stream;
+#define P3(MC, GS) k_sigma_p3<TV, MC, GS><<<g3, 256, 0, s>>>(g, runs, nruns, Bt, V, ldv, W1, ld1)
+  if (mc == 8) { if (gs == 1) P3(8, 1); else if (gs == 2) P3(8, 2); else P3(8, 4); }
+  else if (mc == 4) { if (gs == 1) P3(4, 1); else if (gs == 2) P3(4, 2); else P3(4, 4); }
+  else if (mc == 2) { if (gs == 1) P3(2, 1); else if (gs == 2) P3(2, 2); else P3(2, 4); }
+  else { if (gs == 1) P3(1, 1); else if (gs == 2) P3(1, 2); else P3(1, 4); }
+#undef P3
+  ADC_COUNT_LAUNCH();
+  ADC_CUDA(c, cudaGetLastError());
+  return ADCGPU_OK;
+}
+
 template <typename T, typename TV>
 int sigma_impl(Ctx* c, int m, const T* dV, int64_t ldv, T* dW, int64_t ldw, const T* A, const T* diag,
                const TV* Bt) {
@@ -1270,6 +1358,38 @@ int sigma_impl(Ctx* c, int m, const T* dV, int64_t ldv, T* dW, int64_t ldw, cons
   // pass 1 is faster
   const bool tiled = plan->tiled && plan->d_titems && mt_fit > 0 && m >= 16;
   int c0 = 0;
+  bool umma_used = false;
+  if constexpr (std::is_same<TV, __nv_bfloat16>::value) {
+    // tensor-core pass (tcgen05, sigma_umma.cu) for the C|D segments and the
+    // W2 part of segment A, then segment B (pass 2) and the W1 part of
+    // segment A (pass 3), up to 48 columns per matrix pass
+    if (plan->tiled == 1 && !plan->umma_off && umma_supported(c)) {
+      ST(umma_prepare(c, plan->umma, plan->umma_item_rows));
+      const int2* runs = nullptr;
+      int nruns = 0;
+      ST(umma_runs(plan->umma, &runs, &nruns));
+      for (; c0 < m;) {
+        const int nc = std::min(m - c0, 48);
+        const T* V = dV + (int64_t)c0 * ldv;
+        T* W = dW + (int64_t)c0 * ldw;
+        TAcc* W1 = W1base + (int64_t)c0 * n1;
+        ST(umma_launch(c, plan->umma, V, ldv, nc, W, ldw, W1, n1));
+        for (int b0 = 0; plan->nitems && b0 < nc;) {
+          const int lb = nc - b0, mc = lb >= 8 ? 8 : (lb >= 4 ? 4 : (lb >= 2 ? 2 : 1));
+          ST((launch_p2<T, TV, TAcc>(c, g, plan, mc, Bt, V + (int64_t)b0 * ldv, ldv, W + (int64_t)b0 * ldw, ldw,
+                                     W1 + (int64_t)b0 * n1, n1)));
+          b0 += mc;
+        }
+        for (int b0 = 0; b0 < nc;) {
+          const int lb = nc - b0, mc = lb >= 8 ? 8 : (lb >= 4 ? 4 : (lb >= 2 ? 2 : 1));
+          ST((launch_p3<TV>(c, g, runs, nruns, mc, Bt, V + (int64_t)b0 * ldv, ldv, W1 + (int64_t)b0 * n1, n1)));
+          b0 += mc;
+        }
+        c0 += nc;
+      }
+      umma_used = true;
+    }
+  }
   while (tiled && c0 < m) {
     const int left = m - c0;
     const int mt = left > 8 && mt_fit >= 16 ? 16 : 8;
@@ -1348,6 +1468,7 @@ int sigma_impl(Ctx* c, int m, const T* dV, int64_t ldv, T* dW, int64_t ldw, cons
                                                        reinterpret_cast<float*>(dW), ldw); ADC_COUNT_LAUNCH();
   }
   ADC_CUDA(c, cudaEventRecord(c->st_ev1, s));
+  if (umma_used) ST(umma_check(c, plan->umma));
   c->st_pending = true;
   c->st_pending_cols = m;
   // algorithmic bytes of one sparse product of m columns, counted as for a
@@ -1423,6 +1544,7 @@ void free_sigma_plan(Ctx* c) {
   dfree(c, plan->d_items);
   dfree(c, plan->d_titems);
   dfree(c, plan->d_acc);
+  umma_free(c, plan->umma);
   delete plan;
   c->sigma_plan = nullptr;
 }
@@ -1529,6 +1651,7 @@ extern "C" int adcgpu_sigma_set_shape(adcgpu_ctx* h, int chunk, int mc_fp64, int
   SigmaPlan* plan = reinterpret_cast<SigmaPlan*>(c->sigma_plan);
   plan->staged = ((mc_fp64 | mc_fp32) & 8) ? 1 : 0;
   plan->tiled = ((mc_fp64 | mc_fp32) & 16) ? 0 : (((mc_fp64 | mc_fp32) & 32) ? 2 : 1);
+  plan->umma_off = ((mc_fp64 | mc_fp32) & 64) ? 1 : 0;
   plan->mc_cap[0] = std::min(mc_fp64 & 7, 2);
   plan->mc_cap[1] = std::min(mc_fp32 & 7, 4);
   return build_chunks(c, chunk);
