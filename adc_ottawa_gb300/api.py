@@ -26,6 +26,7 @@ from ._native import DavInfo, DavParams, SilState, lib, ptr
 
 ADCGPU_FP64 = 0
 ADCGPU_MIXED = 1
+ADCGPU_DIRECT = 2   # FP64, coupling block recomputed in every sigma product (the matvec path)
 PRECON_DPR, PRECON_OLSEN, PRECON_MLP, PRECON_FOLD = 1, 2, 3, 4
 
 STATUS = {
@@ -227,9 +228,12 @@ class AdcGpu:
                       precon: int = PRECON_DPR, ldfl: bool = True, lsubdiag: bool = False, guessdim: int = 800,
                       precision: int = ADCGPU_FP64, refine: int = 0, tol_bf16: float = 0.0,
                       tol_fp32: float = 0.0, want_vectors: bool = True,
-                      raise_on_nonconv: bool = True, refine_block: int = 0) -> DavidsonResult:
+                      raise_on_nonconv: bool = True, refine_block: int = 0,
+                      ladc1guess: bool = False) -> DavidsonResult:
+        """ladc1guess: initvec_adc1 (the ADC(1) eigenvectors) as the guess,
+        ahead of lsubdiag, as davdiag_block's lrdadc1 (block_davidson.f90:94-117)."""
         p = DavParams(davstates=davstates, dmain=dmain, maxsubdim=maxsubdim, maxiter=maxiter, precon=precon,
-                      ldfl=int(ldfl), lsubdiag=int(lsubdiag), guessdim=guessdim, davtol=davtol,
+                      ldfl=int(ldfl), lsubdiag=2 if ladc1guess else int(lsubdiag), guessdim=guessdim, davtol=davtol,
                       precision=precision, refine=refine, tol_bf16=tol_bf16, tol_fp32=tol_fp32,
                       refine_block=refine_block)
         ev = np.empty(davstates)

@@ -115,10 +115,68 @@ __global__ void k_cb(Eri E, const double* __restrict__ e, double* __restrict__ c
   cb[k1 * no + k] = x;
 }
 
+// The direct path's intermediates (get_interm_adc2_save, get_matrix.f90
+// :625-701): Ca1_ph_ph(a,a1) (adc_ph.f90:98-152) for a <= a1 and
+// Cb1_ph_ph(k,k1) (:158-211) for k <= k1, in the reference's operation order.
+__global__ void k_ca1(Eri E, const double* __restrict__ e, double* __restrict__ ca) {
+  const int no = E.no, nv = E.nv;
+  int64_t t = blockIdx.x * (int64_t)blockDim.x + threadIdx.x;
+  if (t >= (int64_t)nv * nv) return;
+  int a = (int)(t / nv), a1 = (int)(t % nv);
+  if (a > a1) return;
+  const double ea = e[no + a], ea1 = e[no + a1];
+  double acc = 0.0;
+  for (int r = 0; r < nv; ++r)
+    for (int u = 0; u < no; ++u)
+      for (int v = 0; v < no; ++v) {
+        const double er = e[no + r];
+        double eija = er + ea - e[u] - e[v];
+        double eijc = er + ea1 - e[u] - e[v];
+        double DA = 1.0 / ((er + ea - e[u] - e[v]) * (er + ea1 - e[u] - e[v]));
+        double term = 0.0;
+        term = term + eijc * E.VOVO(a1, u, r, v) * (2.0 * E.VOVO(a, u, r, v) - E.VOVO(r, u, a, v));
+        term = term + eija * E.VOVO(a, v, r, u) * (2.0 * E.VOVO(r, u, a1, v) - E.VOVO(a1, u, r, v));
+        term = DA * term;
+        acc = acc + term;
+      }
+  double x = 0.5 * acc;
+  ca[(int64_t)a * nv + a1] = x;
+  ca[(int64_t)a1 * nv + a] = x;
+}
+
+__global__ void k_cb1(Eri E, const double* __restrict__ e, double* __restrict__ cb) {
+  const int no = E.no, nv = E.nv;
+  int t = blockIdx.x * blockDim.x + threadIdx.x;
+  if (t >= no * no) return;
+  int k = t / no, k1 = t % no;
+  if (k > k1) return;
+  const double ek = e[k], ek1 = e[k1];
+  double acc = 0.0;
+  for (int r = 0; r < nv; ++r)
+    for (int s = 0; s < nv; ++s)
+      for (int u = 0; u < no; ++u) {
+        const double er = e[no + r], es = e[no + s];
+        double eicd = er + es - e[u] - ek;
+        double ejcd = er + es - e[u] - ek1;
+        double DB = 1.0 / ((er + es - e[u] - ek) * (er + es - e[u] - ek1));
+        double term = 0.0;
+        term = term + ejcd * E.VOVO(r, k1, s, u) * (2.0 * E.VOVO(r, k, s, u) - E.VOVO(s, k, r, u));
+        term = term + eicd * E.VOVO(r, u, s, k) * (2.0 * E.VOVO(s, k1, r, u) - E.VOVO(r, k1, s, u));
+        term = DB * term;
+        acc = acc + term;
+      }
+  double x = 0.5 * acc;
+  cb[k * no + k1] = x;
+  cb[k1 * no + k] = x;
+}
+
 // Per (single, (c,i)) tables for CC_ph_ph (adc_ph.f90:918-957):
 //   X[s][t]  = 2 (a k|c i) - (a i|c k)       the first factor of term
 //   D1[s][t] = e(k) - e(a) + (e(i) - e(c))   one factor of the DC denominator
 // with t = c*no + i (c outer, i inner: the reference's loop order).
+// DIRECT: D1[s][t] = 1 / (e(c) + e(a) - e(i) - e(k)), the DC factor of
+// Cc1_ph_ph / Cc2_ph_ph (adc_ph.f90:214-303) for the single s = (a,k).
+template <bool DIRECT>
 __global__ void k_cc_tables(Eri E, const double* __restrict__ e, double* __restrict__ X,
                             double* __restrict__ D1) {
   const int no = E.no, nv = E.nv;
@@ -129,8 +187,12 @@ __global__ void k_cc_tables(Eri E, const double* __restrict__ e, double* __restr
     int a = (int)(s / no), k = (int)(s % no);
     int c = (int)(t / no), i = (int)(t % no);
     X[idx] = 2.0 * E.VOVO(a, k, c, i) - E.VOVO(a, i, c, k);
-    double eic = e[i] - e[no + c];
-    D1[idx] = e[k] - e[no + a] + eic;
+    if (DIRECT) {
+      D1[idx] = 1.0 / (e[no + c] + e[no + a] - e[i] - e[k]);
+    } else {
+      double eic = e[i] - e[no + c];
+      D1[idx] = e[k] - e[no + a] + eic;
+    }
   }
 }
 
@@ -139,6 +201,10 @@ constexpr int TK = 32;   // t-chunk staged in shared memory
 
 // ph-ph block (get_matrix.f90:848-884) and singles diagonal (:286-294).
 // Each thread evaluates one element (s1 <= s2) with the exact serial CC sum.
+// DIRECT: the direct path's ph-ph block (dmatvec_davidson.f90:1100-1107)
+// and singles diagonal (hiivec :917-924): Ca1/Cb1 intermediates and the two
+// serial sums Cc1_ph_ph and Cc2_ph_ph instead of CC_ph_ph.
+template <bool DIRECT>
 __global__ void __launch_bounds__(PT * PT) k_phph(Eri E, const double* __restrict__ e,
                                                   const double* __restrict__ X, const double* __restrict__ D1,
                                                   const double* __restrict__ ca, const double* __restrict__ cb,
@@ -157,7 +223,7 @@ __global__ void __launch_bounds__(PT * PT) k_phph(Eri E, const double* __restric
     int a = s1 / no, k = s1 % no, a1 = s2 / no, k1 = s2 % no;
     hv = 0.5 * (e[k] + e[k1] - e[no + a] - e[no + a1]);
   }
-  double cc = 0.0;
+  double cc = 0.0, cc2 = 0.0;
   for (int t0 = 0; t0 < nt; t0 += TK) {
     __syncthreads();
     for (int l = tid; l < PT * TK; l += PT * PT) {
@@ -176,11 +242,19 @@ __global__ void __launch_bounds__(PT * PT) k_phph(Eri E, const double* __restric
     }
     __syncthreads();
     const int tl = min(TK, nt - t0);
-    for (int c = 0; c < tl; ++c) {
-      double DC = (hv + sEic[c]) / (sD1[ty][c] * sD2[tx][c]);
-      double term = sX1[ty][c] * sX2[tx][c];
-      term = term * DC;
-      cc = cc + term;
+    if (DIRECT) {
+      for (int c = 0; c < tl; ++c) {
+        const double term = sX1[ty][c] * sX2[tx][c];
+        cc = cc + term * sD1[ty][c];     // Cc1: DC of (a, k)
+        cc2 = cc2 + term * sD2[tx][c];   // Cc2: DC of (a1, k1)
+      }
+    } else {
+      for (int c = 0; c < tl; ++c) {
+        double DC = (hv + sEic[c]) / (sD1[ty][c] * sD2[tx][c]);
+        double term = sX1[ty][c] * sX2[tx][c];
+        term = term * DC;
+        cc = cc + term;
+      }
     }
   }
   if (s1 >= n1 || s2 >= n1 || s2 < s1) return;
@@ -188,9 +262,14 @@ __global__ void __launch_bounds__(PT * PT) k_phph(Eri E, const double* __restric
   if (s1 == s2) {
     double x = e[no + a] - e[k];                                   // K_ph_ph
     x = x + (2.0 * E.VOVO(a, k, a, k) - E.VVOO(a, a, k, k));       // C1_ph_ph
-    x = x + ca[(int64_t)a * nv + a];                               // CA_ph_ph(a,a)
-    x = x + cb[k * no + k];                                        // CB_ph_ph(k,k)
-    x = x + cc;                                                    // CC_ph_ph
+    x = x + ca[(int64_t)a * nv + a];                               // CA (Ca1)(a,a)
+    x = x + cb[k * no + k];                                        // CB (Cb1)(k,k)
+    if (DIRECT) {
+      x = x + -0.5 * cc;                                           // Cc1_ph_ph
+      x = x + -0.5 * cc2;                                          // Cc2_ph_ph
+    } else {
+      x = x + cc;                                                  // CC_ph_ph
+    }
     hii[s1] = x;
     A[(int64_t)s1 * n1 + s1] = 0.0;
     return;
@@ -198,11 +277,33 @@ __global__ void __launch_bounds__(PT * PT) k_phph(Eri E, const double* __restric
   double x = 2.0 * E.VOVO(a, k, a1, k1) - E.VVOO(a, a1, k, k1);  // C1_ph_ph
   if (k == k1) x = x + ca[(int64_t)a * nv + a1];
   if (a == a1) x = x + cb[k * no + k1];
-  x = x + cc;
+  if (DIRECT) {
+    x = x + -0.5 * cc;
+    x = x + -0.5 * cc2;
+  } else {
+    x = x + cc;
+  }
   double keep = fabs(x) > MINC ? x : 0.0;
   A[(int64_t)s1 * n1 + s2] = keep;
   A[(int64_t)s2 * n1 + s1] = keep;
   if (keep != 0.0) atomicAdd(kept, 1ull);
+}
+
+// ADC(1) (TDA) matrix of the singles, dense n1 x n1: get_diag_tda_direct
+// (K_ph_ph + C1_ph_ph(a,k,a,k)) and get_offdiag_tda_direct (C1_ph_ph), the
+// matrix whose eigenvectors adc1_guessvecs writes for initvec_adc1
+// (get_matrix.f90:17-82, guessvecs.f90:9-84).
+__global__ void k_tda(Eri E, const double* __restrict__ e, double* __restrict__ M) {
+  const int no = E.no, nv = E.nv;
+  const int64_t n1 = (int64_t)no * nv;
+  for (int64_t t = blockIdx.x * (int64_t)blockDim.x + threadIdx.x; t < n1 * n1;
+       t += (int64_t)gridDim.x * blockDim.x) {
+    const int64_t s1 = t / n1, s2 = t % n1;
+    const int a = (int)(s1 / no), k = (int)(s1 % no), a1 = (int)(s2 / no), k1 = (int)(s2 % no);
+    double x = 2.0 * E.VOVO(a, k, a1, k1) - E.VVOO(a, a1, k, k1);   // C1_ph_ph
+    if (s1 == s2) x = (e[no + a] - e[k]) + x;                        // K_ph_ph + C1_ph_ph
+    M[t] = x;
+  }
 }
 
 // 2p2h diagonal K_2p2h_2p2h (get_matrix.f90:303-306, adc_ph.f90:1090-1096).
@@ -253,14 +354,18 @@ __device__ inline double coupling(const Eri& E, int a, int k, const Double& r) {
 // One warp per stored row of B^T: evaluates its structural entries, applies
 // the minc threshold (get_matrix.f90:904 etc.), zeroes the padding and counts
 // the kept entries.
-__global__ void k_coupling(Eri E, GeomDev g, double* __restrict__ Bt, int64_t* __restrict__ rowcount) {
+// Rows [row_begin, row_end) of the store; Bt holds the values from the
+// value offset vbase on (the whole store: vbase = 0; one chunk of the direct
+// path: vbase = the chunk's first value).  rowcount may be null.
+__global__ void k_coupling(Eri E, GeomDev g, double* __restrict__ Bt, int64_t vbase, int64_t row_begin,
+                           int64_t row_end, int64_t* __restrict__ rowcount) {
   const int lane = threadIdx.x & 31;
   const int64_t warp = (blockIdx.x * (int64_t)blockDim.x + threadIdx.x) >> 5;
   const int64_t nwarps = ((int64_t)gridDim.x * blockDim.x) >> 5;
-  for (int64_t row_i = warp; row_i < g.n2; row_i += nwarps) {
+  for (int64_t row_i = row_begin + warp; row_i < row_end; row_i += nwarps) {
     Double r = decode_row(g, row_i);
     const int64_t L = g.len[r.cls];
-    double* row = Bt + g.off[r.cls] + (row_i - g.start[r.cls]) * L;
+    double* row = Bt + (g.off[r.cls] + (row_i - g.start[r.cls]) * L - vbase);
     int cnt = 0;
     for (int e = lane; e < L; e += 32) {
       int64_t s = entry_single(g, r, e);
@@ -274,7 +379,7 @@ __global__ void k_coupling(Eri E, GeomDev g, double* __restrict__ Bt, int64_t* _
       cnt += keep;
     }
     for (int o = 16; o; o >>= 1) cnt += __shfl_xor_sync(0xffffffffu, cnt, o);
-    if (lane == 0) rowcount[row_i] = cnt;
+    if (lane == 0 && rowcount) rowcount[row_i] = cnt;
   }
 }
 
@@ -370,6 +475,22 @@ int build_eri_blocks_from_packed(Ctx* c, const double* d_packed) {
   return ADCGPU_OK;
 }
 
+int build_adc1_matrix(Ctx* c, double* d_M) {
+  if (!c->d_vovo || !c->d_vvoo) return set_err(c, ADCGPU_NO_MATRIX, "ADC(1) matrix: integrals missing");
+  Eri E{c->d_vovo, c->d_vvoo, c->d_ooov, c->d_vvov, c->geom.no, c->geom.nv};
+  k_tda<<<grid_for(c, c->geom.n1 * c->geom.n1, 256), 256, 0, c->stream>>>(E, c->d_e, d_M); ADC_COUNT_LAUNCH();
+  ADC_CUDA(c, cudaGetLastError());
+  return ADCGPU_OK;
+}
+
+int coupling_values(Ctx* c, double* buf, int64_t vbase, int64_t row0, int64_t row1, int64_t* rowcount) {
+  Eri E{c->d_vovo, c->d_vvoo, c->d_ooov, c->d_vvov, c->geom.no, c->geom.nv};
+  k_coupling<<<c->nsm * 8, 256, 0, c->stream>>>(E, to_dev(c->geom), buf, vbase, row0, row1, rowcount);
+  ADC_COUNT_LAUNCH();
+  ADC_CUDA(c, cudaGetLastError());
+  return ADCGPU_OK;
+}
+
 int build_matrix(Ctx* c) {
   const Geometry& G = c->geom;
   const int no = G.no, nv = G.nv;
@@ -388,19 +509,43 @@ int build_matrix(Ctx* c) {
   ADC_CUDA(c, cudaMemsetAsync(d_kept, 0, sizeof(unsigned long long), s));
   if (!c->d_diag && (st = dmalloc(c, (void**)&c->d_diag, sizeof(double) * G.N))) return st;
   if (!c->d_A && (st = dmalloc(c, (void**)&c->d_A, sizeof(double) * n1 * n1))) return st;
-  if (!c->d_Bt && (st = dmalloc(c, (void**)&c->d_Bt, sizeof(double) * G.off[5]))) return st;
+  // the stored path keeps all of B^T; the direct path one chunk at a time
+  int64_t bt_values = G.off[5];
+  if (c->direct) {
+    c->dchunks = direct_chunk_rows(G, direct_budget(G));
+    bt_values = 0;
+    for (const DirectChunk& dc : c->dchunks) bt_values = std::max(bt_values, dc.vlen);
+  }
+  if (!c->d_Bt && (st = dmalloc(c, (void**)&c->d_Bt, sizeof(double) * bt_values))) return st;
   if (!c->d_rowcount && (st = dmalloc(c, (void**)&c->d_rowcount, sizeof(int64_t) * (G.n2 + n1 + 1))))
     return st;
 
-  k_ca<<<(int)((nv * (int64_t)nv + 127) / 128), 128, 0, s>>>(E, c->d_e, d_ca); ADC_COUNT_LAUNCH();
-  k_cb<<<(no * no + 63) / 64, 64, 0, s>>>(E, c->d_e, d_cb); ADC_COUNT_LAUNCH();
-  k_cc_tables<<<grid_for(c, n1 * n1, 256), 256, 0, s>>>(E, c->d_e, d_X, d_D1); ADC_COUNT_LAUNCH();
-  ADC_CUDA(c, cudaGetLastError());
   dim3 tiles((unsigned)((n1 + PT - 1) / PT), (unsigned)((n1 + PT - 1) / PT));
-  k_phph<<<tiles, dim3(PT, PT), 0, s>>>(E, c->d_e, d_X, d_D1, d_ca, d_cb, c->d_A, c->d_diag, d_kept); ADC_COUNT_LAUNCH();
+  if (c->direct) {
+    // the direct path's formulas (get_interm_adc2_save, hiivec, get_matvec_adc2s_omp)
+    k_ca1<<<(int)((nv * (int64_t)nv + 127) / 128), 128, 0, s>>>(E, c->d_e, d_ca); ADC_COUNT_LAUNCH();
+    k_cb1<<<(no * no + 63) / 64, 64, 0, s>>>(E, c->d_e, d_cb); ADC_COUNT_LAUNCH();
+    k_cc_tables<true><<<grid_for(c, n1 * n1, 256), 256, 0, s>>>(E, c->d_e, d_X, d_D1); ADC_COUNT_LAUNCH();
+    ADC_CUDA(c, cudaGetLastError());
+    k_phph<true><<<tiles, dim3(PT, PT), 0, s>>>(E, c->d_e, d_X, d_D1, d_ca, d_cb, c->d_A, c->d_diag, d_kept);
+    ADC_COUNT_LAUNCH();
+  } else {
+    k_ca<<<(int)((nv * (int64_t)nv + 127) / 128), 128, 0, s>>>(E, c->d_e, d_ca); ADC_COUNT_LAUNCH();
+    k_cb<<<(no * no + 63) / 64, 64, 0, s>>>(E, c->d_e, d_cb); ADC_COUNT_LAUNCH();
+    k_cc_tables<false><<<grid_for(c, n1 * n1, 256), 256, 0, s>>>(E, c->d_e, d_X, d_D1); ADC_COUNT_LAUNCH();
+    ADC_CUDA(c, cudaGetLastError());
+    k_phph<false><<<tiles, dim3(PT, PT), 0, s>>>(E, c->d_e, d_X, d_D1, d_ca, d_cb, c->d_A, c->d_diag, d_kept);
+    ADC_COUNT_LAUNCH();
+  }
   ADC_CUDA(c, cudaGetLastError());
   k_diag2<<<grid_for(c, G.n2, 256), 256, 0, s>>>(g, c->d_e, c->d_diag); ADC_COUNT_LAUNCH();
-  k_coupling<<<c->nsm * 8, 256, 0, s>>>(E, g, c->d_Bt, c->d_rowcount + n1); ADC_COUNT_LAUNCH();
+  if (c->direct) {
+    // the kept count (noffd) from one pass over the chunks; no values stay
+    for (const DirectChunk& dc : c->dchunks)
+      ST(coupling_values(c, c->d_Bt, dc.vbase, dc.row0, dc.row1, c->d_rowcount + n1));
+  } else {
+    ST(coupling_values(c, c->d_Bt, 0, 0, G.n2, c->d_rowcount + n1));
+  }
   ADC_CUDA(c, cudaGetLastError());
   unsigned long long kept_ph = 0;
   ADC_CUDA(c, cudaMemcpyAsync(&kept_ph, d_kept, sizeof(kept_ph), cudaMemcpyDeviceToHost, s));

@@ -79,6 +79,8 @@ static void free_matrix(Ctx* c) {
   c->ws_bytes = 0;
   free_sigma_plan(c);
   c->have_matrix = false;
+  c->direct = 0;
+  c->dchunks.clear();
 }
 
 static void free_eri(Ctx* c) {
@@ -237,7 +239,8 @@ int adcgpu_build_adc2s(adcgpu_ctx* h, int ndim, const int32_t* kpq, int64_t* nof
   CTX_CHECK(c);
   if (!c->have_orb || !c->have_eri) return set_err(c, ADCGPU_BAD_INPUT, "orbitals and ERIs must be set");
   if (ndim != c->geom.N) return set_err(c, ADCGPU_BAD_INPUT, "ndim does not match nocc/nvirt");
-  if (precision != ADCGPU_FP64 && precision != ADCGPU_MIXED) return set_err(c, ADCGPU_BAD_INPUT, "precision");
+  if (precision != ADCGPU_FP64 && precision != ADCGPU_MIXED && precision != ADCGPU_DIRECT)
+    return set_err(c, ADCGPU_BAD_INPUT, "precision");
   if (kpq) {
     std::vector<int32_t> ref((size_t)7 * (ndim + 1));
     adcgpu_select_adc2s(c->geom.no, c->geom.nv, ref.data());
@@ -247,11 +250,13 @@ int adcgpu_build_adc2s(adcgpu_ctx* h, int ndim, const int32_t* kpq, int64_t* nof
                        "kpq is not the C1 ADC(2)-s list of select_atom_is/select_atom_d (flag -1)");
   }
   free_matrix(c);
+  c->direct = precision == ADCGPU_DIRECT ? 1 : 0;
   int st = build_matrix(c);
   if (st) return st;
   st = prepare_desc(c);
   if (st) return st;
-  c->precision = precision;
+  // the direct path multiplies in FP64 like the stored FP64 path
+  c->precision = precision == ADCGPU_DIRECT ? ADCGPU_FP64 : precision;
   if (precision == ADCGPU_MIXED) {
     st = prepare_mixed(c);
     if (st) return st;
@@ -285,6 +290,7 @@ int adcgpu_export_coo(adcgpu_ctx* h, int64_t cap, double* hv, int32_t* oi, int32
   Ctx* c = reinterpret_cast<Ctx*>(h);
   CTX_CHECK(c);
   if (!c->have_matrix) return set_err(c, ADCGPU_NO_MATRIX, "no matrix");
+  if (c->direct) return set_err(c, ADCGPU_UNSUPPORTED, "the direct path stores no coupling block");
   if (cap < c->nnz_kept || !hv || !oi || !oj) return set_err(c, ADCGPU_BAD_INPUT, "cap < noffd");
   const int64_t n = c->nnz_kept;
   double* d_h = nullptr;
@@ -324,6 +330,7 @@ int adcgpu_write_hmlt_files(adcgpu_ctx* h, const char* dir, char flag) {
   Ctx* c = reinterpret_cast<Ctx*>(h);
   CTX_CHECK(c);
   if (!c->have_matrix) return set_err(c, ADCGPU_NO_MATRIX, "no matrix");
+  if (c->direct) return set_err(c, ADCGPU_UNSUPPORTED, "the direct path stores no coupling block");
   const int64_t n = c->nnz_kept, N = c->geom.N;
   std::vector<double> hv(n), diag(N);
   std::vector<int32_t> oi(n), oj(n);

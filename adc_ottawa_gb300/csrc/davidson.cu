@@ -225,6 +225,29 @@ struct DavidsonGPU {
   // configurations.
   int guess_subdiag(const std::vector<double>& hdiag, int subdim);
 
+  // initvec_adc1 (:246-289): the blocksize lowest eigenvectors of the ADC(1)
+  // singles matrix (adc1_guessvecs, guessvecs.f90:9-84) in the singles rows
+  // of V, the doubles rows zero.
+  int guess_adc1() {
+    const int n1 = (int)c->geom.n1;
+    if (blocksize > n1) return set_err(c, ADCGPU_BAD_INPUT, "ADC(1) guess: blocksize exceeds the singles space");
+    double* d_M = nullptr;
+    ST(dmalloc(c, (void**)&d_M, sizeof(double) * (size_t)n1 * n1));
+    int st = build_adc1_matrix(c, d_M);
+    std::vector<double> M((size_t)n1 * n1), w(n1), Vs((size_t)n1 * n1);
+    if (!st) st = d2h(c, M.data(), d_M, sizeof(double) * M.size()) == cudaSuccess ? ADCGPU_OK : ADCGPU_CUDA_ERROR;
+    dfree(c, d_M, 0);
+    if (st) return set_err(c, st, "ADC(1) guess: matrix");
+    if (!host_syev(n1, M.data(), n1, w.data(), Vs.data()))
+      return set_err(c, ADCGPU_EIGEN_FAILED, "ADC(1) matrix diagonalisation failed");
+    std::vector<T> colbuf(n1);
+    for (int i = 0; i < blocksize; ++i) {
+      for (int j = 0; j < n1; ++j) colbuf[j] = (T)Vs[(size_t)i * n1 + j];
+      ADC_CUDA(c, h2d(c, V + (size_t)i * N, colbuf.data(), sizeof(T) * n1));
+    }
+    return ADCGPU_OK;
+  }
+
   // Guess from given vectors (device, ncols columns, T type): orthonormalised.
   int guess_vectors(const T* G, int ncols) {
     int nb = std::min(ncols, blocksize);
@@ -250,6 +273,7 @@ struct DavidsonGPU {
     ST(alloc());
     if (guess_kind == 1) ST(guess_subdiag(hdiag, guessdim));
     else if (guess_kind == 2) ST(guess_vectors(guess_dev, nguess));
+    else if (guess_kind == 3) ST(guess_adc1());
     else ST(guess_ondiag(hdiag));
 
     int currdim = blocksize, bs_curr = blocksize, maxvec_curr = maxvec, nstates_curr = nstates;
@@ -450,6 +474,8 @@ __global__ void k_gather_sub(GeomDev g, const double* __restrict__ A, const doub
 
 template <typename T>
 int DavidsonGPU<T>::guess_subdiag(const std::vector<double>& hdiag, int subdim) {
+  if (c->direct)
+    return set_err(c, ADCGPU_UNSUPPORTED, "initvec_subdiag reads the stored coupling block; the direct path has none");
   if (subdim > N) subdim = (int)N;
   std::vector<int64_t> indx;
   host_heapsort_index(N, hdiag.data(), indx);
@@ -511,7 +537,8 @@ int davidson_solve(Ctx* c, const adcgpu_dav_params* p, double* evals, double* ev
     return set_err(c, ADCGPU_BAD_INPUT, "blocksize/maxvec incompatible with the matrix dimension");
   std::vector<double> hdiag(N);
   ADC_CUDA(c, d2h(c, hdiag.data(), c->d_diag, sizeof(double) * N));
-  const int guess_kind = p->lsubdiag ? 1 : 0;
+  // lsubdiag: 1 initvec_subdiag, 2 initvec_adc1, 0 initvec_ondiag
+  const int guess_kind = p->lsubdiag == 2 ? 3 : (p->lsubdiag ? 1 : 0);
   const int precon64 = p->precon;
   int st = ADCGPU_OK;
   adcgpu_dav_info inf{};
@@ -629,7 +656,8 @@ extern "C" int adcgpu_davidson_trace(adcgpu_ctx* h, const adcgpu_dav_params* p, 
   int st = dmalloc(c, (void**)&out, sizeof(double) * (size_t)N * blocksize);
   if (st) return st;
   int it = 0, nc = 0, nout = 0;
-  st = D.run(hdiag, p->lsubdiag ? 1 : 0, p->guessdim, nullptr, 0, ev, out, blocksize, &nout, &it, &nc);
+  st = D.run(hdiag, p->lsubdiag == 2 ? 3 : (p->lsubdiag ? 1 : 0), p->guessdim, nullptr, 0, ev, out, blocksize,
+             &nout, &it, &nc);
   if (st == ADCGPU_OK || st == ADCGPU_NOT_CONVERGED) {
     d2h(c, evecs, out, sizeof(double) * (size_t)N * nstates);
     for (int i = 0; i < nstates; ++i) evals[i] = ev[i];

@@ -40,6 +40,7 @@
 
 #include <cuda_runtime.h>
 #include <stdint.h>
+#include <algorithm>
 #include <atomic>
 #include <thread>
 #include <string>
@@ -195,6 +196,44 @@ __host__ __device__ inline int64_t entry_single(const GeomDev& g, const Double& 
   return (int64_t)a * no + (seg == 0 ? r.kp : r.lp);
 }
 
+// Chunk of whole slabs of the B^T store (the direct path recomputes the
+// coupling values of one chunk at a time): storage rows [row0, row1), values
+// [vbase, vbase + vlen), and the ranges of the sigma work lists that cover
+// those rows (tiled items, pass-1 chunks, pass-2 items).
+struct DirectChunk {
+  int64_t row0 = 0, row1 = 0, vbase = 0, vlen = 0;
+  int ti0 = 0, ti1 = 0, ch0 = 0, ch1 = 0, it0 = 0, it1 = 0;
+};
+
+// Whole slabs grouped in store order into chunks of at most 'budget' values
+// (a slab larger than the budget forms a chunk of its own).
+inline std::vector<DirectChunk> direct_chunk_rows(const Geometry& G, int64_t budget) {
+  std::vector<DirectChunk> out;
+  DirectChunk cur;
+  bool open = false;
+  for (int cls = 0; cls < 5; ++cls) {
+    const int64_t sl = G.slab_len(cls), L = G.len[cls];
+    for (int64_t s0 = G.start[cls]; s0 < G.start[cls + 1]; s0 += sl) {
+      const int64_t v0 = G.off[cls] + (s0 - G.start[cls]) * L, nvals = sl * L;
+      if (open && cur.vlen + nvals > budget) { out.push_back(cur); open = false; }
+      if (!open) { cur = DirectChunk(); cur.row0 = s0; cur.vbase = v0; open = true; }
+      cur.row1 = s0 + sl;
+      cur.vlen += nvals;
+    }
+  }
+  if (open) out.push_back(cur);
+  return out;
+}
+
+// Value budget of a direct-path chunk: at most 2^27 values (1 GiB in FP64)
+// and a quarter of the store, never less than the largest slab.
+inline int64_t direct_budget(const Geometry& G) {
+  int64_t slab = 0;
+  for (int cls = 0; cls < 5; ++cls)
+    if (G.start[cls + 1] > G.start[cls]) slab = std::max(slab, G.slab_len(cls) * G.len[cls]);
+  return std::max(slab, std::min<int64_t>((G.off[5] + 3) / 4, (int64_t)1 << 27));
+}
+
 // ---------------------------------------------------------------------------
 // Context.
 // ---------------------------------------------------------------------------
@@ -212,6 +251,8 @@ struct Ctx {
   Geometry geom;
   bool have_orb = false, have_eri = false, have_matrix = false;
   int precision = ADCGPU_FP64;
+  int direct = 0;                 // 1: matrix-free coupling block (d_Bt is one chunk's buffer)
+  std::vector<DirectChunk> dchunks;   // its chunks (row and value ranges)
   char flag = 'i';
   std::vector<double> e;          // orbital energies (host copy)
   double* d_e = nullptr;          // device orbital energies [nbas]
@@ -314,6 +355,11 @@ void dfree(Ctx* c, void* p, size_t bytes = 0);
 // build_kernels.cu
 int build_eri_blocks_from_packed(Ctx* c, const double* d_packed);
 int build_matrix(Ctx* c);
+// the ADC(1) (TDA) singles matrix, n1 x n1 (d_M: n1 * n1 doubles)
+int build_adc1_matrix(Ctx* c, double* d_M);
+// coupling values of store rows [row0, row1) into buf, which holds the values
+// from offset vbase on; kept-entry counts per row into rowcount (may be null)
+int coupling_values(Ctx* c, double* buf, int64_t vbase, int64_t row0, int64_t row1, int64_t* rowcount);
 int export_coo_device(Ctx* c, double* d_h, int32_t* d_oi, int32_t* d_oj);
 
 // sigma.cu : W = H V for m columns (column-major, leading dim ld), FP64 or FP32.
@@ -333,6 +379,7 @@ struct SigmaPlan {
   void* umma = nullptr;       // tensor-core pass plan (sigma_umma.cu), built on first use
   int umma_item_rows = 4096;  // rows per tensor-core work item (autotuned)
   int umma_off = 0;           // 1: the tensor-core pass is not used
+  std::vector<DirectChunk> dchunks;   // direct path: chunks with their work-list ranges
 };
 int prepare_desc(Ctx* c);
 int build_chunks(Ctx* c, int chunk);

@@ -1326,8 +1326,6 @@ int sigma_impl(Ctx* c, int m, const T* dV, int64_t ldv, T* dW, int64_t ldw, cons
   ADC_CUDA(c, cudaGetLastError());
   SigmaPlan* plan = reinterpret_cast<SigmaPlan*>(c->sigma_plan);
   if (!plan) return set_err(c, ADCGPU_NO_MATRIX, "sigma plan missing");
-  const int2* chunks = plan->d_chunks;
-  const int2* items = plan->d_items;
   // FP64 path: coupling contributions to W1 go straight into W.  FP32 path:
   // into an FP64 n1 x m accumulator, added to W1 at the end (a singles row
   // sums ~ n2 n1 / N products; FP32 atomics there would floor the residual).
@@ -1345,123 +1343,150 @@ int sigma_impl(Ctx* c, int m, const T* dV, int64_t ldv, T* dW, int64_t ldw, cons
     ADC_CUDA(c, cudaMemsetAsync(plan->d_acc, 0, need, s));
     W1base = reinterpret_cast<TAcc*>(plan->d_acc);
   }
-  // tiled pass 1 (k_sigma_tile) when its shared memory fits: widest column
-  // group first; segment B still runs through pass 2 in groups of <= 4
-  // FP32: 16 columns keep two blocks per SM (their loads overlap the other's
-  // arithmetic); FP64 is bound by the FP64 pipe at one block per SM
-  constexpr int MTMAX = 16;
-  const size_t smax = (size_t)smem_optin_max(c);
-  int mt_fit = 0;
-  for (int mt = MTMAX; mt >= 8 && !mt_fit; mt /= 2)
-    if (tile_smem_bytes(G.nvP, G.noP, mt, sizeof(T), sizeof(T)) <= smax) mt_fit = mt;
-  // a column tile always computes MT columns: below 16 columns the per-warp
-  // pass 1 is faster
-  const bool tiled = plan->tiled && plan->d_titems && mt_fit > 0 && m >= 16;
-  int c0 = 0;
+  // The coupling part over the work lists of P (the whole store, or the
+  // rows of one chunk of the direct path) with the values at BtP.
   bool umma_used = false;
-  if constexpr (std::is_same<TV, __nv_bfloat16>::value) {
-    // tensor-core pass (tcgen05, sigma_umma.cu) for the C|D segments and the
-    // W2 part of segment A, then segment B (pass 2) and the W1 part of
-    // segment A (pass 3), up to 48 columns per matrix pass
-    if (plan->tiled == 1 && !plan->umma_off && umma_supported(c)) {
-      ST(umma_prepare(c, plan->umma, plan->umma_item_rows));
-      const int2* runs = nullptr;
-      int nruns = 0;
-      ST(umma_runs(plan->umma, &runs, &nruns));
-      for (; c0 < m;) {
-        const int nc = std::min(m - c0, 48);
-        const T* V = dV + (int64_t)c0 * ldv;
-        T* W = dW + (int64_t)c0 * ldw;
-        TAcc* W1 = W1base + (int64_t)c0 * n1;
-        ST(umma_launch(c, plan->umma, V, ldv, nc, W, ldw, W1, n1));
-        for (int b0 = 0; plan->nitems && b0 < nc;) {
-          const int lb = nc - b0, mc = lb >= 8 ? 8 : (lb >= 4 ? 4 : (lb >= 2 ? 2 : 1));
-          ST((launch_p2<T, TV, TAcc>(c, g, plan, mc, Bt, V + (int64_t)b0 * ldv, ldv, W + (int64_t)b0 * ldw, ldw,
-                                     W1 + (int64_t)b0 * n1, n1)));
-          b0 += mc;
-        }
-        for (int b0 = 0; b0 < nc;) {
-          const int lb = nc - b0, mc = lb >= 8 ? 8 : (lb >= 4 ? 4 : (lb >= 2 ? 2 : 1));
-          ST((launch_p3<TV>(c, g, runs, nruns, mc, Bt, V + (int64_t)b0 * ldv, ldv, W1 + (int64_t)b0 * n1, n1)));
-          b0 += mc;
-        }
-        c0 += nc;
-      }
-      umma_used = true;
-    }
-  }
-  while (tiled && c0 < m) {
-    const int left = m - c0;
-    const int mt = left > 8 && mt_fit >= 16 ? 16 : 8;
-    const int ncols = std::min(left, mt);
-    const T* V = dV + (int64_t)c0 * ldv;
-    T* W = dW + (int64_t)c0 * ldw;
-    TAcc* W1 = sizeof(T) == 8 ? reinterpret_cast<TAcc*>(W) : W1base + (int64_t)c0 * n1;
-    const int64_t ld1 = sizeof(T) == 8 ? ldw : (int64_t)n1;
-    const size_t smem = tile_smem_bytes(G.nvP, G.noP, mt, sizeof(T), sizeof(T));
+  auto coupling = [&](const SigmaPlan* P, const TV* BtP, bool allow_umma) -> int {
+    int c0 = 0;
+    // tiled pass 1 (k_sigma_tile) when its shared memory fits: widest column
+    // group first; segment B still runs through pass 2 in groups of <= 4
+    // FP32: 16 columns keep two blocks per SM (their loads overlap the other's
+    // arithmetic); FP64 is bound by the FP64 pipe at one block per SM
+    constexpr int MTMAX = 16;
+    const size_t smax = (size_t)smem_optin_max(c);
+    int mt_fit = 0;
+    for (int mt = MTMAX; mt >= 8 && !mt_fit; mt /= 2)
+      if (tile_smem_bytes(G.nvP, G.noP, mt, sizeof(T), sizeof(T)) <= smax) mt_fit = mt;
+    // a column tile always computes MT columns: below 16 columns the per-warp
+    // pass 1 is faster
+    const bool tiled = P->tiled && P->d_titems && mt_fit > 0 && m >= 16;
     if constexpr (std::is_same<TV, __nv_bfloat16>::value) {
-      if (plan->tiled == 1 && tile_mma_smem_bytes(G.nvP, G.noP) <= smax) {
-        // tensor-core tile: 16 columns per pass
-        const int nc = std::min(left, MMA_MT);
-        ST((launch_tile_mma<TAcc>(c, g, plan, Bt, diag, V, ldv, nc, W, ldw, W1, ld1)));
-        for (int b0 = 0; plan->nitems && b0 < nc;) {
-          const int lb = nc - b0, mc = lb >= 8 ? 8 : (lb >= 4 ? 4 : (lb >= 2 ? 2 : 1));
-          ST((launch_p2<T, TV, TAcc>(c, g, plan, mc, Bt, V + (int64_t)b0 * ldv, ldv, W + (int64_t)b0 * ldw, ldw,
-                                     W1 + (int64_t)b0 * ld1, ld1)));
-          b0 += mc;
+      // tensor-core pass (tcgen05, sigma_umma.cu) for the C|D segments and the
+      // W2 part of segment A, then segment B (pass 2) and the W1 part of
+      // segment A (pass 3), up to 48 columns per matrix pass
+      if (allow_umma && P->tiled == 1 && !P->umma_off && umma_supported(c)) {
+        ST(umma_prepare(c, plan->umma, plan->umma_item_rows));
+        const int2* runs = nullptr;
+        int nruns = 0;
+        ST(umma_runs(plan->umma, &runs, &nruns));
+        for (; c0 < m;) {
+          const int nc = std::min(m - c0, 48);
+          const T* V = dV + (int64_t)c0 * ldv;
+          T* W = dW + (int64_t)c0 * ldw;
+          TAcc* W1 = W1base + (int64_t)c0 * n1;
+          ST(umma_launch(c, plan->umma, V, ldv, nc, W, ldw, W1, n1));
+          for (int b0 = 0; P->nitems && b0 < nc;) {
+            const int lb = nc - b0, mc = lb >= 8 ? 8 : (lb >= 4 ? 4 : (lb >= 2 ? 2 : 1));
+            ST((launch_p2<T, TV, TAcc>(c, g, P, mc, BtP, V + (int64_t)b0 * ldv, ldv, W + (int64_t)b0 * ldw, ldw,
+                                       W1 + (int64_t)b0 * n1, n1)));
+            b0 += mc;
+          }
+          for (int b0 = 0; b0 < nc;) {
+            const int lb = nc - b0, mc = lb >= 8 ? 8 : (lb >= 4 ? 4 : (lb >= 2 ? 2 : 1));
+            ST((launch_p3<TV>(c, g, runs, nruns, mc, BtP, V + (int64_t)b0 * ldv, ldv, W1 + (int64_t)b0 * n1, n1)));
+            b0 += mc;
+          }
+          c0 += nc;
         }
-        c0 += nc;
-        continue;
+        umma_used = true;
       }
     }
-    if (mt == 16) ST((launch_tile<T, TV, TAcc, 16>(c, g, plan, Bt, diag, V, ldv, ncols, W, ldw, W1, ld1, smem)));
-    else ST((launch_tile<T, TV, TAcc, 8>(c, g, plan, Bt, diag, V, ldv, ncols, W, ldw, W1, ld1, smem)));
-    ADC_CUDA(c, cudaGetLastError());
-    // segment B: pass 2 over the same columns
-    int b0 = 0;
-    while (plan->nitems && b0 < ncols) {
-      const int lb = ncols - b0;
-      const int mc = (sizeof(T) == 4 && lb >= 8) ? 8 : (lb >= 4 ? 4 : (lb >= 2 ? 2 : 1));
-      const T* Vb = V + (int64_t)b0 * ldv;
-      T* Wb = W + (int64_t)b0 * ldw;
-      TAcc* W1b = W1 + (int64_t)b0 * ld1;
-      ST((launch_p2<T, TV, TAcc>(c, g, plan, mc, Bt, Vb, ldv, Wb, ldw, W1b, ld1)));
+    while (tiled && c0 < m) {
+      const int left = m - c0;
+      const int mt = left > 8 && mt_fit >= 16 ? 16 : 8;
+      const int ncols = std::min(left, mt);
+      const T* V = dV + (int64_t)c0 * ldv;
+      T* W = dW + (int64_t)c0 * ldw;
+      TAcc* W1 = sizeof(T) == 8 ? reinterpret_cast<TAcc*>(W) : W1base + (int64_t)c0 * n1;
+      const int64_t ld1 = sizeof(T) == 8 ? ldw : (int64_t)n1;
+      const size_t smem = tile_smem_bytes(G.nvP, G.noP, mt, sizeof(T), sizeof(T));
+      if constexpr (std::is_same<TV, __nv_bfloat16>::value) {
+        if (P->tiled == 1 && tile_mma_smem_bytes(G.nvP, G.noP) <= smax) {
+          // tensor-core tile: 16 columns per pass
+          const int nc = std::min(left, MMA_MT);
+          ST((launch_tile_mma<TAcc>(c, g, P, BtP, diag, V, ldv, nc, W, ldw, W1, ld1)));
+          for (int b0 = 0; P->nitems && b0 < nc;) {
+            const int lb = nc - b0, mc = lb >= 8 ? 8 : (lb >= 4 ? 4 : (lb >= 2 ? 2 : 1));
+            ST((launch_p2<T, TV, TAcc>(c, g, P, mc, BtP, V + (int64_t)b0 * ldv, ldv, W + (int64_t)b0 * ldw, ldw,
+                                       W1 + (int64_t)b0 * ld1, ld1)));
+            b0 += mc;
+          }
+          c0 += nc;
+          continue;
+        }
+      }
+      if (mt == 16) ST((launch_tile<T, TV, TAcc, 16>(c, g, P, BtP, diag, V, ldv, ncols, W, ldw, W1, ld1, smem)));
+      else ST((launch_tile<T, TV, TAcc, 8>(c, g, P, BtP, diag, V, ldv, ncols, W, ldw, W1, ld1, smem)));
       ADC_CUDA(c, cudaGetLastError());
-      b0 += mc;
+      // segment B: pass 2 over the same columns
+      int b0 = 0;
+      while (P->nitems && b0 < ncols) {
+        const int lb = ncols - b0;
+        const int mc = (sizeof(T) == 4 && lb >= 8) ? 8 : (lb >= 4 ? 4 : (lb >= 2 ? 2 : 1));
+        const T* Vb = V + (int64_t)b0 * ldv;
+        T* Wb = W + (int64_t)b0 * ldw;
+        TAcc* W1b = W1 + (int64_t)b0 * ld1;
+        ST((launch_p2<T, TV, TAcc>(c, g, P, mc, BtP, Vb, ldv, Wb, ldw, W1b, ld1)));
+        ADC_CUDA(c, cudaGetLastError());
+        b0 += mc;
+      }
+      c0 += ncols;
     }
-    c0 += ncols;
-  }
-  while (c0 < m) {
-    const int left = m - c0;
-    const T* V = dV + (int64_t)c0 * ldv;
-    T* W = dW + (int64_t)c0 * ldw;
-    TAcc* W1 = sizeof(T) == 8 ? reinterpret_cast<TAcc*>(W) : W1base + (int64_t)c0 * n1;
-    const int64_t ld1 = sizeof(T) == 8 ? ldw : (int64_t)n1;
-    int cap = plan->mc_cap[sizeof(T) == 8 ? 0 : 1];
-    if (sizeof(T) == 8) cap = std::min(cap, 2);
-    const int mc = (left >= 4 && cap >= 4) ? 4 : ((left >= 2 && cap >= 2) ? 2 : 1);
-    const int g1 = std::min(plan->nchunks, c->nsm * 4 * 16) / 4 + 1;   // 4 warps per block
-    const int g2 = std::min(plan->nitems, c->nsm * 8 * 8) / 8 + 1;
-#define LAUNCH_P2(MC, GS) \
-  k_sigma_p2<T, TV, TAcc, MC, GS><<<g2, 256, 0, s>>>(g, items, plan->nitems, Bt, V, ldv, W, ldw, W1, ld1); ADC_COUNT_LAUNCH();
-#define LAUNCH(MC)                                                                                              \
-  if (plan->staged) {                                                                                           \
-    constexpr int NS = sizeof(TV) == 2 ? 8 : 4;                                                                 \
-    const size_t smem = (size_t)4 * NS * (32 * 16 * sizeof(TV) + 16 * MC);                                    \
-    auto kern = k_sigma_p1s<T, TV, TAcc, MC, NS>;                                                               \
-    ADC_CUDA(c, cudaFuncSetAttribute(kern, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem));            \
-    kern<<<g1, 128, smem, s>>>(g, chunks, plan->nchunks, Bt, diag, V, ldv, W, ldw, W1, ld1); ADC_COUNT_LAUNCH();                   \
-  } else {                                                                                                      \
-    k_sigma_p1<T, TV, TAcc, MC><<<g1, 128, 0, s>>>(g, chunks, plan->nchunks, Bt, diag, V, ldv, W, ldw, W1, ld1); ADC_COUNT_LAUNCH(); \
-  }                                                                                                             \
-  if (plan->nitems) {                                                                                           \
-    if (G.noP <= 8) { LAUNCH_P2(MC, 1) } else if (G.noP <= 16) { LAUNCH_P2(MC, 2) } else { LAUNCH_P2(MC, 4) }   \
-  }
-    if (mc == 4) { LAUNCH(4) } else if (mc == 2) { LAUNCH(2) } else { LAUNCH(1) }
-#undef LAUNCH
-#undef LAUNCH_P2
-    ADC_CUDA(c, cudaGetLastError());
-    c0 += mc;
+    while (c0 < m) {
+      const int left = m - c0;
+      const T* V = dV + (int64_t)c0 * ldv;
+      T* W = dW + (int64_t)c0 * ldw;
+      TAcc* W1 = sizeof(T) == 8 ? reinterpret_cast<TAcc*>(W) : W1base + (int64_t)c0 * n1;
+      const int64_t ld1 = sizeof(T) == 8 ? ldw : (int64_t)n1;
+      int cap = P->mc_cap[sizeof(T) == 8 ? 0 : 1];
+      if (sizeof(T) == 8) cap = std::min(cap, 2);
+      const int mc = (left >= 4 && cap >= 4) ? 4 : ((left >= 2 && cap >= 2) ? 2 : 1);
+      const int g1 = std::min(P->nchunks, c->nsm * 4 * 16) / 4 + 1;   // 4 warps per block
+      const int g2 = std::min(P->nitems, c->nsm * 8 * 8) / 8 + 1;
+  #define LAUNCH_P2(MC, GS) \
+    k_sigma_p2<T, TV, TAcc, MC, GS><<<g2, 256, 0, s>>>(g, P->d_items, P->nitems, BtP, V, ldv, W, ldw, W1, ld1); ADC_COUNT_LAUNCH();
+  #define LAUNCH(MC)                                                                                              \
+    if (P->staged) {                                                                                           \
+      constexpr int NS = sizeof(TV) == 2 ? 8 : 4;                                                                 \
+      const size_t smem = (size_t)4 * NS * (32 * 16 * sizeof(TV) + 16 * MC);                                    \
+      auto kern = k_sigma_p1s<T, TV, TAcc, MC, NS>;                                                               \
+      ADC_CUDA(c, cudaFuncSetAttribute(kern, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem));            \
+      kern<<<g1, 128, smem, s>>>(g, P->d_chunks, P->nchunks, BtP, diag, V, ldv, W, ldw, W1, ld1); ADC_COUNT_LAUNCH();                   \
+    } else {                                                                                                      \
+      k_sigma_p1<T, TV, TAcc, MC><<<g1, 128, 0, s>>>(g, P->d_chunks, P->nchunks, BtP, diag, V, ldv, W, ldw, W1, ld1); ADC_COUNT_LAUNCH(); \
+    }                                                                                                             \
+    if (P->nitems) {                                                                                           \
+      if (G.noP <= 8) { LAUNCH_P2(MC, 1) } else if (G.noP <= 16) { LAUNCH_P2(MC, 2) } else { LAUNCH_P2(MC, 4) }   \
+    }
+      if (mc == 4) { LAUNCH(4) } else if (mc == 2) { LAUNCH(2) } else { LAUNCH(1) }
+  #undef LAUNCH
+  #undef LAUNCH_P2
+      ADC_CUDA(c, cudaGetLastError());
+      c0 += mc;
+    }
+    return ADCGPU_OK;
+  };
+  if (c->direct) {
+    // direct (matrix-free) path: the coupling values are recomputed for each
+    // chunk of whole slabs into the chunk buffer and used at once
+    if constexpr (std::is_same<TV, double>::value) {
+      for (const DirectChunk& dc : plan->dchunks) {
+        ST(coupling_values(c, c->d_Bt, dc.vbase, dc.row0, dc.row1, nullptr));
+        SigmaPlan view = *plan;
+        view.d_titems = plan->d_titems + dc.ti0; view.ntitems = dc.ti1 - dc.ti0;
+        view.d_chunks = plan->d_chunks + dc.ch0; view.nchunks = dc.ch1 - dc.ch0;
+        view.d_items = plan->d_items + dc.it0; view.nitems = dc.it1 - dc.it0;
+        // the kernels address row r at Bt + off[cls] + (r - start[cls]) L;
+        // shifting the base by the chunk's first value puts its rows in the buffer
+        const TV* BtP = reinterpret_cast<const TV*>(reinterpret_cast<uintptr_t>(c->d_Bt) -
+                                                    (uintptr_t)dc.vbase * sizeof(TV));
+        ST(coupling(&view, BtP, false));
+      }
+    } else {
+      return set_err(c, ADCGPU_UNSUPPORTED, "the direct path computes in FP64");
+    }
+  } else {
+    ST(coupling(plan, Bt, true));
   }
   if (sizeof(T) == 4) {
     k_w1_finalize<<<(n1 * m + 255) / 256, 256, 0, s>>>(n1, m, reinterpret_cast<const double*>(W1base),
@@ -1498,9 +1523,15 @@ __global__ void k_to_bf16(const double* __restrict__ x, __nv_bfloat16* __restric
 int build_chunks(Ctx* c, int chunk) {
   const Geometry& G = c->geom;
   std::vector<int2> chunks, items, titems;
+  // direct path: the work-list ranges of each chunk of slabs
+  std::vector<DirectChunk> dch = c->direct ? c->dchunks : std::vector<DirectChunk>();
+  size_t di = 0;
   for (int cls = 0; cls < 5; ++cls) {
     const int64_t r0 = G.start[cls], r1 = G.start[cls + 1], sl = G.slab_len(cls);
     for (int64_t s0 = r0; s0 < r1; s0 += sl) {
+      if (di < dch.size() && s0 == dch[di].row0) {
+        dch[di].ti0 = (int)titems.size(); dch[di].ch0 = (int)chunks.size(); dch[di].it0 = (int)items.size();
+      }
       for (int64_t a = s0; a < s0 + sl; a += chunk)
         chunks.push_back(make_int2((int)a, (int)std::min<int64_t>(a + chunk, s0 + sl)));
       // tiled pass 1: equal pieces of at most TILE_ITEM_ROWS rows per slab
@@ -1509,6 +1540,10 @@ int build_chunks(Ctx* c, int chunk) {
         titems.push_back(make_int2((int)a, (int)std::min<int64_t>(a + per, s0 + sl)));
       if (cls == 1 || cls >= 3)
         for (int bp = 1; bp < G.nv; ++bp) items.push_back(make_int2((int)s0, bp));
+      if (di < dch.size() && s0 + sl == dch[di].row1) {
+        dch[di].ti1 = (int)titems.size(); dch[di].ch1 = (int)chunks.size(); dch[di].it1 = (int)items.size();
+        ++di;
+      }
     }
   }
   SigmaPlan* plan = reinterpret_cast<SigmaPlan*>(c->sigma_plan);
@@ -1529,6 +1564,7 @@ int build_chunks(Ctx* c, int chunk) {
   plan->nchunks = (int)chunks.size();
   plan->nitems = (int)items.size();
   plan->chunk = chunk;
+  plan->dchunks = dch;
   return ADCGPU_OK;
 }
 

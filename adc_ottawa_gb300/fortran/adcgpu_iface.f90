@@ -204,6 +204,28 @@ contains
   end subroutine write_fspace_adc2_1_gpu
 
 !#######################################################################
+! The matvec (direct) path: get_interm_adc2_save (get_matrix.f90:625-701)
+! and davdir_block (dmatvec_davidson.f90:41-149).  The ph-ph block and the
+! diagonal are built from Ca1/Cb1/Cc1/Cc2 and kept on the device; the
+! coupling block is recomputed from the integrals in every sigma product,
+! as get_matvec_adc2s_omp (:1031-1230) does, so nothing is written to
+! SCRATCH.  The Davidson settings are those of davdiag_block_gpu.
+
+  subroutine davdir_block_gpu(matdim, kpq)
+    use parameters, only: nbas, nocc, hamflag
+    integer, intent(in)                                 :: matdim
+    integer, dimension(7,0:nBas**2*nOcc**2), intent(in) :: kpq
+    integer(c_int)     :: st
+    integer(c_int64_t) :: n
+    integer*8          :: noffd
+    call adcgpu_init
+    st = adcgpu_build_adc2s(gpu_ctx, int(matdim,c_int), kpq, n, hamflag, 2_c_int)
+    call adcgpu_check(st, 'get_interm_adc2_save')
+    noffd = n
+    call davdiag_block_gpu(matdim, noffd)
+  end subroutine davdir_block_gpu
+
+!#######################################################################
 ! davdiag_block (block_davidson.f90:33-145), initial space ('i') or final
 ! space ('f') parameters as selected by hamflag.
 
@@ -218,10 +240,12 @@ contains
     if (hamflag.eq.'i') then
        p%davstates=davstates; p%dmain=dmain; p%maxsubdim=maxsubdim; p%maxiter=maxiter
        p%precon=precon; p%ldfl=merge(1,0,ldfl); p%lsubdiag=merge(1,0,lsubdiag)
+       if (ladc1guess) p%lsubdiag=2     ! initvec_adc1 ahead of initvec_subdiag (:107-117)
        p%guessdim=guessdim; p%davtol=davtol
     else
        p%davstates=davstates_f; p%dmain=dmain_f; p%maxsubdim=maxsubdim_f; p%maxiter=maxiter_f
        p%precon=precon_f; p%ldfl=merge(1,0,ldfl_f); p%lsubdiag=merge(1,0,lsubdiag_f)
+       if (ladc1guess_f) p%lsubdiag=2
        p%guessdim=guessdim_f; p%davtol=davtol_f
     endif
     p%precision=0; p%refine=0; p%tol_bf16=0.0_dp; p%tol_fp32=0.0_dp

@@ -54,8 +54,13 @@ enum adcgpu_status {
 /* Storage precision of the stored matrix used by the sigma-vector product. */
 enum adcgpu_precision {
   ADCGPU_FP64 = 0,   /* FP64 values, FP64 vectors: the plain drop-in path      */
-  ADCGPU_MIXED = 1   /* BF16/FP32 values, FP32 vectors and subspace GEMMs,
+  ADCGPU_MIXED = 1,  /* BF16/FP32 values, FP32 vectors and subspace GEMMs,
                         FP64 Rayleigh-Ritz, Gram-Schmidt and residual norms    */
+  ADCGPU_DIRECT = 2  /* FP64 as ADCGPU_FP64, but the coupling block is not
+                        stored: every sigma product recomputes it from the
+                        integrals, a chunk of slabs at a time (the matvec
+                        path, get_matvec_adc2s_omp dmatvec_davidson.f90
+                        :1031-1230; ph-ph block from Ca1/Cb1/Cc1/Cc2)        */
 };
 
 /* Preconditioners (parameters.f90 precon; block_davidson.f90:1119-1123). */
@@ -171,7 +176,8 @@ typedef struct {
   int maxiter;       /* niter                                       */
   int precon;        /* adcgpu_precon                               */
   int ldfl;          /* deflation of converged vectors (1/0)        */
-  int lsubdiag;      /* 1: initvec_subdiag, 0: initvec_ondiag       */
+  int lsubdiag;      /* 1: initvec_subdiag, 2: initvec_adc1 (the
+                        reference's ladc1guess), 0: initvec_ondiag  */
   int guessdim;      /* subspace dimension for initvec_subdiag      */
   double davtol;     /* residual-norm tolerance                     */
   int precision;     /* adcgpu_precision for the iterations         */

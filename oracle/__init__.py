@@ -46,6 +46,8 @@ def lib():
         L.orc_select.restype = C.c_int
         L.orc_build.argtypes = [C.c_int, C.c_int, _dp, _dp, C.c_int]
         L.orc_build.restype = C.c_void_p
+        L.orc_build_direct.argtypes = [C.c_int, C.c_int, _dp, _dp, C.c_int]
+        L.orc_build_direct.restype = C.c_void_p
         L.orc_matrix_ndim.argtypes = [C.c_void_p]
         L.orc_matrix_ndim.restype = C.c_int64
         L.orc_matrix_nnz.argtypes = [C.c_void_p]
@@ -61,6 +63,10 @@ def lib():
         L.orc_heapsort_index_desc.argtypes = [C.c_int, _dp, _ip]
         L.orc_davidson.argtypes = [C.c_void_p, _ip, C.c_double, C.c_int, _dp, _dp, _ip]
         L.orc_davidson.restype = C.c_int
+        L.orc_davidson_guess.argtypes = [C.c_void_p, _ip, C.c_double, C.c_int, _dp, _dp, _dp, _ip]
+        L.orc_davidson_guess.restype = C.c_int
+        L.orc_adc1_matrix.argtypes = [C.c_int, C.c_int, _dp, _dp, _dp]
+        L.orc_adc1_matrix.restype = C.c_int
         L.orc_block_lanczos.argtypes = [C.c_void_p, C.c_int, C.c_int, C.c_int, _dp, C.c_int, _dp, _dp]
         L.orc_block_lanczos.restype = C.c_int
         L.orc_autocorr.argtypes = [C.c_void_p, _dp, C.c_double, C.c_double, C.c_int, C.c_double,
@@ -110,6 +116,25 @@ def adc2s_dim(no: int, nv: int) -> int:
     return int(lib().orc_adc2s_dim(no, nv, _p(cnt, _ip)))
 
 
+def adc1_matrix(no: int, nv: int, e, eri) -> np.ndarray:
+    """The ADC(1) singles matrix (get_diag/offdiag_tda_direct), n1 x n1."""
+    e = np.ascontiguousarray(e, np.float64)
+    eri = np.ascontiguousarray(eri, np.float64)
+    M = np.zeros((no * nv, no * nv), order="F")
+    assert lib().orc_adc1_matrix(no, nv, _p(e), _p(eri), _p(M)) == no * nv
+    return M
+
+
+def adc1_guess(no: int, nv: int, e, eri, ndim: int, blocksize: int) -> np.ndarray:
+    """initvec_adc1's start block: the blocksize lowest ADC(1) eigenvectors
+    (numpy's LAPACK, ascending) in the singles rows of an ndim x blocksize
+    block."""
+    _, U = np.linalg.eigh(adc1_matrix(no, nv, e, eri))
+    G = np.zeros((ndim, blocksize), order="F")
+    G[: no * nv] = U[:, :blocksize]
+    return G
+
+
 def select(no: int, nv: int) -> np.ndarray:
     """kpq(7, 0:ndim) as a (ndim+1, 7) int32 array (row c = Fortran column c)."""
     n1 = no * nv
@@ -131,6 +156,15 @@ class Matrix:
         e = np.ascontiguousarray(e, dtype=np.float64)
         eri = np.ascontiguousarray(eri, dtype=np.float64)
         return cls(lib().orc_build(no, nv, _p(e), _p(eri), nthreads))
+
+    @classmethod
+    def build_direct(cls, no, nv, e, eri, nthreads=0):
+        """The matrix of the direct (matvec) path: ph-ph block from
+        Ca1/Cb1/Cc1/Cc2 (adc_ph.f90:98-303), coupling and 2p2h diagonal as
+        in the stored path."""
+        e = np.ascontiguousarray(e, dtype=np.float64)
+        eri = np.ascontiguousarray(eri, dtype=np.float64)
+        return cls(lib().orc_build_direct(no, nv, _p(e), _p(eri), nthreads))
 
     @classmethod
     def from_coo(cls, diag, h, oi, oj):
@@ -173,14 +207,23 @@ class Matrix:
         return W
 
     def davidson(self, nstates, tol, blocksize=0, maxvec=-1, niter=100, precon=1, deflate=True,
-                 subdiag=False, guessdim=800, nthreads=0, want_vectors=False):
+                 subdiag=False, guessdim=800, nthreads=0, want_vectors=False, guess=None):
+        """guess: ndim x blocksize start vectors (initvec_adc1 places the
+        ADC(1) eigenvectors this way); otherwise initvec_subdiag/_ondiag."""
         ip = np.array([nstates, blocksize, maxvec, niter, precon, int(deflate), int(subdiag), guessdim],
                       dtype=np.int32)
         ev = np.empty(nstates)
         vecs = np.empty((self.ndim, nstates), order="F") if want_vectors else None
         iout = np.zeros(3, np.int32)
-        st = lib().orc_davidson(self.h, _p(ip, _ip), tol, nthreads, _p(ev),
-                                _p(vecs) if want_vectors else None, _p(iout, _ip))
+        if guess is not None:
+            bs = blocksize if blocksize > 0 else max(nstates + 5, 2 * nstates)
+            G = np.asfortranarray(guess, np.float64)
+            assert G.shape == (self.ndim, bs), (G.shape, bs)
+            st = lib().orc_davidson_guess(self.h, _p(ip, _ip), tol, nthreads, _p(G), _p(ev),
+                                          _p(vecs) if want_vectors else None, _p(iout, _ip))
+        else:
+            st = lib().orc_davidson(self.h, _p(ip, _ip), tol, nthreads, _p(ev),
+                                    _p(vecs) if want_vectors else None, _p(iout, _ip))
         return st, ev, vecs, dict(iterations=int(iout[0]), nmult=int(iout[1]), nconv=int(iout[2]))
 
     def block_lanczos(self, q0, ncycles, orthotype=0, nthreads=0):

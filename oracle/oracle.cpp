@@ -127,6 +127,70 @@ double CB_ph_ph(const System& S, int k, int k1) {                      // :819-9
   return -0.5 * cb;
 }
 
+// The direct (matvec) path's ph-ph formulas, adc_ph.f90:98-303, used by
+// hiivec and get_matvec_adc2s_omp (dmatvec_davidson.f90:888-978,1031-1230).
+double Ca1_ph_ph(const System& S, int a, int a1) {                     // :98-152
+  const std::vector<double>& e = S.e;
+  double ca = 0.0;
+  for (int r = S.no + 1; r <= S.nbas; ++r)
+    for (int u = 1; u <= S.no; ++u)
+      for (int v = 1; v <= S.no; ++v) {
+        double eija = e[r] + e[a] - e[u] - e[v];
+        double eijc = e[r] + e[a1] - e[u] - e[v];
+        double DA = 1.0 / ((e[r] + e[a] - e[u] - e[v]) * (e[r] + e[a1] - e[u] - e[v]));
+        double term = 0.0;
+        term = term + eijc * S.v(a1, u, r, v) * (2.0 * S.v(u, a, v, r) - S.v(u, r, v, a));
+        term = term + eija * S.v(a, v, r, u) * (2.0 * S.v(u, r, v, a1) - S.v(u, a1, v, r));
+        term = DA * term;
+        ca = ca + term;
+      }
+  return 0.5 * ca;
+}
+
+double Cb1_ph_ph(const System& S, int k, int k1) {                     // :158-211
+  const std::vector<double>& e = S.e;
+  double cb = 0.0;
+  for (int r = S.no + 1; r <= S.nbas; ++r)
+    for (int s = S.no + 1; s <= S.nbas; ++s)
+      for (int u = 1; u <= S.no; ++u) {
+        double eicd = e[r] + e[s] - e[u] - e[k];
+        double ejcd = e[r] + e[s] - e[u] - e[k1];
+        double DB = 1.0 / ((e[r] + e[s] - e[u] - e[k]) * (e[r] + e[s] - e[u] - e[k1]));
+        double term = 0.0;
+        term = term + ejcd * S.v(r, k1, s, u) * (2.0 * S.v(k, r, u, s) - S.v(k, s, u, r));
+        term = term + eicd * S.v(r, u, s, k) * (2.0 * S.v(k1, s, u, r) - S.v(k1, r, u, s));
+        term = DB * term;
+        cb = cb + term;
+      }
+  return 0.5 * cb;
+}
+
+double Cc1_ph_ph(const System& S, int a, int k, int a1, int k1) {       // :214-256
+  const std::vector<double>& e = S.e;
+  double cc = 0.0;
+  for (int r = S.no + 1; r <= S.nbas; ++r)
+    for (int s = 1; s <= S.no; ++s) {
+      double DC = 1.0 / (e[r] + e[a] - e[s] - e[k]);
+      double term = (2.0 * S.v(a, k, r, s) - S.v(a, s, r, k)) * (2.0 * S.v(a1, k1, r, s) - S.v(a1, s, r, k1));
+      term = term * DC;
+      cc = cc + term;
+    }
+  return -0.5 * cc;
+}
+
+double Cc2_ph_ph(const System& S, int a, int k, int a1, int k1) {       // :261-303
+  const std::vector<double>& e = S.e;
+  double cc = 0.0;
+  for (int r = S.no + 1; r <= S.nbas; ++r)
+    for (int s = 1; s <= S.no; ++s) {
+      double DC = 1.0 / (e[r] + e[a1] - e[s] - e[k1]);
+      double term = (2.0 * S.v(a, k, r, s) - S.v(a, s, r, k)) * (2.0 * S.v(a1, k1, r, s) - S.v(a1, s, r, k1));
+      term = term * DC;
+      cc = cc + term;
+    }
+  return -0.5 * cc;
+}
+
 double CC_ph_ph(const System& S, int a, int k, int a1, int k1) {        // :918-957
   const std::vector<double>& e = S.e;
   double cc = 0.0;
@@ -221,7 +285,23 @@ int orc_select(int no, int nv, int32_t* kpq_out) {
 // (get_matrix.f90:705-1186).  Entries are collected per single i in the loop
 // order of the reference (ph-ph, then the C5, C4, C3, C1, C2 class loops), so
 // the COO order equals that of the serial twin get_offdiag_adc2_save.
+static void* build_impl(int no, int nv, const double* e, const double* eri, int nthreads, bool direct);
+
 void* orc_build(int no, int nv, const double* e, const double* eri, int nthreads) {
+  return build_impl(no, nv, e, eri, nthreads, false);
+}
+
+// The matrix the direct path multiplies on the fly (get_matvec_adc2s_omp,
+// dmatvec_davidson.f90:1031-1230, diagonal hiivec :888-978): ph-ph block from
+// Ca1/Cb1/Cc1/Cc2 with the same abs > 1e-12 test, the coupling block and the
+// 2p2h diagonal as in the stored path.  Stored here as COO so the oracle's
+// Davidson multiplies it; the product equals the on-the-fly one up to the
+// reference's grouping of each element's terms.
+void* orc_build_direct(int no, int nv, const double* e, const double* eri, int nthreads) {
+  return build_impl(no, nv, e, eri, nthreads, true);
+}
+
+static void* build_impl(int no, int nv, const double* e, const double* eri, int nthreads, bool direct) {
   System S;
   S.no = no; S.nv = nv; S.nbas = no + nv; S.eri = eri;
   S.e.assign(S.nbas + 1, 0.0);
@@ -244,13 +324,13 @@ void* orc_build(int no, int nv, const double* e, const double* eri, int nthreads
 #pragma omp parallel for schedule(dynamic) num_threads(nthreads)
   for (int i = 1; i <= nv; ++i)
     for (int j = i; j <= nv; ++j) {
-      double x = CA_ph_ph(S, no + i, no + j);
+      double x = direct ? Ca1_ph_ph(S, no + i, no + j) : CA_ph_ph(S, no + i, no + j);
       ca[(size_t)(i - 1) * nv + (j - 1)] = x; ca[(size_t)(j - 1) * nv + (i - 1)] = x;
     }
 #pragma omp parallel for schedule(dynamic) num_threads(nthreads)
   for (int i = 1; i <= no; ++i)
     for (int j = i; j <= no; ++j) {
-      double x = CB_ph_ph(S, i, j);
+      double x = direct ? Cb1_ph_ph(S, i, j) : CB_ph_ph(S, i, j);
       cb[(size_t)(i - 1) * no + (j - 1)] = x; cb[(size_t)(j - 1) * no + (i - 1)] = x;
     }
 
@@ -261,9 +341,16 @@ void* orc_build(int no, int nv, const double* e, const double* eri, int nthreads
     int a = c.a, j = c.j;
     double x = K_ph_ph(S.e[a], S.e[j]);
     x = x + C1_ph_ph(S, a, j, a, j);
-    x = x + CA_ph_ph(S, a, a);
-    x = x + CB_ph_ph(S, j, j);
-    x = x + CC_ph_ph(S, a, j, a, j);
+    if (direct) {   // hiivec :917-924
+      x = x + Ca1_ph_ph(S, a, a);
+      x = x + Cb1_ph_ph(S, j, j);
+      x = x + Cc1_ph_ph(S, a, j, a, j);
+      x = x + Cc2_ph_ph(S, a, j, a, j);
+    } else {
+      x = x + CA_ph_ph(S, a, a);
+      x = x + CB_ph_ph(S, j, j);
+      x = x + CC_ph_ph(S, a, j, a, j);
+    }
     M->diag[i - 1] = x;
   }
   for (int64_t i = ndim1 + 1; i <= ndim; ++i) {
@@ -298,7 +385,12 @@ void* orc_build(int no, int nv, const double* e, const double* eri, int nthreads
             x = C1_ph_ph(S, a, k, cj.a, cj.j);
             if (k == cj.j) x = x + ca[(size_t)(a - no - 1) * nv + (cj.a - no - 1)];
             if (a == cj.a) x = x + cb[(size_t)(k - 1) * no + (cj.j - 1)];
-            x = x + CC_ph_ph(S, a, k, cj.a, cj.j);
+            if (direct) {   // dmatvec_davidson.f90:1100-1107
+              x = x + Cc1_ph_ph(S, a, k, cj.a, cj.j);
+              x = x + Cc2_ph_ph(S, a, k, cj.a, cj.j);
+            } else {
+              x = x + CC_ph_ph(S, a, k, cj.a, cj.j);
+            }
             break;
           case 1: x = C5_ph_2p2h(S, a, k, cj.a, cj.j); break;
           case 2: x = C4_ph_2p2h(S, a, k, cj.a, cj.b, cj.j); break;
@@ -628,8 +720,47 @@ void orc_heapsort_index_desc(int n, const double* arr, int32_t* indx_out) {
 //          [3]=niter [4]=ipre (1 DPR, 2 Olsen) [5]=ldeflate [6]=lsub
 //          [7]=subdim(guessdim)
 // iout:    [0]=iterations [1]=nmult [2]=nconv
+static int davidson_impl(void* m, const int* iparams, double tol, int nthreads, const double* guess,
+                         double* evals, double* evecs, int* iout);
+
 int orc_davidson(void* m, const int* iparams, double tol, int nthreads, double* evals,
                  double* evecs, int* iout) {
+  return davidson_impl(m, iparams, tol, nthreads, nullptr, evals, evecs, iout);
+}
+
+// The same run started from given vectors (matdim x blocksize column-major),
+// as initvec_adc1 (block_davidson.f90:246-289) places the ADC(1) eigenvectors.
+int orc_davidson_guess(void* m, const int* iparams, double tol, int nthreads, const double* guess,
+                       double* evals, double* evecs, int* iout) {
+  return davidson_impl(m, iparams, tol, nthreads, guess, evals, evecs, iout);
+}
+
+// get_diag_tda_direct and get_offdiag_tda_direct (get_matrix.f90:17-82): the
+// ADC(1) singles matrix K_ph_ph + C1_ph_ph in select_atom_is order, dense
+// n1 x n1 column-major; its eigenvectors are what adc1_guessvecs
+// (guessvecs.f90:9-84) writes for initvec_adc1.
+int orc_adc1_matrix(int no, int nv, const double* e, const double* eri, double* M_out) {
+  System S;
+  S.no = no; S.nv = nv; S.nbas = no + nv; S.eri = eri;
+  S.e.assign(S.nbas + 1, 0.0);
+  for (int p = 1; p <= S.nbas; ++p) S.e[p] = e[p - 1];
+  std::vector<Conf> kpq; int cnt[5];
+  select_configs(no, nv, kpq, cnt);
+  const int n1 = cnt[0];
+  for (int i = 1; i <= n1; ++i) {
+    const Conf& ci = kpq[i];
+    M_out[(size_t)(i - 1) * n1 + (i - 1)] = K_ph_ph(S.e[ci.a], S.e[ci.j]) + C1_ph_ph(S, ci.a, ci.j, ci.a, ci.j);
+    for (int j = i + 1; j <= n1; ++j) {
+      const Conf& cj = kpq[j];
+      M_out[(size_t)(j - 1) * n1 + (i - 1)] = C1_ph_ph(S, ci.a, ci.j, cj.a, cj.j);
+      M_out[(size_t)(i - 1) * n1 + (j - 1)] = C1_ph_ph(S, cj.a, cj.j, ci.a, ci.j);
+    }
+  }
+  return n1;
+}
+
+static int davidson_impl(void* m, const int* iparams, double tol, int nthreads, const double* guess,
+                         double* evals, double* evecs, int* iout) {
   OrcMatrix* M = (OrcMatrix*)m;
 #ifdef _OPENMP
   if (nthreads <= 0) nthreads = omp_get_max_threads();
@@ -653,7 +784,9 @@ int orc_davidson(void* m, const int* iparams, double tol, int nthreads, double* 
   const std::vector<double>& hii = M->diag;
 
   // initial vectors
-  if (lsub) {
+  if (guess) {
+    for (int i = 0; i < blocksize; ++i) std::memcpy(&vmat[(size_t)i * N], guess + (size_t)i * N, sizeof(double) * N);
+  } else if (lsub) {
     // initvec_subdiag :293-459
     if (subdim > matdim) subdim = (int)matdim;
     std::vector<int> indxhii;

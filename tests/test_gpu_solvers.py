@@ -40,6 +40,23 @@ def test_davidson_subdiag_guess(cfg1):
     assert np.abs(res.evals - ev).max() < 1e-8
 
 
+def test_davidson_adc1_guess(cfg1):
+    """initvec_adc1: started from the lowest ADC(1) eigenvectors the GPU
+    Davidson reaches the oracle's eigenvalues (1e-8 Ha) in the same number of
+    iterations as the oracle started from the same block (the Ritz values
+    depend on the span only, so eigenvector signs do not matter)."""
+    from tests.conftest import system
+
+    g, ref = cfg1
+    e, eri = system(5, 19, 1234)
+    res = g.davdiag_block(6, 1e-8, ladc1guess=True)
+    G = oracle.adc1_guess(5, 19, e, eri, g.ndim, 12)
+    st, ev, _, info = ref.davidson(6, 1e-8, guess=G)
+    assert st == 0 and res.status == 0
+    assert np.abs(res.evals - ev).max() < 1e-8
+    assert abs(res.iterations - info["iterations"]) <= 1
+
+
 def test_davidson_nonconvergence_status(cfg1):
     from adc_ottawa_gb300 import AdcGpuError
 
