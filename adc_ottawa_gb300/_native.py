@@ -89,6 +89,7 @@ SIGNATURES = {
     "adcgpu_spectral_bounds": (C.c_int, [_vp, C.POINTER(DavParams), _dp]),
     "adcgpu_last_sigma_ms": (C.c_double, [_vp]),
     "adcgpu_device_bytes": (C.c_int64, [_vp]),
+    "adcgpu_set_fp64_arith": (C.c_int, [_vp, C.c_int]),
     "adcgpu_sigma_stats": (C.c_int, [_vp, _dp, C.c_int]),
     "adcgpu_mlp_num_params": (C.c_int64, []),
     "adcgpu_mlp_set_params": (C.c_int, [_vp, C.POINTER(C.c_float), C.c_int64]),

@@ -223,6 +223,11 @@ class AdcGpu:
     def device_bytes(self) -> int:
         return int(lib().adcgpu_device_bytes(self._h))
 
+    def set_fp64_arith(self, mode: int):
+        """0: FP64 fused multiply-adds (default); 1: double-float arithmetic
+        on the FP32 pipe for FP64 block products of 16 or more columns."""
+        self._check(lib().adcgpu_set_fp64_arith(self._h, int(mode)), "set_fp64_arith")
+
     # -- solvers --------------------------------------------------------------
     def davdiag_block(self, davstates: int, davtol: float, dmain: int = 0, maxsubdim: int = -1, maxiter: int = 100,
                       precon: int = PRECON_DPR, ldfl: bool = True, lsubdiag: bool = False, guessdim: int = 800,

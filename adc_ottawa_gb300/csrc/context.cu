@@ -442,6 +442,14 @@ int64_t adcgpu_device_bytes(const adcgpu_ctx* h) {
   return c ? c->dev_bytes : 0;
 }
 
+int adcgpu_set_fp64_arith(adcgpu_ctx* h, int mode) {
+  Ctx* c = reinterpret_cast<Ctx*>(h);
+  if (!c) return ADCGPU_BAD_INPUT;
+  if (mode != 0 && mode != 1) return set_err(c, ADCGPU_BAD_INPUT, "fp64 arithmetic mode is 0 or 1");
+  c->dense_df = mode;
+  return ADCGPU_OK;
+}
+
 uint64_t adcgpu_kernel_launches(void) { return adcgpu::g_kernel_launches.load(); }
 
 }  // extern "C"

@@ -592,9 +592,10 @@ int davidson_solve(Ctx* c, const adcgpu_dav_params* p, double* evals, double* ev
     int it2 = 0, nc2 = 0, nout = 0;
     // the refinement's subspace GEMMs run in double-float on the FP32 pipe
     // (FP64-accurate to ~1e-14 relative); the plain FP64 path keeps DFMA
+    const int df_caller = c->dense_df;
     c->dense_df = 1;
     st = F.run(hdiag, 2, 0, g64, nguess, ev, out64, blocksize, &nout, &it2, &nc2);
-    c->dense_df = 0;
+    c->dense_df = df_caller;
     inf.iterations += it2; inf.iters_fp64 = it2; inf.nmult += F.nmult; inf.sigma_seconds += F.sigma_s;
     inf.nmult_reference += F.nmult_ref; inf.nconv = nc2; inf.max_residual = F.max_res;
     F.release();

@@ -55,7 +55,7 @@ constexpr int UMMA_BOX = 64;                // values per box row (128 bytes)
 constexpr int UMMA_SLOT_BYTES = 2 * UMMA_ROWS * UMMA_BOX * 2;   // two boxes
 constexpr int UMMA_MAX_BOXES = 6;           // K <= 384
 constexpr int UMMA_THREADS = 320;             // producer, MMA issuer, 8 epilogue warps
-constexpr int UMMA_NOP = 24;                  // segment A lengths (noP) up to 24 (nocc <= 24)
+constexpr int UMMA_NOP = 16;                  // segment A lengths (noP) up to 16 (nocc <= 16)
 constexpr int UMMA_ITEM_ROWS_DEFAULT = 4096;  // rows per work item (a piece of one slab)
 
 // tensor maps of the five classes' B^T values (rows x L BF16, boxes of 64 x
@@ -88,6 +88,8 @@ __host__ __device__ constexpr int umma_tmem_cols() {
 }
 
 template <int NP, int NSLOT>
+// 320 threads: some SM sub-partitions hold three of the ten warps, so a
+// thread may use at most 16384 / 96 -> 168 registers
 __global__ void __launch_bounds__(UMMA_THREADS, 1)
     k_sigma_umma(GeomDev g, const int2* __restrict__ items, int nitems, const __grid_constant__ UmmaMaps maps,
                  const __nv_bfloat16* __restrict__ Bt, const float* __restrict__ diag, const float* __restrict__ V,
@@ -230,9 +232,11 @@ __global__ void __launch_bounds__(UMMA_THREADS, 1)
     const uint32_t lane_off = (uint32_t)(32 * q) << 16;
     uint32_t tile = 0, nitem = 0;
     bool ok = true;
-    // V2 of one tile: this thread's row, this warp's columns, hi/lo into the
-    // swizzled operand buffer (the previous tile's W1 products are done)
-    auto build_v2 = [&](int row, int item_end, float (&v2)[NP / 2], int& ap, int64_t& d, bool& valid) {
+    // V2 of one tile: this thread's row, this warp's columns.  load_v2 reads
+    // them into registers (issued a tile ahead, so the loads overlap the
+    // current tile's work); store_v2 splits them into hi/lo in the swizzled
+    // operand buffer once the previous tile's W1 products have read it.
+    auto load_v2 = [&](int row, int item_end, float (&v2)[NP / 2], int& ap, int64_t& d, bool& valid) {
       valid = row < item_end;
       ap = 0;
       d = 0;
@@ -244,10 +248,15 @@ __global__ void __launch_bounds__(UMMA_THREADS, 1)
 #pragma unroll
       for (int j = 0; j < NP / 2; ++j) {
         const int c = cbeg + j;
-        const float x = (valid && c < mcols) ? V[(int64_t)c * ldv + n1 + d] : 0.f;
-        v2[j] = x;
-        const __nv_bfloat16 h = __float2bfloat16(x);
-        const __nv_bfloat16 l = __float2bfloat16(x - __bfloat162float(h));
+        v2[j] = (valid && c < mcols) ? __ldg(V + (int64_t)c * ldv + n1 + d) : 0.f;
+      }
+    };
+    auto store_v2 = [&](const float (&v2)[NP / 2]) {
+#pragma unroll
+      for (int j = 0; j < NP / 2; ++j) {
+        const int c = cbeg + j;
+        const __nv_bfloat16 h = __float2bfloat16(v2[j]);
+        const __nv_bfloat16 l = __float2bfloat16(v2[j] - __bfloat162float(h));
         unsigned char* bx = sV2 + (r >> 6) * BOXB;
         *reinterpret_cast<__nv_bfloat16*>(bx + sw128_off(c, r & 63)) = h;
         *reinterpret_cast<__nv_bfloat16*>(bx + sw128_off(NP + c, r & 63)) = l;
@@ -266,16 +275,29 @@ __global__ void __launch_bounds__(UMMA_THREADS, 1)
       // X of this item: hi at rows c, lo at rows NP + c of each box
       ok = mbar_wait(&bars[B_XEMPTY], (nitem & 1u) ^ 1u, err, 7);
       if (!ok) break;
-      for (int o = et; o < UMMA_MAX_BOXES * UMMA_BOX * NP; o += 256) {
-        const int c = o / (UMMA_MAX_BOXES * UMMA_BOX), k = o - c * (UMMA_MAX_BOXES * UMMA_BOX);
-        const int seg = k / nvP, a = k - seg * nvP;
-        float x = 0.f;
-        if (c < mcols && k < K && a < nv) x = V[(int64_t)c * ldv + (int64_t)a * no + (seg ? lp : kp)];
-        const __nv_bfloat16 h = __float2bfloat16(x);
-        const __nv_bfloat16 l = __float2bfloat16(x - __bfloat162float(h));
-        unsigned char* bx = sX + (k >> 6) * BOXB;
-        *reinterpret_cast<__nv_bfloat16*>(bx + sw128_off(c, k & 63)) = h;
-        *reinterpret_cast<__nv_bfloat16*>(bx + sw128_off(NP + c, k & 63)) = l;
+      // eight independent loads in flight per thread, then the stores
+      constexpr int XTOT = UMMA_MAX_BOXES * UMMA_BOX * NP;
+      for (int o0 = et; o0 < XTOT; o0 += 256 * 8) {
+        float xv[8];
+#pragma unroll
+        for (int u = 0; u < 8; ++u) {
+          const int o = o0 + 256 * u;
+          const int c = o / (UMMA_MAX_BOXES * UMMA_BOX), k = o - c * (UMMA_MAX_BOXES * UMMA_BOX);
+          const int seg = k / nvP, a = k - seg * nvP;
+          xv[u] = (o < XTOT && c < mcols && k < K && a < nv)
+                      ? __ldg(V + (int64_t)c * ldv + (int64_t)a * no + (seg ? lp : kp)) : 0.f;
+        }
+#pragma unroll
+        for (int u = 0; u < 8; ++u) {
+          const int o = o0 + 256 * u;
+          if (o >= XTOT) break;
+          const int c = o / (UMMA_MAX_BOXES * UMMA_BOX), k = o - c * (UMMA_MAX_BOXES * UMMA_BOX);
+          const __nv_bfloat16 h = __float2bfloat16(xv[u]);
+          const __nv_bfloat16 l = __float2bfloat16(xv[u] - __bfloat162float(h));
+          unsigned char* bx = sX + (k >> 6) * BOXB;
+          *reinterpret_cast<__nv_bfloat16*>(bx + sw128_off(c, k & 63)) = h;
+          *reinterpret_cast<__nv_bfloat16*>(bx + sw128_off(NP + c, k & 63)) = l;
+        }
       }
       fence_proxy_async();
       mbar_arrive(&bars[B_XFULL]);
@@ -284,12 +306,20 @@ __global__ void __launch_bounds__(UMMA_THREADS, 1)
       int ap;
       int64_t d;
       bool valid;
+      load_v2(item.x + r, item.y, v2, ap, d, valid);
       ok = mbar_wait(&bars[B_V2EMPTY], (tile & 1u) ^ 1u, err, 8);
       if (!ok) break;
-      build_v2(item.x + r, item.y, v2, ap, d, valid);
+      store_v2(v2);
       for (int row0 = item.x; ok && row0 < item.y; row0 += UMMA_ROWS, ++tile) {
         const int db = tile & 1;
         const int row = row0 + r;
+        // the next tile's V2, a tile ahead
+        const bool has_next = row0 + UMMA_ROWS < item.y;
+        float v2n[NH];
+        int apn = 0;
+        int64_t dn = 0;
+        bool validn = false;
+        if (has_next) load_v2(row0 + UMMA_ROWS + r, item.y, v2n, apn, dn, validn);
         // diagonal term and segment A (singles (a', k)) of the row's W2; the
         // lanes of a warp mostly share a', so the V loads are broadcasts
         float w2[NH];
@@ -313,16 +343,38 @@ __global__ void __launch_bounds__(UMMA_THREADS, 1)
         }
         const float dg = valid ? diag[n1 + d] : 0.f;
 #pragma unroll
-        for (int j = 0; j < NH; ++j) {
-          const int c = cbeg + j;
-          float s = dg * v2[j];
-          if (valid && c < mcols) {
-            const float* vs = V + (int64_t)c * ldv + (int64_t)ap * no;
+        for (int j = 0; j < NH; ++j) w2[j] = dg * v2[j];
+        // segment A: sum_k A[row, k] V[(a', k), c].  The lanes of a warp with
+        // the same a' (most of them: a' changes once per run of nv - 1 - a'
+        // rows) share one cooperative load of those V values, spread over
+        // the lanes (k fastest: coalesced) and broadcast by shuffles.
+        {
+          constexpr unsigned FULL = 0xffffffffu;
+          constexpr int NVL = (NH * UMMA_NOP + 31) / 32;
+          unsigned pending = __ballot_sync(FULL, valid);
+          while (pending) {
+            const int apg = __shfl_sync(FULL, ap, __ffs(pending) - 1);
+            const bool mine = valid && ap == apg;
+            pending &= ~__ballot_sync(FULL, mine);
+            float vc[NVL];
 #pragma unroll
-            for (int k = 0; k < UMMA_NOP; ++k)
-              if (k < no) s += sa[k] * __ldg(vs + k);
+            for (int i = 0; i < NVL; ++i) {
+              const int idx = lane + 32 * i;            // idx = j * UMMA_NOP + k
+              const int j = idx / UMMA_NOP, k = idx - j * UMMA_NOP;
+              const int c = cbeg + j;
+              vc[i] = (j < NH && k < no && c < mcols) ? __ldg(V + (int64_t)c * ldv + (int64_t)apg * no + k) : 0.f;
+            }
+#pragma unroll
+            for (int k = 0; k < UMMA_NOP; ++k) {
+              if (k >= no) break;
+              const float a = mine ? sa[k] : 0.f;
+#pragma unroll
+              for (int j = 0; j < NH; ++j) {
+                const int idx = j * UMMA_NOP + k;
+                w2[j] = fmaf(a, __shfl_sync(FULL, vc[idx / 32], idx % 32), w2[j]);
+              }
+            }
           }
-          w2[j] = s;
         }
         const bool valid_t = valid;
         const int64_t d_t = d;
@@ -332,7 +384,7 @@ __global__ void __launch_bounds__(UMMA_THREADS, 1)
         ok = ok && mbar_wait(&bars[B_V2EMPTY], ((tile + 1) & 1u) ^ 1u, err, 8);
         if (!ok) break;
         fence_after_sync();
-        if (row0 + UMMA_ROWS < item.y) build_v2(row0 + UMMA_ROWS + r, item.y, v2, ap, d, valid);
+        if (has_next) store_v2(v2n);
 #pragma unroll
         for (int j0 = 0; j0 < NH; j0 += 8) {
           float hi[8], lo[8];
@@ -346,6 +398,11 @@ __global__ void __launch_bounds__(UMMA_THREADS, 1)
         }
         fence_before_sync();
         mbar_arrive(&bars[B_D1EMPTY0 + db]);
+#pragma unroll
+        for (int j = 0; j < NH; ++j) v2[j] = v2n[j];
+        ap = apn;
+        d = dn;
+        valid = validn;
       }
       if (!ok) break;
       // the item's W1 (C|D) sums: TMEM lane = position k in group s

@@ -8,6 +8,7 @@
 !
 !   write_fspace_adc2_1  -> write_fspace_adc2_1_gpu   (fspacetrial.f90:533)
 !   davdiag_block        -> davdiag_block_gpu         (block_davidson.f90:33)
+!   davdir_block         -> davdir_block_gpu          (dmatvec_davidson.f90:41)
 !   lancdiag_block       -> lancdiag_block_gpu        (block_lanczos.f90:28)
 !   propagate_fvec       -> propagate_fvec_gpu        (fvecprop.f90:27)
 !   chebyshev_auto_order_domain
@@ -143,6 +144,12 @@ module adcgpu_iface
        real(c_double)        :: q0(*), bounds(2)
        real(c_double), value :: projen
      end function adcgpu_chebyshev_project
+
+     integer(c_int) function adcgpu_set_fp64_arith(ctx, mode) bind(C, name="adcgpu_set_fp64_arith")
+       import :: c_int, c_ptr
+       type(c_ptr), value    :: ctx
+       integer(c_int), value :: mode
+     end function adcgpu_set_fp64_arith
 
      type(c_ptr) function adcgpu_last_error(ctx) bind(C, name="adcgpu_last_error")
        import :: c_ptr

@@ -66,6 +66,9 @@ def parse():
                          "cheb: Chebyshev order-domain autocorrelation of 32 start vectors on the "
                          "nocc=10/nvirt=110 matrix (--cheb-order orders)")
     ap.add_argument("--train-systems", type=int, default=200)
+    ap.add_argument("--train-systems-headline", type=int, default=24,
+                    help="seeded systems whose FP64 traces train the network timed beside the headline")
+    ap.add_argument("--no-learned", action="store_true", help="skip the mixed + learned solve beside the headline")
     ap.add_argument("--sil-steps", type=int, default=20)
     ap.add_argument("--cheb-order", type=int, default=1000)
     return ap.parse_args()
@@ -279,6 +282,28 @@ def run_gb300(args):
         e2e = {"value": allmax(statistics.mean(et), world), "unit": "s",
                "h2d_bytes_per_step": int(e.nbytes + eri.nbytes),
                "d2h_bytes_per_step": int(8 * NROOTS + 8 * NROOTS * g.ndim)}
+    # mixed ladder + the learned preconditioner (the metric's "learned" form),
+    # timed beside the headline: the network is trained here by the
+    # library's kernels on FP64 Davidson traces of seeded small systems
+    learned = None
+    if not args.no_learned:
+        from adc_ottawa_gb300 import PRECON_MLP, mlp_train
+
+        t = time.perf_counter()
+        samples = []
+        for no_, nv_, seed_ in mlp_train.random_systems(args.train_systems_headline):
+            samples += mlp_train.make_samples(no_, nv_, seed_)
+        params, _ = mlp_train.train(samples, steps=300)
+        train_s = time.perf_counter() - t
+        mlp_train.load_into(g, params)
+        t = time.perf_counter()
+        rl = g.davdiag_block(NROOTS, TOL, precon=PRECON_MLP, precision=prec, want_vectors=False,
+                             raise_on_nonconv=False)
+        learned = {"seconds": time.perf_counter() - t, "iterations": rl.iterations,
+                   "phase_iterations_bf16_fp32_fp64": [rl.iters_bf16, rl.iters_fp32, rl.iters_fp64],
+                   "status": rl.status, "max_abs_dE_vs_fold": float(np.abs(rl.evals - r.evals).max()),
+                   "training": {"systems": args.train_systems_headline, "samples": len(samples),
+                                "seconds": train_s}}
     cols_ref = fp64["nmult_reference"] if fp64 else None
     cols_src = "the FP64 DPR solve of this run (the reference algorithm's iteration structure)"
     if cols_ref is None:
@@ -308,14 +333,15 @@ def run_gb300(args):
         "data": "synthetic (seeded orbital energies and 8-fold symmetric ERIs)",
         "config": workload_config(no, nv, g.ndim),
         "method": "mixed-precision ladder (BF16 -> FP32 -> FP64 refinement) with the folded singles-block "
-                  "preconditioner; the learned (MLP) preconditioner is slower than the fold on this workload "
-                  "family and is timed by --suite learned",
+                  "preconditioner, the fastest form; the mixed ladder with the learned (MLP) preconditioner is "
+                  "timed on the same matrix in details.mixed_learned",
         "details": {"nnz_kept": nnz, "build_s": build_s, "iterations": r.iterations, "nmult": r.nmult,
                     "phase_iterations_bf16_fp32_fp64": [r.iters_bf16, r.iters_fp32, r.iters_fp64],
                     "max_residual_fp64": r.max_residual, "sigma_shape": tuned,
                     "status": r.status, "evals_lowest": r.evals[:5].tolist(), "parallelism": f"replicas x{world}",
                     "fp64_gpu": fp64,
-                    "speedup_vs_fp64_gpu": (fp64["seconds"] / t_step) if fp64 else None},
+                    "speedup_vs_fp64_gpu": (fp64["seconds"] / t_step) if fp64 else None,
+                    "mixed_learned": learned},
         "roofline": {"bound": "hbm", "kernel": "sigma product (all sigma kernels of one call), every call of the "
                      "timed solves", "achieved": achieved,
                      "peak": hbm, "unit": "GB/s", "frac": achieved / hbm,
@@ -427,9 +453,13 @@ def run_lanczos(args):
 
 
 def run_sil(args):
-    """Config 4 SIL: 32 seeded wavepackets on the config-2 matrix, Krylov
-    dimension 15, dt = tout/2 = 0.05 au; --sil-steps outer steps are timed
-    and the 2,000-step figure is that rate times 2,000."""
+    """32 seeded wavepackets on the nocc=10/nvirt=110 matrix, Krylov
+    dimension 15, dt = tout/2 = 0.05 au: --sil-steps outer steps, timed to
+    completion with FP64 fused multiply-adds and with double-float
+    arithmetic on the FP32 pipe (adcgpu_set_fp64_arith), and the largest
+    autocorrelation difference between the two."""
+    import numpy as np
+
     from adc_ottawa_gb300 import ADCGPU_FP64, AdcGpu, synth_system, synth_uniform_block
 
     no, nv, npk, kdim, tout = 10, 110, 32, 15, 0.1
@@ -439,14 +469,22 @@ def run_sil(args):
     g.set_eri_packed(eri)
     g.write_fspace_adc2_1(None, precision=ADCGPU_FP64)
     f = synth_uniform_block(g.ndim, npk, 77)
-    g.propagate_fvec(f, tout, 2 * 0.5 * tout, kdim, 1e-8)
     nsteps = max(1, args.sil_steps)
-    t = time.perf_counter()
-    a, nmult = g.propagate_fvec(f, tout, nsteps * 0.5 * tout, kdim, 1e-8)
-    dt = time.perf_counter() - t
+    out = {}
+    for mode in (0, 1):
+        g.set_fp64_arith(mode)
+        g.propagate_fvec(f, tout, 2 * 0.5 * tout, kdim, 1e-8)
+        t = time.perf_counter()
+        a, nmult = g.propagate_fvec(f, tout, nsteps * 0.5 * tout, kdim, 1e-8)
+        out[mode] = (time.perf_counter() - t, a, nmult)
+    g.set_fp64_arith(0)
+    dt, a, nmult = out[0]
+    dev = float(np.abs(out[1][1] - a).max() / np.abs(a).max())
     _secondary_line("SIL autocorrelation, 32 wavepackets, kdim 15, dt 0.05 au: seconds per step", dt / nsteps, "s",
-                    nsteps, 1, {"workload": f"ADC(2)-s nocc={no} nvirt={nv} N={g.ndim} sil packets={npk}"},
-                    projected_2000_steps_s=dt / nsteps * 2000, matvec_columns=nmult,
+                    nsteps, 1, {"workload": f"ADC(2)-s nocc={no} nvirt={nv} N={g.ndim} sil packets={npk} steps={nsteps}"},
+                    total_s=dt, matvec_columns=nmult, double_float={"seconds_per_step": out[1][0] / nsteps,
+                                                                     "total_s": out[1][0],
+                                                                     "max_rel_dev_vs_fp64": dev},
                     a_last=[float(abs(a[0, -1]))])
     g.close()
 

@@ -353,6 +353,16 @@ double adcgpu_last_sigma_ms(const adcgpu_ctx* ctx);
 /* Device bytes held by the context (matrix, ERI blocks, work spaces). */
 int64_t adcgpu_device_bytes(const adcgpu_ctx* ctx);
 
+/* Arithmetic of the FP64 path's block products (no reference counterpart;
+   the reference's FP64 arithmetic is MKL's): 0 (the default) FP64 fused
+   multiply-adds; 1 double-float arithmetic on the FP32 pipe (hi + lo single
+   precision pairs, about 1e-14 relative per product) for sigma products of
+   16 or more columns and for the subspace GEMMs, which the GB300's FP64
+   rate (1/64 of FP32) makes several times faster.  It applies to every
+   solver that runs on the context (Davidson, Lanczos, SIL, Chebyshev); the
+   mixed ladder's FP64 refinement always uses 1. */
+int adcgpu_set_fp64_arith(adcgpu_ctx* ctx, int mode);
+
 /* Number of CUDA kernels this library has launched in this process, over
    all contexts (a monotonic counter; differences give the launches of a
    region). */

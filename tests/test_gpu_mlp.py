@@ -103,11 +103,13 @@ def test_trained_network_gain_over_dpr(gpu, capsys):
     """What the trained network gains over the diagonal preconditioner it
     replaces: trained by the library's kernels on residual -> correction
     pairs from FP64 Davidson traces of 24 seeded systems, then run on 4
-    held-out systems.  The network must converge to the same eigenvalues;
-    the measured iteration ratio (learned / diagonal) is printed and may not
-    exceed 1.15.  On these synthetic ADC(2)-s matrices a per-configuration
-    scaling of the diagonal correction gains little: the residual error sits
-    in the singles-doubles coupling, which ADCGPU_PRECON_FOLD addresses."""
+    held-out systems.  The network must converge to the same eigenvalues in
+    fewer iterations than the diagonal preconditioner (a strict gain; the
+    measured ratio learned / diagonal is printed: 138 / 144 on a GB300).  On
+    these synthetic ADC(2)-s matrices a per-configuration scaling of the
+    diagonal correction gains little: the residual error sits in the
+    singles-doubles coupling, which ADCGPU_PRECON_FOLD addresses.  The loss
+    must fall over the training run."""
     from adc_ottawa_gb300 import mlp_train
 
     samples = []
@@ -115,7 +117,7 @@ def test_trained_network_gain_over_dpr(gpu, capsys):
         samples += mlp_train.make_samples(no, nv, seed)
     params, losses = mlp_train.train(samples, steps=300)
     assert np.isfinite(losses).all()
-    assert losses[-30:].mean() <= losses[:30].mean() + 0.02
+    assert losses[-30:].mean() < losses[:30].mean()
     rows = mlp_train.evaluate(params, mlp_train.random_systems(4, seed=99991))
     it_dpr = sum(r["iters_dpr"] for r in rows)
     it_mlp = sum(r["iters_mlp"] for r in rows)
@@ -125,4 +127,4 @@ def test_trained_network_gain_over_dpr(gpu, capsys):
     for r in rows:
         assert r["status"] == [0, 0]
         assert r["max_dE"] < 1e-8
-    assert it_mlp <= 1.15 * it_dpr
+    assert it_mlp < it_dpr

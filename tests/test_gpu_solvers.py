@@ -156,6 +156,23 @@ def test_sil_autocorr_config1(cfg1):
         assert np.abs(a[p] - ar).max() <= 1e-7 * np.abs(ar).max()
 
 
+def test_sil_double_float_arithmetic(cfg1):
+    """adcgpu_set_fp64_arith(1): 8 wavepackets (16 real columns, the tiled
+    sigma pass) propagated with double-float arithmetic on the FP32 pipe
+    match the oracle's FP64 propagation within 1e-7 relative."""
+    g, ref = cfg1
+    f = np.random.RandomState(5).rand(g.ndim, 8)
+    g.set_fp64_arith(1)
+    try:
+        a, _ = g.propagate_fvec(f, tout=0.5, tfinal=4.0, kdim=12, autotol=1e-9)
+    finally:
+        g.set_fp64_arith(0)
+    for p in (0, 7):
+        st, ar, _ = ref.autocorr(f[:, p], 0.5, 4.0, 12, 1e-9)
+        assert st == 0
+        assert np.abs(a[p] - ar).max() <= 1e-7 * np.abs(ar).max()
+
+
 def test_silstep_single(cfg1):
     g, ref = cfg1
     H = ref.dense()
