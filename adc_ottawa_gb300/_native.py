@@ -61,6 +61,10 @@ SIGNATURES = {
     "adcgpu_eri_packed_size": (C.c_int64, [C.c_int]),
     "adcgpu_synth_eri_packed": (C.c_int, [C.c_int, C.c_uint64, _dp, C.c_int]),
     "adcgpu_synth_uniform_block": (C.c_int, [C.c_int64, C.c_int, C.c_uint64, _dp]),
+    "adcgpu_synth_dipole": (C.c_int, [C.c_int, C.c_uint64, _dp]),
+    "adcgpu_set_dipole": (C.c_int, [_vp, _dp]),
+    "adcgpu_modified_tm_adc2": (C.c_int, [_vp, C.c_int, _ip, _dp]),
+    "adcgpu_fill_stvc": (C.c_int, [C.c_int, _dp, C.c_int, _ip]),
     "adcgpu_adc2s_dim": (C.c_int64, [C.c_int, C.c_int, _ip]),
     "adcgpu_select_adc2s": (C.c_int, [C.c_int, C.c_int, _ip]),
     "adcgpu_ctx_create": (C.c_int, [C.c_int, C.POINTER(_vp)]),

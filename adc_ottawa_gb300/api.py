@@ -80,6 +80,54 @@ def synth_uniform_block(nrow: int, ncol: int, seed: int) -> np.ndarray:
     return out
 
 
+def synth_dipole(nbas: int, seed: int) -> np.ndarray:
+    """Seeded synthetic dipole matrix dpl (nbas x nbas, symmetric, column-major)."""
+    d = np.empty((nbas, nbas), order="F")
+    st = lib().adcgpu_synth_dipole(nbas, seed, ptr(d))
+    if st:
+        raise AdcGpuError(st, "synth_dipole")
+    return d
+
+
+def fill_stvc(vctr: np.ndarray, lmain: int) -> np.ndarray:
+    """fill_stvc (fspacetrial.f90:1255-1270): 1-based indices of the lmain
+    largest vctr**2, in dsortindxa1('D') order."""
+    v = np.ascontiguousarray(vctr, np.float64)
+    out = np.zeros(lmain, np.int32)
+    st = lib().adcgpu_fill_stvc(len(v), ptr(v), lmain, ptr(out, _ip))
+    if st:
+        raise AdcGpuError(st, "fill_stvc")
+    return out
+
+
+def lanczos_guess_vecs(mtm: np.ndarray, n1: int, lmain: int, lancguess: int = 1) -> np.ndarray:
+    """The final-space Lanczos start block from the f-vector
+    (lanczos_guess_vecs, adc2_opa.f90:380-520, and init_vec_unit /
+    init_vec_1h1p2h2p, block_lanczos.f90:201-289), ADC(2)-s:
+
+    - lancguess 1: unit vectors on the lmain singles with the largest f^2;
+    - lancguess 3: (e_k1 +- e_k2)/sqrt(2) pairing the i-th largest single k1
+      with the i-th largest double k2, '+' when f(k1) > 0 and f(k2) > 0.
+    """
+    mtm = np.asarray(mtm, np.float64)
+    ndim = len(mtm)
+    Q = np.zeros((ndim, lmain), order="F")
+    if lancguess == 1:
+        for i, k in enumerate(fill_stvc(mtm[:n1], lmain)):
+            Q[k - 1, i] = 1.0
+    elif lancguess == 3:
+        i1 = fill_stvc(mtm[:n1], lmain)
+        i2 = n1 + fill_stvc(mtm[n1:], lmain)
+        fac = 1.0 / np.sqrt(2.0)
+        for i in range(lmain):
+            k1, k2 = int(i1[i]), int(i2[i])
+            Q[k1 - 1, i] = fac
+            Q[k2 - 1, i] = fac if (mtm[k1 - 1] > 0 and mtm[k2 - 1] > 0) else -fac
+    else:
+        raise AdcGpuError(12, "lanczos_guess_vecs: lancguess 1 or 3 (ADC(2)-s)")
+    return Q
+
+
 def adc2s_dim(nocc: int, nvirt: int):
     cnt = np.zeros(5, np.int32)
     n = lib().adcgpu_adc2s_dim(nocc, nvirt, ptr(cnt, _ip))
@@ -250,6 +298,25 @@ class AdcGpu:
         return DavidsonResult(ev, vec, st, info.iterations, info.nmult, info.nconv, info.seconds, info.sigma_seconds,
                               info.max_residual, info.iters_bf16, info.iters_fp32, info.iters_fp64,
                               info.nmult_reference)
+
+    # -- dipole start vectors --------------------------------------------------------
+    def set_dipole(self, dpl: np.ndarray):
+        """The dipole matrix dpl (nbas x nbas) of one component in the MO basis."""
+        d = np.asfortranarray(dpl, np.float64)
+        nb = self.nocc + self.nvirt
+        if d.shape != (nb, nb):
+            raise AdcGpuError(12, f"set_dipole: dpl must be {nb} x {nb}")
+        self._check(lib().adcgpu_set_dipole(self._h, ptr(d)), "set_dipole")
+
+    def get_modifiedtm_adc2(self, kpq: np.ndarray | None = None) -> np.ndarray:
+        """get_modifiedtm_adc2 (get_moment.f90:153-442): the f-vector
+        <Psi_J|D|Psi_0> over the ADC(2)-s intermediate states."""
+        ndim, _ = adc2s_dim(self.nocc, self.nvirt)
+        kp = None if kpq is None else np.ascontiguousarray(kpq, np.int32)
+        mtm = np.empty(ndim)
+        self._check(lib().adcgpu_modified_tm_adc2(self._h, ndim, None if kp is None else ptr(kp, _ip), ptr(mtm)),
+                    "get_modifiedtm_adc2")
+        return mtm
 
     def lancdiag_block(self, q0: np.ndarray, ncycles: int, orthotype: int = 0, want_tmat: bool = True,
                        want_evals: bool = True, want_ritz: bool = False):

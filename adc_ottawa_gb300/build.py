@@ -39,6 +39,7 @@ SOURCES = [
     ("sil.cu", []),
     ("chebyshev.cu", []),
     ("mlp.cu", []),
+    ("fvec.cu", ["--fmad=false"]),
 ]
 
 

@@ -43,8 +43,17 @@ __host__ __device__ inline int64_t canon(int64_t p, int64_t q, int64_t r, int64_
   return pq >= rs ? pq * (pq + 1) / 2 + rs : rs * (rs + 1) / 2 + pq;
 }
 
+// (P, Q) with P >= Q from the triangular index t = P(P+1)/2 + Q.
+__host__ __device__ inline void untri(int64_t t, int64_t& P, int64_t& Q) {
+  P = (int64_t)((sqrt(8.0 * (double)t + 1.0) - 1.0) * 0.5);
+  while (P * (P + 1) / 2 > t) --P;
+  while ((P + 1) * (P + 2) / 2 <= t) ++P;
+  Q = t - P * (P + 1) / 2;
+}
+
 // Gather one ERI block from the canonical packed array.
-// kind 0: (a i|b j) 1: (a b|i j) 2: (i j|k a) 3: (a b|i c)
+// kind 0: (a i|b j) 1: (a b|i j) 2: (i j|k a) 3: (a b|i c) 4: (i j|k l)
+// 5: (a c|b d) packed over virtual pairs, index tri(pair(a,c), pair(b,d))
 __global__ void k_gather_block(const double* __restrict__ packed, double* __restrict__ out, int kind,
                                int no, int nv, int64_t total) {
   for (int64_t t = blockIdx.x * (int64_t)blockDim.x + threadIdx.x; t < total;
@@ -52,6 +61,11 @@ __global__ void k_gather_block(const double* __restrict__ packed, double* __rest
     int64_t x = t;
     int p, q, r, s;
     switch (kind) {
+      case 4: { int l = x % no; x /= no; int k = x % no; x /= no; int j = x % no; int i = (int)(x / no);
+                p = i; q = j; r = k; s = l; } break;
+      case 5: { int64_t P, Q, a, c, b, d;
+                untri(x, P, Q); untri(P, a, c); untri(Q, b, d);
+                p = no + (int)a; q = no + (int)c; r = no + (int)b; s = no + (int)d; } break;
       case 0: { int j = x % no; x /= no; int b = x % nv; x /= nv; int i = x % no; int a = (int)(x / no);
                 p = no + a; q = i; r = no + b; s = j; } break;
       case 1: { int j = x % no; x /= no; int i = x % no; x /= no; int b = x % nv; int a = (int)(x / nv);
@@ -461,10 +475,12 @@ inline int grid_for(const Ctx* c, int64_t n, int block) {
 
 int build_eri_blocks_from_packed(Ctx* c, const double* d_packed) {
   const int no = c->geom.no, nv = c->geom.nv;
-  const int64_t sz[4] = {(int64_t)nv * no * nv * no, (int64_t)nv * nv * no * no,
-                         (int64_t)no * no * no * nv, (int64_t)nv * nv * no * nv};
-  double** dst[4] = {&c->d_vovo, &c->d_vvoo, &c->d_ooov, &c->d_vvov};
-  for (int k = 0; k < 4; ++k) {
+  const int64_t npv = (int64_t)nv * (nv + 1) / 2;
+  const int64_t sz[6] = {(int64_t)nv * no * nv * no, (int64_t)nv * nv * no * no,
+                         (int64_t)no * no * no * nv, (int64_t)nv * nv * no * nv,
+                         (int64_t)no * no * no * no, npv * (npv + 1) / 2};
+  double** dst[6] = {&c->d_vovo, &c->d_vvoo, &c->d_ooov, &c->d_vvov, &c->d_oooo, &c->d_vvvv};
+  for (int k = 0; k < 6; ++k) {
     if (*dst[k]) { dfree(c, *dst[k], 0); *dst[k] = nullptr; }
     int st = dmalloc(c, (void**)dst[k], sizeof(double) * sz[k]);
     if (st) return st;

@@ -84,7 +84,7 @@ static void free_matrix(Ctx* c) {
 }
 
 static void free_eri(Ctx* c) {
-  double** ps[] = {&c->d_vovo, &c->d_vvoo, &c->d_ooov, &c->d_vvov};
+  double** ps[] = {&c->d_vovo, &c->d_vvoo, &c->d_ooov, &c->d_vvov, &c->d_oooo, &c->d_vvvv};
   for (double** p : ps) {
     dfree(c, *p);
     *p = nullptr;
@@ -139,6 +139,7 @@ int adcgpu_ctx_destroy(adcgpu_ctx* h) {
   free_mlp(c);
   dfree(c, c->d_e);
   dfree(c, c->d_sil);
+  dfree(c, c->d_dpl);
   cudaEventDestroy(c->ev0);
   cudaEventDestroy(c->ev1);
   if (c->st_ev0) cudaEventDestroy(c->st_ev0);
@@ -163,6 +164,8 @@ int adcgpu_set_orbitals(adcgpu_ctx* h, int nocc, int nvirt, const double* e) {
   if (g.N > INT32_MAX) return set_err(c, ADCGPU_UNSUPPORTED, "ADC(2) dimension exceeds int32 kpq indexing");
   free_matrix(c);
   free_eri(c);
+  dfree(c, c->d_dpl);
+  c->d_dpl = nullptr;
   c->geom = g;
   c->e.assign(e, e + nocc + nvirt);
   dfree(c, c->d_e);
@@ -205,16 +208,29 @@ int adcgpu_set_eri_mo_complex(adcgpu_ctx* h, const double* buf) {
   auto V = [&](int64_t r, int64_t s, int64_t u, int64_t v) {
     return buf[2 * (((v * n + u) * n + s) * n + r)];
   };
-  const int64_t sz[4] = {(int64_t)nv * no * nv * no, (int64_t)nv * nv * no * no, (int64_t)no * no * no * nv,
-                         (int64_t)nv * nv * no * nv};
-  double** dst[4] = {&c->d_vovo, &c->d_vvoo, &c->d_ooov, &c->d_vvov};
-  for (int k = 0; k < 4; ++k) {
+  const int64_t npv = (int64_t)nv * (nv + 1) / 2;
+  const int64_t sz[6] = {(int64_t)nv * no * nv * no, (int64_t)nv * nv * no * no, (int64_t)no * no * no * nv,
+                         (int64_t)nv * nv * no * nv, (int64_t)no * no * no * no, npv * (npv + 1) / 2};
+  double** dst[6] = {&c->d_vovo, &c->d_vvoo, &c->d_ooov, &c->d_vvov, &c->d_oooo, &c->d_vvvv};
+  // (P, Q), P >= Q, of the triangular index t = P(P+1)/2 + Q
+  auto untri = [](int64_t t, int64_t& P, int64_t& Q) {
+    P = (int64_t)((std::sqrt(8.0 * (double)t + 1.0) - 1.0) * 0.5);
+    while (P * (P + 1) / 2 > t) --P;
+    while ((P + 1) * (P + 2) / 2 <= t) ++P;
+    Q = t - P * (P + 1) / 2;
+  };
+  for (int k = 0; k < 6; ++k) {
     std::vector<double> hb(sz[k]);
 #pragma omp parallel for schedule(static)
     for (int64_t t = 0; t < sz[k]; ++t) {
       int64_t x = t;
       int64_t p, q, r, s;
       switch (k) {
+        case 4: { int64_t l = x % no; x /= no; int64_t kk = x % no; x /= no; int64_t j = x % no; int64_t i = x / no;
+                  p = i; q = j; r = kk; s = l; } break;
+        case 5: { int64_t P, Q, a, cc, b, d;
+                  untri(x, P, Q); untri(P, a, cc); untri(Q, b, d);
+                  p = no + a; q = no + cc; r = no + b; s = no + d; } break;
         case 0: { int64_t j = x % no; x /= no; int64_t b = x % nv; x /= nv; int64_t i = x % no; int64_t a = x / no;
                   p = no + a; q = i; r = no + b; s = j; } break;
         case 1: { int64_t j = x % no; x /= no; int64_t i = x % no; x /= no; int64_t b = x % nv; int64_t a = x / nv;
@@ -276,6 +292,34 @@ int adcgpu_build_adc2s(adcgpu_ctx* h, int ndim, const int32_t* kpq, int64_t* nof
   c->have_matrix = true;
   if (noffd_out) *noffd_out = c->nnz_kept;
   return ADCGPU_OK;
+}
+
+int adcgpu_set_dipole(adcgpu_ctx* h, const double* dpl) {
+  Ctx* c = reinterpret_cast<Ctx*>(h);
+  CTX_CHECK(c);
+  if (!c->have_orb) return set_err(c, ADCGPU_BAD_INPUT, "set orbitals first");
+  if (!dpl) return set_err(c, ADCGPU_BAD_INPUT, "null dipole matrix");
+  const int64_t nb = c->geom.no + c->geom.nv;
+  if (!c->d_dpl) ST(dmalloc(c, (void**)&c->d_dpl, sizeof(double) * nb * nb));
+  ADC_CUDA(c, h2d(c, c->d_dpl, dpl, sizeof(double) * nb * nb));
+  return ADCGPU_OK;
+}
+
+int adcgpu_modified_tm_adc2(adcgpu_ctx* h, int ndim, const int32_t* kpq, double* mtm) {
+  Ctx* c = reinterpret_cast<Ctx*>(h);
+  CTX_CHECK(c);
+  if (!c->have_orb || !c->have_eri) return set_err(c, ADCGPU_BAD_INPUT, "orbitals and ERIs must be set");
+  if (!c->d_dpl) return set_err(c, ADCGPU_BAD_INPUT, "set the dipole matrix first (adcgpu_set_dipole)");
+  if (ndim != c->geom.N || !mtm) return set_err(c, ADCGPU_BAD_INPUT, "ndim does not match nocc/nvirt");
+  std::vector<int32_t> ref((size_t)7 * (ndim + 1));
+  adcgpu_select_adc2s(c->geom.no, c->geom.nv, ref.data());
+  if (kpq) {
+    for (size_t i = 0; i < ref.size(); ++i)
+      if (ref[i] != kpq[i] && !(i >= 5 && i < 7))
+        return set_err(c, ADCGPU_UNSUPPORTED,
+                       "kpq is not the C1 ADC(2)-s list of select_atom_is/select_atom_d (flag -1)");
+  }
+  return modified_tm_adc2(c, ndim, ref.data(), mtm);
 }
 
 int adcgpu_get_diag(adcgpu_ctx* h, double* hii) {

@@ -261,6 +261,9 @@ struct Ctx {
   double* d_vvoo = nullptr;       // (a b|i j) [nv][nv][no][no]
   double* d_ooov = nullptr;       // (i j|k a) [no][no][no][nv]
   double* d_vvov = nullptr;       // (a b|i c) [nv][nv][no][nv]
+  double* d_oooo = nullptr;       // (i j|k l) [no][no][no][no]
+  double* d_vvvv = nullptr;       // (a c|b d) over virtual pairs: [tri(pair(a,c), pair(b,d))]
+  double* d_dpl = nullptr;        // dipole matrix dpl(p,q) [nbas][nbas] (q-major), adcgpu_set_dipole
   // matrix
   double* d_diag = nullptr;       // hii [N]
   double* d_A = nullptr;          // ph-ph block, n1 x n1 dense symmetric (0 where |h|<=minc)
@@ -361,6 +364,10 @@ int build_adc1_matrix(Ctx* c, double* d_M);
 // from offset vbase on; kept-entry counts per row into rowcount (may be null)
 int coupling_values(Ctx* c, double* buf, int64_t vbase, int64_t row0, int64_t row1, int64_t* rowcount);
 int export_coo_device(Ctx* c, double* d_h, int32_t* d_oi, int32_t* d_oj);
+
+// fvec.cu : the ADC(2) f-vector (get_modifiedtm_adc2) of the dipole matrix
+// d_dpl over kpq columns 1..ndim (kpq validated by the caller); mtm on the host
+int modified_tm_adc2(Ctx* c, int64_t ndim, const int32_t* kpq, double* mtm);
 
 // sigma.cu : W = H V for m columns (column-major, leading dim ld), FP64 or FP32.
 struct SigmaPlan {

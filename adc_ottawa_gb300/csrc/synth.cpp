@@ -63,7 +63,7 @@ inline double normal01(uint64_t key, uint64_t counter) {
   }
 }
 
-enum : uint64_t { PURPOSE_OCC = 1, PURPOSE_VIRT = 2, PURPOSE_ERI = 3, PURPOSE_BLOCK = 4 };
+enum : uint64_t { PURPOSE_OCC = 1, PURPOSE_VIRT = 2, PURPOSE_ERI = 3, PURPOSE_BLOCK = 4, PURPOSE_DIPOLE = 5 };
 
 }  // namespace
 
@@ -121,6 +121,19 @@ extern "C" int adcgpu_synth_uniform_block(int64_t nrow, int ncol, uint64_t seed,
   if (nrow <= 0 || ncol <= 0 || !out) return ADCGPU_BAD_INPUT;
   const uint64_t key = stream_key(seed, PURPOSE_BLOCK);
   for (int64_t k = 0; k < nrow * (int64_t)ncol; ++k) out[k] = uniform01(key, (uint64_t)k);
+  return ADCGPU_OK;
+}
+
+extern "C" int adcgpu_synth_dipole(int nbas, uint64_t seed, double* dpl) {
+  if (nbas <= 0 || !dpl) return ADCGPU_BAD_INPUT;
+  const uint64_t key = stream_key(seed, PURPOSE_DIPOLE);
+  for (int p = 0; p < nbas; ++p)
+    for (int q = 0; q <= p; ++q) {
+      const uint64_t idx = (uint64_t)p * (p + 1) / 2 + q;
+      const double x = normal01(key, idx) * 0.5 * adcsynth::exp_series(-0.1 * (p - q));
+      dpl[(size_t)q * nbas + p] = x;
+      dpl[(size_t)p * nbas + q] = x;
+    }
   return ADCGPU_OK;
 }
 

@@ -98,6 +98,13 @@ int adcgpu_synth_eri_packed(int nbas, uint64_t seed, double* eri, int nthreads);
    (the random_number draws of init_vecs_random, block_lanczos.f90:402-439). */
 int adcgpu_synth_uniform_block(int64_t nrow, int ncol, uint64_t seed, double* out);
 
+/* Dipole matrix dpl(p,q) of one Cartesian component in the MO basis (the
+   reference reads it from the GAMESS dipole integrals into the global dpl,
+   source/qclib/load_electronic_structure.f90): nbas x nbas, column-major,
+   symmetric, one draw per p>=q (1-based):
+   N(0,1) * 0.5 * exp(-0.1|p-q|). */
+int adcgpu_synth_dipole(int nbas, uint64_t seed, double* dpl);
+
 /* ---------------------------------------------------------------------------
  * Configuration list kpq (select_atom_is select_fano.f90:16-60 and
  * select_atom_d flag -1 select_fano.f90:539-718; C1 symmetry, no frozen core).
@@ -153,6 +160,30 @@ int adcgpu_export_coo(adcgpu_ctx* ctx, int64_t cap, double* h, int32_t* oi,
    with the reference's Fortran unformatted sequential record layout
    (filetools.f90:24-44, buf_size = 655360). */
 int adcgpu_write_hmlt_files(adcgpu_ctx* ctx, const char* dir, char flag);
+
+/* ---------------------------------------------------------------------------
+ * Dipole start vectors.
+ * ------------------------------------------------------------------------- */
+
+/* The dipole matrix dpl(p,q) of one component in the MO basis (the module
+   array dpl that dipole_ph.f90 reads): nbas x nbas, column-major.  Held on
+   the device until the orbitals change or the context is destroyed. */
+int adcgpu_set_dipole(adcgpu_ctx* ctx, const double* dpl);
+
+/* get_modifiedtm_adc2(ndim,kpq,mtm,ista), get_moment.f90:153-442: the
+   ADC(2) f-vector mtm(J) = <Psi_J|D|Psi_0> over the ADC(2)-s intermediate
+   states (kpq as for adcgpu_build_adc2s; NULL = that list), from the
+   orbitals, ERIs and dipole matrix of the context.  It is the start vector
+   of the final-space Lanczos (lanczos_guess_vecs, adc2_opa.f90:380-520),
+   of the wavepacket propagation (init_wavepacket, fvecprop.f90:338-357)
+   and of the Chebyshev autocorrelation (adc2_autospec.f90:162).  FP64;
+   mtm: host array of ndim doubles. */
+int adcgpu_modified_tm_adc2(adcgpu_ctx* ctx, int ndim, const int32_t* kpq, double* mtm);
+
+/* fill_stvc(ndim,vctr), fspacetrial.f90:1255-1270: the indices (1-based) of
+   the lmain largest vctr(i)^2 in the order of dsortindxa1('D')
+   (misc.f90:492+), the unit start vectors of lancguess = 1. */
+int adcgpu_fill_stvc(int ndim, const double* vctr, int lmain, int32_t* stvc_lbl);
 
 /* ---------------------------------------------------------------------------
  * Sigma-vector product W = H V for m columns (hxvec_incore,

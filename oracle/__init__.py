@@ -86,6 +86,10 @@ def lib():
         L.orc_synth_uniform_block.restype = C.c_int
         L.orc_adc2s_dim.argtypes = [C.c_int, C.c_int, _ip]
         L.orc_adc2s_dim.restype = C.c_int64
+        L.orc_synth_dipole.argtypes = [C.c_int, C.c_uint64, _dp]
+        L.orc_synth_dipole.restype = C.c_int
+        L.orc_modified_tm_adc2.argtypes = [C.c_int, C.c_int, _dp, _dp, _dp, C.c_int64, _ip, _dp, C.c_int]
+        L.orc_modified_tm_adc2.restype = C.c_int
         _lib = L
     return _lib
 
@@ -109,6 +113,27 @@ def synth_uniform_block(nrow: int, ncol: int, seed: int) -> np.ndarray:
     out = np.empty((nrow, ncol), order="F")
     assert lib().orc_synth_uniform_block(nrow, ncol, seed, _p(out)) == 0
     return out
+
+
+def synth_dipole(nbas: int, seed: int) -> np.ndarray:
+    """The seeded synthetic dipole matrix dpl (nbas x nbas, symmetric)."""
+    d = np.empty((nbas, nbas), order="F")
+    assert lib().orc_synth_dipole(nbas, seed, _p(d)) == 0
+    return d
+
+
+def modified_tm_adc2(no: int, nv: int, e, eri, dpl, sections: int = 3) -> np.ndarray:
+    """get_modifiedtm_adc2's f-vector over the ADC(2)-s configuration list
+    (get_moment.f90:153-442), FP64 in the reference's loop and expression
+    order.  sections: 1 = singles only, 2 = doubles only, 3 = both."""
+    kpq = select(no, nv)
+    ndim = kpq.shape[0] - 1
+    e = np.ascontiguousarray(e, np.float64)
+    eri = np.ascontiguousarray(eri, np.float64)
+    dpl = np.asfortranarray(dpl, np.float64)
+    mtm = np.zeros(ndim)
+    assert lib().orc_modified_tm_adc2(no, nv, _p(e), _p(eri), _p(dpl), ndim, _p(kpq, _ip), _p(mtm), sections) == 0
+    return mtm
 
 
 def adc2s_dim(no: int, nv: int) -> int:
