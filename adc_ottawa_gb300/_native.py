@@ -65,6 +65,9 @@ SIGNATURES = {
     "adcgpu_set_dipole": (C.c_int, [_vp, _dp]),
     "adcgpu_modified_tm_adc2": (C.c_int, [_vp, C.c_int, _ip, _dp]),
     "adcgpu_fill_stvc": (C.c_int, [C.c_int, _dp, C.c_int, _ip]),
+    "adcgpu_cvs_dim": (C.c_int64, [C.c_int, C.c_int, C.c_int, _ip, _ip]),
+    "adcgpu_select_adc2s_cvs": (C.c_int, [C.c_int, C.c_int, C.c_int, _ip, _ip]),
+    "adcgpu_build_adc2s_cvs": (C.c_int, [_vp, C.c_int, _ip, C.c_int, _ip, _i64p, C.c_char]),
     "adcgpu_adc2s_dim": (C.c_int64, [C.c_int, C.c_int, _ip]),
     "adcgpu_select_adc2s": (C.c_int, [C.c_int, C.c_int, _ip]),
     "adcgpu_ctx_create": (C.c_int, [C.c_int, C.POINTER(_vp)]),

@@ -80,6 +80,25 @@ def synth_uniform_block(nrow: int, ncol: int, seed: int) -> np.ndarray:
     return out
 
 
+def cvs_dim(nocc: int, nvirt: int, core) -> int:
+    """Dimension of the CVS space of the core orbitals (1-based occupied indices)."""
+    core = np.ascontiguousarray(core, np.int32)
+    n = int(lib().adcgpu_cvs_dim(nocc, nvirt, len(core), ptr(core, _ip), None))
+    if n <= 0:
+        raise AdcGpuError(12, "cvs_dim: 0 < ncore < nocc distinct occupied orbitals")
+    return n
+
+
+def select_adc2s_cvs(nocc: int, nvirt: int, core) -> np.ndarray:
+    """select_atom_is_cvs + select_atom_d_cvs: the CVS kpq as (ndim+1, 7) int32."""
+    core = np.ascontiguousarray(core, np.int32)
+    kpq = np.zeros((cvs_dim(nocc, nvirt, core) + 1, 7), np.int32)
+    st = lib().adcgpu_select_adc2s_cvs(nocc, nvirt, len(core), ptr(core, _ip), ptr(kpq, _ip))
+    if st:
+        raise AdcGpuError(st, "select_adc2s_cvs")
+    return kpq
+
+
 def synth_dipole(nbas: int, seed: int) -> np.ndarray:
     """Seeded synthetic dipole matrix dpl (nbas x nbas, symmetric, column-major)."""
     d = np.empty((nbas, nbas), order="F")
@@ -223,10 +242,27 @@ class AdcGpu:
     # -- builder --------------------------------------------------------------
     def write_fspace_adc2_1(self, kpq: np.ndarray | None = None, chr: str = "i", precision: int = ADCGPU_FP64) -> int:
         """Build H on the device; returns noffdel (kept off-diagonal count)."""
+        self.ndim = adc2s_dim(self.nocc, self.nvirt)[0]
         noff = C.c_int64(0)
         kp = None if kpq is None else ptr(np.ascontiguousarray(kpq, np.int32), _ip)
         self._check(lib().adcgpu_build_adc2s(self._h, self.ndim, kp, C.byref(noff), chr.encode(), precision),
                     "write_fspace_adc2_1")
+        self.noffd = int(noff.value)
+        return self.noffd
+
+    def write_fspace_adc2_1_cvs(self, core, kpq: np.ndarray | None = None, chr: str = "i") -> int:
+        """write_fspace_adc2_1_cvs (fspacetrial.f90:566-596): build the CVS
+        matrix of the core orbitals (1-based occupied indices) on the device,
+        FP64; returns noffdel.  The solvers then work in the CVS space
+        (self.ndim becomes its dimension)."""
+        core = np.ascontiguousarray(core, np.int32)
+        ndim = cvs_dim(self.nocc, self.nvirt, core)
+        noff = C.c_int64(0)
+        kp = None if kpq is None else np.ascontiguousarray(kpq, np.int32)
+        self._check(lib().adcgpu_build_adc2s_cvs(self._h, ndim, None if kp is None else ptr(kp, _ip), len(core),
+                                                 ptr(core, _ip), C.byref(noff), chr.encode()),
+                    "write_fspace_adc2_1_cvs")
+        self.ndim = ndim
         self.noffd = int(noff.value)
         return self.noffd
 
@@ -310,8 +346,9 @@ class AdcGpu:
 
     def get_modifiedtm_adc2(self, kpq: np.ndarray | None = None) -> np.ndarray:
         """get_modifiedtm_adc2 (get_moment.f90:153-442): the f-vector
-        <Psi_J|D|Psi_0> over the ADC(2)-s intermediate states."""
-        ndim, _ = adc2s_dim(self.nocc, self.nvirt)
+        <Psi_J|D|Psi_0> over the ADC(2)-s intermediate states, or over the
+        CVS states of a CVS kpq."""
+        ndim = adc2s_dim(self.nocc, self.nvirt)[0] if kpq is None else len(kpq) - 1
         kp = None if kpq is None else np.ascontiguousarray(kpq, np.int32)
         mtm = np.empty(ndim)
         self._check(lib().adcgpu_modified_tm_adc2(self._h, ndim, None if kp is None else ptr(kp, _ip), ptr(mtm)),

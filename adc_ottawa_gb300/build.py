@@ -40,6 +40,7 @@ SOURCES = [
     ("chebyshev.cu", []),
     ("mlp.cu", []),
     ("fvec.cu", ["--fmad=false"]),
+    ("cvs.cu", []),
 ]
 
 

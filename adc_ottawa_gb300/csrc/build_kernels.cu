@@ -397,6 +397,122 @@ __global__ void k_coupling(Eri E, GeomDev g, double* __restrict__ Bt, int64_t vb
   }
 }
 
+// CVS build ------------------------------------------------------------------
+// ph-ph block of the core singles (get_offdiag_adc2_save_cvs_omp, get_matrix.f90
+// :1452-1478) and their diagonal (get_diag_adc2_save :286-294).  The element
+// (i, j < i) is evaluated with row i's indices first, as the reference's loop
+// (j = 1..i-1) does; CC_ph_ph is the same serial sum over (c, i) as k_phph.
+// sidx[i] is the ADC(2)-s single index of CVS single i.
+__global__ void k_phph_cvs(Eri E, const double* __restrict__ e, const double* __restrict__ X,
+                           const double* __restrict__ D1, const double* __restrict__ ca,
+                           const double* __restrict__ cb, const int32_t* __restrict__ sidx, int cn1,
+                           double* __restrict__ Ac, double* __restrict__ hii, unsigned long long* __restrict__ kept) {
+  const int no = E.no, nv = E.nv;
+  const int64_t n1 = (int64_t)no * nv;
+  for (int64_t t = blockIdx.x * (int64_t)blockDim.x + threadIdx.x; t < (int64_t)cn1 * cn1;
+       t += (int64_t)gridDim.x * blockDim.x) {
+    const int i = (int)(t / cn1), j = (int)(t % cn1);
+    if (j > i) continue;
+    const int64_t s1 = sidx[i], s2 = sidx[j];
+    const int a = (int)(s1 / no), k = (int)(s1 % no), a1 = (int)(s2 / no), k1 = (int)(s2 % no);
+    const double hv = 0.5 * (e[k] + e[k1] - e[no + a] - e[no + a1]);
+    double cc = 0.0;
+    for (int64_t u = 0; u < n1; ++u) {
+      const double eic = e[u % no] - e[no + u / no];
+      const double DC = (hv + eic) / (D1[s1 * n1 + u] * D1[s2 * n1 + u]);
+      double term = X[s1 * n1 + u] * X[s2 * n1 + u];
+      term = term * DC;
+      cc = cc + term;
+    }
+    if (i == j) {
+      double x = e[no + a] - e[k];                                   // K_ph_ph
+      x = x + (2.0 * E.VOVO(a, k, a, k) - E.VVOO(a, a, k, k));       // C1_ph_ph
+      x = x + ca[(int64_t)a * nv + a];
+      x = x + cb[k * no + k];
+      x = x + cc;
+      hii[i] = x;
+      Ac[(int64_t)i * cn1 + i] = x;
+      continue;
+    }
+    double x = 2.0 * E.VOVO(a, k, a1, k1) - E.VVOO(a, a1, k, k1);
+    if (k == k1) x = x + ca[(int64_t)a * nv + a1];
+    if (a == a1) x = x + cb[k * no + k1];
+    x = x + cc;
+    const double keep = fabs(x) > MINC ? x : 0.0;
+    Ac[(int64_t)i * cn1 + j] = keep;
+    Ac[(int64_t)j * cn1 + i] = keep;
+    if (keep != 0.0) atomicAdd(kept, 1ull);
+  }
+}
+
+// A CVS double row from its kpq column (7 int32: cnf, spin, k, l, a, b, type;
+// 1-based orbitals); type 3, 4, 5 map to the classes a=b,i<j / 4I / 4II.
+__device__ inline Double cvs_row(const int32_t* q, int no) {
+  Double r;
+  r.kp = q[2] - 1; r.lp = q[3] - 1;
+  r.ap = q[4] - no - 1; r.bp = q[5] - no - 1;
+  r.cls = q[6] - 1;
+  return r;
+}
+
+// Candidate e of a CVS double row: the core singles that the coincidence
+// tests of C1/C2/C3_ph_2p2h can reach, (a',k), (b',k) for core k, then
+// (a,k') and (a,l') for the core one of k', l' (a not in {a',b'}).  Returns
+// the CVS single index a*ncore + corepos[k], or -1.
+__device__ inline int cvs_candidate(const Double& r, int e, int nv, int ncore, const int* __restrict__ corepos,
+                                    const int* __restrict__ coreorb, int& a, int& k) {
+  if (e < ncore) { a = r.ap; k = coreorb[e]; }
+  else if (e < 2 * ncore) { if (r.ap == r.bp) return -1; a = r.bp; k = coreorb[e - ncore]; }
+  else if (e < 2 * ncore + nv) { a = e - 2 * ncore; k = r.kp; if (corepos[k] < 0 || a == r.ap || a == r.bp) return -1; }
+  else { a = e - 2 * ncore - nv; k = r.lp; if (corepos[k] < 0 || a == r.ap || a == r.bp) return -1; }
+  return a * ncore + corepos[k];
+}
+
+// One warp per CVS double row: count (FILL = false) or write (FILL = true)
+// the kept coupling entries (|x| > minc, get_matrix.f90:1503-1620).
+template <bool FILL>
+__global__ void k_cvs_coupling(Eri E, const int32_t* __restrict__ cols, int64_t n2, int ncore,
+                               const int* __restrict__ corepos, const int* __restrict__ coreorb,
+                               int64_t* __restrict__ rowcnt, const int64_t* __restrict__ rowptr,
+                               int32_t* __restrict__ ccol, double* __restrict__ cval) {
+  const int lane = threadIdx.x & 31;
+  const int no = E.no, nv = E.nv;
+  const int L = 2 * ncore + 2 * nv;
+  const int64_t warp = (blockIdx.x * (int64_t)blockDim.x + threadIdx.x) >> 5;
+  const int64_t nwarps = ((int64_t)gridDim.x * blockDim.x) >> 5;
+  for (int64_t row = warp; row < n2; row += nwarps) {
+    const Double r = cvs_row(cols + 7 * row, no);
+    int cnt = 0;
+    int64_t base = FILL ? rowptr[row] : 0;
+    for (int e0 = 0; e0 < L; e0 += 32) {
+      const int e = e0 + lane;
+      int a = 0, k = 0, j = -1;
+      double x = 0.0;
+      if (e < L) j = cvs_candidate(r, e, nv, ncore, corepos, coreorb, a, k);
+      if (j >= 0) x = coupling(E, a, k, r);
+      const bool keep = j >= 0 && fabs(x) > MINC;
+      const unsigned m = __ballot_sync(0xffffffffu, keep);
+      if (FILL && keep) {
+        const int64_t o = base + __popc(m & ((1u << lane) - 1));
+        ccol[o] = j;
+        cval[o] = x;
+      }
+      base += __popc(m);
+      cnt += __popc(m);
+    }
+    if (!FILL && lane == 0) rowcnt[row] = cnt;
+  }
+}
+
+// K_2p2h_2p2h of the CVS doubles (get_diag_adc2_save :298-301)
+__global__ void k_cvs_diag2(const int32_t* __restrict__ cols, int64_t n2, int no, const double* __restrict__ e,
+                            double* __restrict__ hii) {
+  for (int64_t t = blockIdx.x * (int64_t)blockDim.x + threadIdx.x; t < n2; t += (int64_t)gridDim.x * blockDim.x) {
+    const Double r = cvs_row(cols + 7 * t, no);
+    hii[t] = e[no + r.ap] + e[no + r.bp] - e[r.kp] - e[r.lp];
+  }
+}
+
 // COO export -----------------------------------------------------------------
 __global__ void k_count_phph_rows(const double* __restrict__ A, int n1, int64_t* __restrict__ cnt) {
   int s1 = blockIdx.x;
@@ -612,6 +728,98 @@ int export_coo_device(Ctx* c, double* d_h, int32_t* d_oi, int32_t* d_oj) {
   dfree(c, d_tmp, tmp_bytes);
   dfree(c, d_pos, sizeof(int64_t) * (nrows + 1));
   return ADCGPU_OK;
+}
+
+
+int build_matrix_cvs(Ctx* c, const int32_t* kpq, int64_t ndim, int ncore, const int32_t* core) {
+  const Geometry& G = c->geom;
+  const int no = G.no, nv = G.nv;
+  const int64_t n1 = G.n1;
+  const int cn1 = kpq[0];
+  const int64_t n2 = ndim - cn1;
+  Eri E{c->d_vovo, c->d_vvoo, c->d_ooov, c->d_vvov, no, nv};
+  cudaStream_t s = c->stream;
+  std::vector<int> corepos(no, -1), coreorb(ncore);
+  {
+    // core holes in hcentre (ascending) order, the order of the CVS singles
+    std::vector<int> sorted(core, core + ncore);
+    std::sort(sorted.begin(), sorted.end());
+    for (int i = 0; i < ncore; ++i) { coreorb[i] = sorted[i] - 1; corepos[sorted[i] - 1] = i; }
+  }
+  std::vector<int32_t> sidx(cn1);
+  for (int i = 0; i < cn1; ++i) {
+    const int32_t* q = kpq + 7 * (i + 1);
+    sidx[i] = (q[4] - no - 1) * no + (q[2] - 1);
+  }
+  double *d_ca = nullptr, *d_cb = nullptr, *d_X = nullptr, *d_D1 = nullptr;
+  int32_t *d_sidx = nullptr, *d_cols = nullptr;
+  int *d_corepos = nullptr, *d_coreorb = nullptr;
+  unsigned long long* d_kept = nullptr;
+  int64_t* d_cnt = nullptr;
+  void* d_tmp = nullptr;
+  size_t tmp_bytes = 0;
+  auto cleanup = [&]() {
+    dfree(c, d_ca); dfree(c, d_cb); dfree(c, d_X); dfree(c, d_D1); dfree(c, d_sidx); dfree(c, d_cols);
+    dfree(c, d_corepos); dfree(c, d_coreorb); dfree(c, d_kept); dfree(c, d_cnt); dfree(c, d_tmp);
+  };
+  auto run = [&]() -> int {
+    ST(dmalloc(c, (void**)&d_ca, sizeof(double) * nv * nv));
+    ST(dmalloc(c, (void**)&d_cb, sizeof(double) * no * no));
+    ST(dmalloc(c, (void**)&d_X, sizeof(double) * n1 * n1));
+    ST(dmalloc(c, (void**)&d_D1, sizeof(double) * n1 * n1));
+    ST(dmalloc(c, (void**)&d_sidx, sizeof(int32_t) * cn1));
+    ST(dmalloc(c, (void**)&d_cols, sizeof(int32_t) * 7 * std::max<int64_t>(n2, 1)));
+    ST(dmalloc(c, (void**)&d_corepos, sizeof(int) * no));
+    ST(dmalloc(c, (void**)&d_coreorb, sizeof(int) * ncore));
+    ST(dmalloc(c, (void**)&d_kept, sizeof(unsigned long long)));
+    ST(dmalloc(c, (void**)&d_cnt, sizeof(int64_t) * (n2 + 1)));
+    ST(dmalloc(c, (void**)&c->d_diag, sizeof(double) * ndim));
+    ST(dmalloc(c, (void**)&c->d_Ac, sizeof(double) * (size_t)cn1 * cn1));
+    ST(dmalloc(c, (void**)&c->d_crow, sizeof(int64_t) * (n2 + 1)));
+    ADC_CUDA(c, cudaMemsetAsync(d_kept, 0, sizeof(unsigned long long), s));
+    ADC_CUDA(c, cudaMemsetAsync(d_cnt, 0, sizeof(int64_t) * (n2 + 1), s));
+    ADC_CUDA(c, cudaMemsetAsync(c->d_Ac, 0, sizeof(double) * (size_t)cn1 * cn1, s));
+    ADC_CUDA(c, cudaMemcpyAsync(d_sidx, sidx.data(), sizeof(int32_t) * cn1, cudaMemcpyHostToDevice, s));
+    ADC_CUDA(c, cudaMemcpyAsync(d_corepos, corepos.data(), sizeof(int) * no, cudaMemcpyHostToDevice, s));
+    ADC_CUDA(c, cudaMemcpyAsync(d_coreorb, coreorb.data(), sizeof(int) * ncore, cudaMemcpyHostToDevice, s));
+    if (n2 > 0)
+      ADC_CUDA(c, cudaMemcpyAsync(d_cols, kpq + 7 * (cn1 + 1), sizeof(int32_t) * 7 * n2, cudaMemcpyHostToDevice, s));
+    k_ca<<<(int)((nv * (int64_t)nv + 127) / 128), 128, 0, s>>>(E, c->d_e, d_ca); ADC_COUNT_LAUNCH();
+    k_cb<<<(no * no + 63) / 64, 64, 0, s>>>(E, c->d_e, d_cb); ADC_COUNT_LAUNCH();
+    k_cc_tables<false><<<grid_for(c, n1 * n1, 256), 256, 0, s>>>(E, c->d_e, d_X, d_D1); ADC_COUNT_LAUNCH();
+    k_phph_cvs<<<grid_for(c, (int64_t)cn1 * cn1, 128), 128, 0, s>>>(E, c->d_e, d_X, d_D1, d_ca, d_cb, d_sidx, cn1,
+                                                                     c->d_Ac, c->d_diag, d_kept);
+    ADC_COUNT_LAUNCH();
+    k_cvs_diag2<<<grid_for(c, n2, 256), 256, 0, s>>>(d_cols, n2, no, c->d_e, c->d_diag + cn1); ADC_COUNT_LAUNCH();
+    k_cvs_coupling<false><<<c->nsm * 8, 256, 0, s>>>(E, d_cols, n2, ncore, d_corepos, d_coreorb, d_cnt, nullptr,
+                                                      nullptr, nullptr);
+    ADC_COUNT_LAUNCH();
+    ADC_CUDA(c, cudaGetLastError());
+    cub::DeviceScan::ExclusiveSum(nullptr, tmp_bytes, d_cnt, c->d_crow, n2 + 1, s);
+    ST(dmalloc(c, &d_tmp, tmp_bytes));
+    cub::DeviceScan::ExclusiveSum(d_tmp, tmp_bytes, d_cnt, c->d_crow, n2 + 1, s);
+    int64_t nnz = 0;
+    unsigned long long kept_ph = 0;
+    ADC_CUDA(c, cudaMemcpyAsync(&nnz, c->d_crow + n2, sizeof(int64_t), cudaMemcpyDeviceToHost, s));
+    ADC_CUDA(c, cudaMemcpyAsync(&kept_ph, d_kept, sizeof(kept_ph), cudaMemcpyDeviceToHost, s));
+    ADC_CUDA(c, cudaStreamSynchronize(s));
+    ST(dmalloc(c, (void**)&c->d_ccol, sizeof(int32_t) * std::max<int64_t>(nnz, 1)));
+    ST(dmalloc(c, (void**)&c->d_cval, sizeof(double) * std::max<int64_t>(nnz, 1)));
+    k_cvs_coupling<true><<<c->nsm * 8, 256, 0, s>>>(E, d_cols, n2, ncore, d_corepos, d_coreorb, nullptr, c->d_crow,
+                                                     c->d_ccol, c->d_cval);
+    ADC_COUNT_LAUNCH();
+    ADC_CUDA(c, cudaGetLastError());
+    ADC_CUDA(c, cudaStreamSynchronize(s));
+    c->cvs_n1 = cn1;
+    c->cvs_N = ndim;
+    c->cvs_nnz = nnz;
+    c->nnz_ph = (int64_t)kept_ph;
+    c->nnz_kept = (int64_t)kept_ph + nnz;
+    return ADCGPU_OK;
+  };
+  int st = run();
+  cleanup();
+  return st;
 }
 
 }  // namespace adcgpu

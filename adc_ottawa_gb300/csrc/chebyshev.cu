@@ -245,7 +245,7 @@ static int cheb_check(Ctx* c, int nvec, const void* q0, const double* bounds, in
 // block.  The subspace columns of H come from the sigma product of unit
 // vectors, 64 at a time, so the stored matrix is never exported.
 static int singlesubspace_block(Ctx* c, int b, std::vector<double>& q0) {
-  const int64_t N = c->geom.N;
+  const int64_t N = mat_dim(c);
   std::vector<double> hii(N), neg(N);
   ADC_CUDA(c, cudaMemcpyAsync(hii.data(), c->d_diag, sizeof(double) * N, cudaMemcpyDeviceToHost, c->stream));
   ADC_CUDA(c, cudaStreamSynchronize(c->stream));
@@ -311,7 +311,7 @@ extern "C" int adcgpu_chebyshev_auto(adcgpu_ctx* h, int nvec, const double* q0, 
   ST(cheb_check(c, nvec, q0, bounds, chebyord));
   if (!auto_out) return set_err(c, ADCGPU_BAD_INPUT, "auto_out required");
   const int ord = chebyord - chebyord % 2;   // chebyshev_initialise (:136)
-  const int64_t N = c->geom.N, n1 = c->geom.n1;
+  const int64_t N = mat_dim(c), n1 = mat_n1(c);
   ChebGPU G;
   G.c = c; G.N = N; G.P = nvec; G.ord = ord;
   ST(G.alloc(false, n1, q1h1p != nullptr));
@@ -353,7 +353,7 @@ extern "C" int adcgpu_chebyshev_project(adcgpu_ctx* h, int nvec, double* q0, con
   cudaSetDevice(c->device);
   ST(cheb_check(c, nvec, q0, bounds, chebyord));
   const int ord = chebyord - chebyord % 2;
-  const int64_t N = c->geom.N;
+  const int64_t N = mat_dim(c);
   // project_psi0 (:420-446): escale, the Jackson damping g_k and the
   // step-function coefficients f_k, with the reference's expression order
   const double pi = 3.1415926535897932;   // constants.f90:8
@@ -391,7 +391,7 @@ extern "C" int adcgpu_spectral_bounds(adcgpu_ctx* h, const adcgpu_dav_params* fp
   cudaSetDevice(c->device);
   if (!c->have_matrix) return set_err(c, ADCGPU_NO_MATRIX, "build the matrix first");
   if (!bounds) return set_err(c, ADCGPU_BAD_INPUT, "bounds required");
-  if (c->geom.N < 200) return set_err(c, ADCGPU_BAD_INPUT, "the Lanczos estimate needs ndim >= 200 (2 x 100 vectors)");
+  if (mat_dim(c) < 200) return set_err(c, ADCGPU_BAD_INPUT, "the Lanczos estimate needs ndim >= 200 (2 x 100 vectors)");
   // lower bound: one-root block Davidson (specbounds.f90:151-176).  The
   // reference sets davstates_f, dmain_f, maxsubdim_f, davtol_f and
   // lsubdiag_f; maxiter, precon, ldfl and guessdim stay the caller's

@@ -78,6 +78,7 @@ static void free_matrix(Ctx* c) {
   }
   c->ws_bytes = 0;
   free_sigma_plan(c);
+  free_cvs(c);
   c->have_matrix = false;
   c->direct = 0;
   c->dchunks.clear();
@@ -310,23 +311,77 @@ int adcgpu_modified_tm_adc2(adcgpu_ctx* h, int ndim, const int32_t* kpq, double*
   CTX_CHECK(c);
   if (!c->have_orb || !c->have_eri) return set_err(c, ADCGPU_BAD_INPUT, "orbitals and ERIs must be set");
   if (!c->d_dpl) return set_err(c, ADCGPU_BAD_INPUT, "set the dipole matrix first (adcgpu_set_dipole)");
-  if (ndim != c->geom.N || !mtm) return set_err(c, ADCGPU_BAD_INPUT, "ndim does not match nocc/nvirt");
+  if (!mtm) return set_err(c, ADCGPU_BAD_INPUT, "null mtm");
+  if (ndim == c->geom.N) {
+    std::vector<int32_t> ref((size_t)7 * (ndim + 1));
+    adcgpu_select_adc2s(c->geom.no, c->geom.nv, ref.data());
+    if (kpq) {
+      for (size_t i = 0; i < ref.size(); ++i)
+        if (ref[i] != kpq[i] && !(i >= 5 && i < 7))
+          return set_err(c, ADCGPU_UNSUPPORTED,
+                         "kpq is not the C1 ADC(2)-s list of select_atom_is/select_atom_d (flag -1)");
+    }
+    return modified_tm_adc2(c, ndim, ref.data(), mtm);
+  }
+  // a CVS list: its core orbitals are the holes of its singles
+  if (!kpq || kpq[1] != 0 || kpq[2] != 0 || kpq[0] <= 0 || kpq[0] % c->geom.nv != 0)
+    return set_err(c, ADCGPU_BAD_INPUT, "ndim matches neither the ADC(2)-s nor a CVS list (kpq required)");
+  std::vector<int32_t> core;
+  for (int i = 1; i <= kpq[0] / c->geom.nv; ++i) core.push_back(kpq[7 * i + 2]);
+  int32_t cnt[5];
+  if (adcgpu_cvs_dim(c->geom.no, c->geom.nv, (int)core.size(), core.data(), cnt) != ndim)
+    return set_err(c, ADCGPU_BAD_INPUT, "ndim does not match the CVS list");
   std::vector<int32_t> ref((size_t)7 * (ndim + 1));
-  adcgpu_select_adc2s(c->geom.no, c->geom.nv, ref.data());
+  adcgpu_select_adc2s_cvs(c->geom.no, c->geom.nv, (int)core.size(), core.data(), ref.data());
+  for (size_t i = 0; i < ref.size(); ++i)
+    if (ref[i] != kpq[i] && !(i >= 5 && i < 7))
+      return set_err(c, ADCGPU_UNSUPPORTED, "kpq is not a C1 CVS list of select_atom_is_cvs/select_atom_d_cvs");
+  return modified_tm_adc2(c, ndim, ref.data(), mtm);
+}
+
+int adcgpu_build_adc2s_cvs(adcgpu_ctx* h, int ndim, const int32_t* kpq, int ncore, const int32_t* core,
+                           int64_t* noffd_out, char flag) {
+  Ctx* c = reinterpret_cast<Ctx*>(h);
+  CTX_CHECK(c);
+  if (!c->have_orb || !c->have_eri) return set_err(c, ADCGPU_BAD_INPUT, "orbitals and ERIs must be set");
+  int32_t cnt[5];
+  const int64_t nd = adcgpu_cvs_dim(c->geom.no, c->geom.nv, ncore, core, cnt);
+  if (nd <= 0) return set_err(c, ADCGPU_BAD_INPUT, "core: 0 < ncore < nocc distinct occupied orbitals (1-based)");
+  if (ndim != nd) return set_err(c, ADCGPU_BAD_INPUT, "ndim does not match the CVS space of the core orbitals");
+  std::vector<int32_t> ref((size_t)7 * (ndim + 1));
+  if (adcgpu_select_adc2s_cvs(c->geom.no, c->geom.nv, ncore, core, ref.data()) != ADCGPU_OK)
+    return set_err(c, ADCGPU_BAD_INPUT, "CVS configuration list");
   if (kpq) {
     for (size_t i = 0; i < ref.size(); ++i)
       if (ref[i] != kpq[i] && !(i >= 5 && i < 7))
         return set_err(c, ADCGPU_UNSUPPORTED,
-                       "kpq is not the C1 ADC(2)-s list of select_atom_is/select_atom_d (flag -1)");
+                       "kpq is not the C1 CVS list of select_atom_is_cvs/select_atom_d_cvs for these core orbitals");
   }
-  return modified_tm_adc2(c, ndim, ref.data(), mtm);
+  free_matrix(c);
+  int st = build_matrix_cvs(c, ref.data(), ndim, ncore, core);
+  if (st) { free_matrix(c); return st; }
+  c->cvs = 1;
+  c->cvs_kpq = std::move(ref);
+  c->precision = ADCGPU_FP64;
+  {
+    std::vector<double> ah((size_t)ndim);
+    ADC_CUDA(c, d2h(c, ah.data(), c->d_diag, sizeof(double) * ah.size()));
+    c->diag_order_thread = std::thread([c, ah = std::move(ah)]() mutable {
+      for (double& x : ah) x = std::fabs(x);
+      host_heapsort_index((int64_t)ah.size(), ah.data(), c->diag_order);
+    });
+  }
+  c->flag = flag;
+  c->have_matrix = true;
+  if (noffd_out) *noffd_out = c->nnz_kept;
+  return ADCGPU_OK;
 }
 
 int adcgpu_get_diag(adcgpu_ctx* h, double* hii) {
   Ctx* c = reinterpret_cast<Ctx*>(h);
   CTX_CHECK(c);
   if (!c->have_matrix) return set_err(c, ADCGPU_NO_MATRIX, "no matrix");
-  ADC_CUDA(c, d2h(c, hii, c->d_diag, sizeof(double) * c->geom.N));
+  ADC_CUDA(c, d2h(c, hii, c->d_diag, sizeof(double) * mat_dim(c)));
   return ADCGPU_OK;
 }
 
@@ -345,7 +400,7 @@ int adcgpu_export_coo(adcgpu_ctx* h, int64_t cap, double* hv, int32_t* oi, int32
   if ((st = dmalloc(c, (void**)&d_j, sizeof(int32_t) * n))) {
     dfree(c, d_h, sizeof(double) * n); dfree(c, d_i, sizeof(int32_t) * n); return st;
   }
-  st = export_coo_device(c, d_h, d_i, d_j);
+  st = c->cvs ? export_coo_cvs(c, d_h, d_i, d_j) : export_coo_device(c, d_h, d_i, d_j);
   if (!st) {
     d2h(c, hv, d_h, sizeof(double) * n);
     d2h(c, oi, d_i, sizeof(int32_t) * n);
@@ -375,7 +430,7 @@ int adcgpu_write_hmlt_files(adcgpu_ctx* h, const char* dir, char flag) {
   CTX_CHECK(c);
   if (!c->have_matrix) return set_err(c, ADCGPU_NO_MATRIX, "no matrix");
   if (c->direct) return set_err(c, ADCGPU_UNSUPPORTED, "the direct path stores no coupling block");
-  const int64_t n = c->nnz_kept, N = c->geom.N;
+  const int64_t n = c->nnz_kept, N = mat_dim(c);
   std::vector<double> hv(n), diag(N);
   std::vector<int32_t> oi(n), oj(n);
   int st = adcgpu_export_coo(h, n, hv.data(), oi.data(), oj.data());
@@ -426,7 +481,7 @@ int adcgpu_sigma_device(adcgpu_ctx* h, int m, const void* dv, void* dw, int64_t 
   Ctx* c = reinterpret_cast<Ctx*>(h);
   CTX_CHECK(c);
   if (!c->have_matrix) return set_err(c, ADCGPU_NO_MATRIX, "no matrix");
-  if (m <= 0 || ld < c->geom.N || !dv || !dw) return set_err(c, ADCGPU_BAD_INPUT, "sigma arguments");
+  if (m <= 0 || ld < mat_dim(c) || !dv || !dw) return set_err(c, ADCGPU_BAD_INPUT, "sigma arguments");
   ADC_CUDA(c, cudaEventRecord(c->ev0, c->stream));
   int st = c->precision == ADCGPU_MIXED
                ? sigma_fp32(c, m, (const float*)dv, ld, (float*)dw, ld)
@@ -445,7 +500,7 @@ int adcgpu_sigma(adcgpu_ctx* h, int m, const double* v, double* w) {
   CTX_CHECK(c);
   if (!c->have_matrix) return set_err(c, ADCGPU_NO_MATRIX, "no matrix");
   if (m <= 0 || !v || !w) return set_err(c, ADCGPU_BAD_INPUT, "sigma arguments");
-  const int64_t N = c->geom.N;
+  const int64_t N = mat_dim(c);
   const size_t n = (size_t)N * m;
   int st;
   if (c->precision == ADCGPU_FP64) {

@@ -524,9 +524,16 @@ template struct DavidsonGPU<float>;
 int davidson_solve(Ctx* c, const adcgpu_dav_params* p, double* evals, double* evecs, adcgpu_dav_info* info,
                    const MlpPrecond* mlp) {
   const double t_start = now_s();
-  const int64_t N = c->geom.N;
+  const int64_t N = mat_dim(c);
   int nstates = p->davstates;
   if (nstates <= 0 || nstates > N) return set_err(c, ADCGPU_BAD_INPUT, "davstates");
+  if (c->cvs) {
+    // the CVS matrix is FP64 with the reference's own preconditioners and guess
+    if (p->precision != ADCGPU_FP64) return set_err(c, ADCGPU_UNSUPPORTED, "CVS matrix: FP64 iterations only");
+    if (p->precon != ADCGPU_PRECON_DPR && p->precon != ADCGPU_PRECON_OLSEN)
+      return set_err(c, ADCGPU_UNSUPPORTED, "CVS matrix: DPR or Olsen preconditioner");
+    if (p->lsubdiag) return set_err(c, ADCGPU_UNSUPPORTED, "CVS matrix: initvec_ondiag guess");
+  }
   int blocksize = p->dmain > 0 ? p->dmain : std::max(nstates + 5, 2 * nstates);
   int maxvec = p->maxsubdim >= 0 ? p->maxsubdim : 4 * blocksize;
   {
@@ -642,7 +649,7 @@ extern "C" int adcgpu_davidson_trace(adcgpu_ctx* h, const adcgpu_dav_params* p, 
     return ADCGPU_BAD_INPUT;
   cudaSetDevice(c->device);
   if (!c->have_matrix) return set_err(c, ADCGPU_NO_MATRIX, "build the matrix first");
-  const int64_t N = c->geom.N;
+  const int64_t N = mat_dim(c);
   const int nstates = p->davstates;
   int blocksize = p->dmain > 0 ? p->dmain : std::max(nstates + 5, 2 * nstates);
   int maxvec = p->maxsubdim >= 0 ? p->maxsubdim : 4 * blocksize;

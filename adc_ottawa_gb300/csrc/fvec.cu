@@ -33,6 +33,7 @@
 // the matrices above run over.  The dense products are FP64 GEMMs on the
 // CUDA cores (GB300 has no fast FP64 tensor path); the result differs from
 // the reference's loop order only by FP64 rounding (about 1e-15 relative).
+#include <algorithm>
 #include <cmath>
 #include <vector>
 
@@ -536,7 +537,9 @@ int modified_tm_adc2(Ctx* c, int64_t ndim, const int32_t* kpq, double* mtm) {
   const int no = c->geom.no, nv = c->geom.nv;
   if (no > FV_MAXNO) return set_err(c, ADCGPU_UNSUPPORTED, "f-vector: nocc above 32");
   if (!c->d_oooo || !c->d_vvvv) return set_err(c, ADCGPU_BAD_INPUT, "f-vector: (oo|oo) and (vv|vv) blocks missing");
-  const int64_t n1 = c->geom.n1, nn = n1 * n1, n2 = ndim - n1;
+  // kpq: the ADC(2)-s list or a CVS list (singles on core holes, no i=j
+  // doubles); the 1h1p block is evaluated for all singles and gathered
+  const int64_t n1 = c->geom.n1, nn = n1 * n1, ns = kpq[0], n2 = ndim - ns;
   const int64_t nv2 = (int64_t)nv * nv, no2 = (int64_t)no * no;
   cudaStream_t s = c->stream;
   // a-batch of the (vv|vv) rows: at most ~1 GiB of rows
@@ -552,7 +555,7 @@ int modified_tm_adc2(Ctx* c, int64_t ndim, const int32_t* kpq, double* mtm) {
   const int64_t nws = std::max<int64_t>((int64_t)nsplit_a * nv2, 1);
   Buf bufs[] = {{&T, nn}, {&Km, nn}, {&X2, nn}, {&Tsw, nn}, {&A1, nn}, {&L2, nn}, {&J, nn}, {&Z, nn}, {&Y, nn},
                 {&W, nn}, {&Tcd, nn}, {&Ab, (int64_t)na * nv * nv2}, {&Ap, nv2 * no2}, {&Bp, no2 * no2},
-                {&vec, nvec}, {&ws, nws}, {&dout, ndim}};
+                {&vec, nvec}, {&ws, nws}, {&dout, n1 + n2}};
   const int nbuf = (int)(sizeof(bufs) / sizeof(bufs[0]));
   for (Buf& b : bufs) *b.p = nullptr;
   int st = ADCGPU_OK;
@@ -628,13 +631,23 @@ int modified_tm_adc2(Ctx* c, int64_t ndim, const int32_t* kpq, double* mtm) {
     ADC_COUNT_LAUNCH();
     // 2h2p block over kpq columns n1+1 .. ndim
     if (n2 > 0) {
-      ADC_CUDA(c, h2d(c, dcols, kpq + 7 * (n1 + 1), sizeof(int32_t) * 7 * (size_t)n2));
+      ADC_CUDA(c, h2d(c, dcols, kpq + 7 * (ns + 1), sizeof(int32_t) * 7 * (size_t)n2));
       FvEri V{c->d_vovo, no, nv};
       k_fv_doubles<<<fv_grid(c, n2, 128), 128, 0, s>>>(V, e, dpl, dcols, n2, dout + n1);
       ADC_COUNT_LAUNCH();
     }
     ADC_CUDA(c, cudaGetLastError());
-    ADC_CUDA(c, d2h(c, mtm, dout, sizeof(double) * (size_t)ndim));
+    if (ns == n1) {
+      ADC_CUDA(c, d2h(c, mtm, dout, sizeof(double) * (size_t)ndim));
+    } else {
+      std::vector<double> full((size_t)(n1 + n2));
+      ADC_CUDA(c, d2h(c, full.data(), dout, sizeof(double) * full.size()));
+      for (int64_t i = 0; i < ns; ++i) {
+        const int32_t* q = kpq + 7 * (i + 1);
+        mtm[i] = full[(size_t)(q[4] - no - 1) * no + (q[2] - 1)];
+      }
+      std::copy(full.begin() + n1, full.end(), mtm + ns);
+    }
     return ADCGPU_OK;
   };
   st = run();

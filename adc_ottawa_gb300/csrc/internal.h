@@ -298,6 +298,16 @@ struct Ctx {
   std::unordered_map<void*, size_t> dev_allocs;   // dmalloc pointer -> size
   // learned preconditioner (MlpState, mlp.cu); DPR is used when absent
   void* mlp = nullptr;
+  // CVS matrix (write_fspace_adc2_1_cvs): singles on core holes only; the
+  // ph-ph block dense (diagonal included), the coupling block as CSR over the
+  // doubles rows (kept entries, column = CVS single index)
+  int cvs = 0;
+  int64_t cvs_n1 = 0, cvs_N = 0, cvs_nnz = 0;
+  std::vector<int32_t> cvs_kpq;   // 7 x (cvs_N + 1)
+  double* d_Ac = nullptr;         // cvs_n1 x cvs_n1
+  int64_t* d_crow = nullptr;      // row offsets, n2 + 1
+  int32_t* d_ccol = nullptr;
+  double* d_cval = nullptr;
   // SIL persistent state for adcgpu_silstep (device Krylov vectors)
   double* d_sil = nullptr;
   int64_t sil_cap = 0;
@@ -365,8 +375,21 @@ int build_adc1_matrix(Ctx* c, double* d_M);
 int coupling_values(Ctx* c, double* buf, int64_t vbase, int64_t row0, int64_t row1, int64_t* rowcount);
 int export_coo_device(Ctx* c, double* d_h, int32_t* d_oi, int32_t* d_oj);
 
+// Dimension and singles count of the matrix the context holds (the CVS
+// matrix when one was built, else the ADC(2)-s space of the orbitals).
+inline int64_t mat_dim(const Ctx* c) { return c->cvs ? c->cvs_N : c->geom.N; }
+inline int64_t mat_n1(const Ctx* c) { return c->cvs ? c->cvs_n1 : c->geom.n1; }
+
+// CVS (build_kernels.cu, cvs.cu): build from a validated CVS kpq (host,
+// 7 x (ndim+1)), the FP64 sigma product, the COO export and the release
+int build_matrix_cvs(Ctx* c, const int32_t* kpq, int64_t ndim, int ncore, const int32_t* core);
+int sigma_cvs(Ctx* c, int m, const double* dV, int64_t ldv, double* dW, int64_t ldw);
+int export_coo_cvs(Ctx* c, double* d_h, int32_t* d_oi, int32_t* d_oj);
+void free_cvs(Ctx* c);
+
 // fvec.cu : the ADC(2) f-vector (get_modifiedtm_adc2) of the dipole matrix
-// d_dpl over kpq columns 1..ndim (kpq validated by the caller); mtm on the host
+// d_dpl over kpq columns 1..ndim (an ADC(2)-s or CVS list validated by the
+// caller); mtm on the host
 int modified_tm_adc2(Ctx* c, int64_t ndim, const int32_t* kpq, double* mtm);
 
 // sigma.cu : W = H V for m columns (column-major, leading dim ld), FP64 or FP32.

@@ -319,8 +319,8 @@ extern "C" int adcgpu_block_lanczos(adcgpu_ctx* h, int lmain, int ncycles, int o
   if (c->precision != ADCGPU_FP64 && c->precision != ADCGPU_MIXED) return ADCGPU_BAD_INPUT;
   if (lmain <= 0 || ncycles <= 0 || !q0 || (orthotype != 0 && orthotype != 1))
     return set_err(c, ADCGPU_BAD_INPUT, "lmain, ncycles, q0 and orthotype in {0,1} required");
-  if ((int64_t)lmain * ncycles > c->geom.N) return set_err(c, ADCGPU_BAD_INPUT, "nvec exceeds the dimension");
+  if ((int64_t)lmain * ncycles > mat_dim(c)) return set_err(c, ADCGPU_BAD_INPUT, "nvec exceeds the dimension");
   LanczosGPU L;
-  L.c = c; L.N = c->geom.N; L.b = lmain; L.ncycles = ncycles;
+  L.c = c; L.N = mat_dim(c); L.b = lmain; L.ncycles = ncycles;
   return L.run(orthotype, q0, tmat, evals, ritz);
 }

@@ -1694,6 +1694,7 @@ extern "C" int adcgpu_sigma_set_shape(adcgpu_ctx* h, int chunk, int mc_fp64, int
 }
 
 int sigma_fp64(Ctx* c, int m, const double* dV, int64_t ldv, double* dW, int64_t ldw) {
+  if (c->cvs) return sigma_cvs(c, m, dV, ldv, dW, ldw);
   return sigma_impl<double, double>(c, m, dV, ldv, dW, ldw, c->d_A, c->d_diag, c->d_Bt);
 }
 
@@ -1712,6 +1713,7 @@ int singles_block_product(Ctx* c, int m, const float* V, int64_t ldv, float* W, 
 }
 
 int sigma_fp32(Ctx* c, int m, const float* dV, int64_t ldv, float* dW, int64_t ldw) {
+  if (c->cvs) return set_err(c, ADCGPU_UNSUPPORTED, "the CVS matrix is held in FP64 only");
   if (c->mixed_bf16)
     return sigma_impl<float, __nv_bfloat16>(c, m, dV, ldv, dW, ldw, c->d_A32, c->d_diag32,
                                             (const __nv_bfloat16*)c->d_Bt16);

@@ -423,7 +423,7 @@ extern "C" int adcgpu_autocorr(adcgpu_ctx* h, int nwp, const double* f, double t
   if (c->precision != ADCGPU_FP64) return set_err(c, ADCGPU_BAD_INPUT, "SIL runs on the FP64 matrix");
   if (nwp <= 0 || !f || !auto_out || tout <= 0.0 || tfinal < 0.0 || kdim < 2)
     return set_err(c, ADCGPU_BAD_INPUT, "autocorr arguments");
-  const int64_t N = c->geom.N;
+  const int64_t N = mat_dim(c);
   SilEngine E;
   E.c = c; E.N = N; E.P = nwp; E.kdim = kdim;
   ST(E.alloc());
@@ -492,11 +492,11 @@ extern "C" int adcgpu_silstep(adcgpu_ctx* h, double* psi, double* dtpsi, int psi
   if (!c) return ADCGPU_BAD_INPUT;
   cudaSetDevice(c->device);
   if (!c->have_matrix) return set_err(c, ADCGPU_NO_MATRIX, "build the matrix first");
-  if (psidim != c->geom.N || !psi || !dtpsi) return set_err(c, ADCGPU_BAD_INPUT, "psi dimension");
+  if (psidim != mat_dim(c) || !psi || !dtpsi) return set_err(c, ADCGPU_BAD_INPUT, "psi dimension");
   if (intorder < 2) return ADCGPU_SIL_BAD_ORDER;
   if (!restart) return set_err(c, ADCGPU_UNSUPPORTED, "non-restart SILStep calls keep Krylov vectors; use restart");
   if (!stdform) return set_err(c, ADCGPU_UNSUPPORTED, "Func must be -iH (StdForm) on this path");
-  const int64_t N = c->geom.N;
+  const int64_t N = mat_dim(c);
   SilEngine E;
   E.c = c; E.N = N; E.P = 1; E.kdim = intorder;
   ST(E.alloc());

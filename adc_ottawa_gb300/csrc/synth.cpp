@@ -198,3 +198,72 @@ extern "C" int adcgpu_select_adc2s(int nocc, int nvirt, int32_t* kpq) {
   for (int k = 0; k < 5; ++k) kpq[k] = cnt[k];
   return n == ndim ? ADCGPU_OK : ADCGPU_BAD_INPUT;
 }
+
+// ---------------------------------------------------------------------------
+// CVS kpq: select_atom_is_cvs (select_fano.f90:112-142) and select_atom_d_cvs
+// (:903-1027) for C1 symmetry, no frozen orbitals, hcentre = 1..nocc.  core
+// lists the core orbitals (icore, 1-based occupied indices).  Singles: ap
+// outer, core hole inner (in hcentre order).  Doubles: classes 3 (a=b, i<j)
+// and 4I/4II (a<b, i<j) whose hole pair holds exactly one core orbital; no
+// i=j classes.
+// ---------------------------------------------------------------------------
+static bool cvs_mask(int nocc, int ncore, const int32_t* core, std::vector<char>& is_core) {
+  if (ncore <= 0 || ncore >= nocc || !core) return false;
+  is_core.assign(nocc + 1, 0);
+  for (int i = 0; i < ncore; ++i) {
+    if (core[i] < 1 || core[i] > nocc || is_core[core[i]]) return false;
+    is_core[core[i]] = 1;
+  }
+  return true;
+}
+
+extern "C" int64_t adcgpu_cvs_dim(int nocc, int nvirt, int ncore, const int32_t* core, int32_t* counts5) {
+  std::vector<char> ic;
+  if (nocc <= 0 || nvirt <= 1 || !cvs_mask(nocc, ncore, core, ic)) return -1;
+  int64_t pairs = (int64_t)ncore * (nocc - ncore);   // hole pairs with exactly one core orbital
+  int64_t c1 = (int64_t)ncore * nvirt;
+  int64_t c4 = pairs * nvirt;
+  int64_t c5 = pairs * ((int64_t)nvirt * (nvirt - 1) / 2);
+  if (counts5) {
+    counts5[0] = (int32_t)c1; counts5[1] = 0; counts5[2] = 0;
+    counts5[3] = (int32_t)c4; counts5[4] = (int32_t)c5;
+  }
+  return c1 + c4 + 2 * c5;
+}
+
+extern "C" int adcgpu_select_adc2s_cvs(int nocc, int nvirt, int ncore, const int32_t* core, int32_t* kpq) {
+  std::vector<char> ic;
+  if (!kpq || !cvs_mask(nocc, ncore, core, ic)) return ADCGPU_BAD_INPUT;
+  int32_t cnt[5];
+  const int64_t ndim = adcgpu_cvs_dim(nocc, nvirt, ncore, core, cnt);
+  if (ndim <= 0 || ndim > INT32_MAX) return ADCGPU_BAD_INPUT;
+  const int nbas = nocc + nvirt;
+  std::memset(kpq, 0, sizeof(int32_t) * 7 * (size_t)(ndim + 1));
+  auto put = [&](int64_t col, int cnf, int spin, int a, int b, int j, int k, int type) {
+    int32_t* c = kpq + 7 * col;
+    c[0] = cnf; c[1] = spin; c[2] = j; c[3] = k; c[4] = a; c[5] = b; c[6] = type;
+  };
+  int64_t n = 0;
+  for (int a = nocc + 1; a <= nbas; ++a)                 // select_atom_is_cvs :124-138
+    for (int i = 1; i <= nocc; ++i)
+      if (ic[i]) put(++n, 1, 1, a, -1, i, -1, 0);
+  for (int i = 1; i <= nocc; ++i)                        // a=b, i|=j, one core hole :937-962
+    for (int j = i + 1; j <= nocc; ++j)
+      if (ic[i] + ic[j] == 1)
+        for (int a = nocc + 1; a <= nbas; ++a) put(++n, 2, 1, a, a, i, j, 3);
+  const int64_t start4 = n;
+  for (int i = 1; i <= nocc; ++i)                        // a|=b, i|=j spin I :967-1017
+    for (int j = i + 1; j <= nocc; ++j)
+      if (ic[i] + ic[j] == 1)
+        for (int a = nocc + 1; a <= nbas; ++a)
+          for (int b = a + 1; b <= nbas; ++b) put(++n, 2, 11, a, b, i, j, 4);
+  for (int64_t t = 1; t <= cnt[4]; ++t) {                // spin II copy :1019-1021
+    int32_t* src = kpq + 7 * (start4 + t);
+    int32_t* dst = kpq + 7 * (start4 + cnt[4] + t);
+    std::memcpy(dst, src, 7 * sizeof(int32_t));
+    dst[1] = 12; dst[6] = 5;
+  }
+  n += cnt[4];
+  for (int k = 0; k < 5; ++k) kpq[k] = cnt[k];
+  return n == ndim ? ADCGPU_OK : ADCGPU_BAD_INPUT;
+}

@@ -116,6 +116,16 @@ int64_t adcgpu_adc2s_dim(int nocc, int nvirt, int32_t* counts5);
 /* Fills kpq(7, 0:ndim), column-major int32, column 0 holding the counts. */
 int adcgpu_select_adc2s(int nocc, int nvirt, int32_t* kpq);
 
+/* CVS configuration list: select_atom_is_cvs (select_fano.f90:112-142) and
+   select_atom_d_cvs (:903-1027), C1 symmetry, no frozen orbitals.  core[ncore]
+   holds the core orbitals (the icore list, 1-based occupied indices,
+   0 < ncore < nocc).  Singles (a, core hole); doubles of the classes a=b,i<j
+   and a<b,i<j (spin I, then the spin II copy) whose hole pair holds exactly
+   one core orbital.  adcgpu_cvs_dim returns ndim (-1 on bad input) and fills
+   counts5 = kpq(1..5,0) (may be NULL). */
+int64_t adcgpu_cvs_dim(int nocc, int nvirt, int ncore, const int32_t* core, int32_t* counts5);
+int adcgpu_select_adc2s_cvs(int nocc, int nvirt, int ncore, const int32_t* core, int32_t* kpq);
+
 /* ---------------------------------------------------------------------------
  * Context.
  * ------------------------------------------------------------------------- */
@@ -144,6 +154,19 @@ int adcgpu_set_eri_mo_complex(adcgpu_ctx* ctx, const double* buffer_real);
  * ------------------------------------------------------------------------- */
 int adcgpu_build_adc2s(adcgpu_ctx* ctx, int ndim, const int32_t* kpq,
                        int64_t* noffd_out, char flag, int precision);
+
+/* CVS builder: write_fspace_adc2_1_cvs(ndim,kpq,noffdel,chr),
+   fspacetrial.f90:566-596 (get_offdiag_adc2_save_cvs_omp get_matrix.f90
+   :1323-1726 and get_diag_adc2_save :267-311).  core[ncore] is the icore
+   list; kpq must be the list adcgpu_select_adc2s_cvs produces for it (checked;
+   NULL = that list).  The matrix is held in FP64 (ph-ph block dense, coupling
+   block as compressed rows) and replaces any matrix the context held; the
+   sigma product, Davidson (ondiag guess, DPR or Olsen), block Lanczos, SIL,
+   the COO export and the SCRATCH files then work on it.  The COO lists the
+   ph-ph pairs as the reference's loop writes them (oi > oj), then the
+   coupling entries (oi = single < oj = double). */
+int adcgpu_build_adc2s_cvs(adcgpu_ctx* ctx, int ndim, const int32_t* kpq, int ncore,
+                           const int32_t* core, int64_t* noffd_out, char flag);
 
 /* Diagonal hii(ndim) (get_diag_adc2_save, get_matrix.f90:267-311). */
 int adcgpu_get_diag(adcgpu_ctx* ctx, double* hii);
@@ -176,8 +199,10 @@ int adcgpu_set_dipole(adcgpu_ctx* ctx, const double* dpl);
    orbitals, ERIs and dipole matrix of the context.  It is the start vector
    of the final-space Lanczos (lanczos_guess_vecs, adc2_opa.f90:380-520),
    of the wavepacket propagation (init_wavepacket, fvecprop.f90:338-357)
-   and of the Chebyshev autocorrelation (adc2_autospec.f90:162).  FP64;
-   mtm: host array of ndim doubles. */
+   and of the Chebyshev autocorrelation (adc2_autospec.f90:162).  A CVS kpq
+   (adcgpu_select_adc2s_cvs, ndim its dimension) gives the CVS f-vector (the
+   i=j classes are absent, as lcvs skips them, :365-366).  FP64; mtm: host
+   array of ndim doubles. */
 int adcgpu_modified_tm_adc2(adcgpu_ctx* ctx, int ndim, const int32_t* kpq, double* mtm);
 
 /* fill_stvc(ndim,vctr), fspacetrial.f90:1255-1270: the indices (1-based) of

@@ -86,6 +86,12 @@ def lib():
         L.orc_synth_uniform_block.restype = C.c_int
         L.orc_adc2s_dim.argtypes = [C.c_int, C.c_int, _ip]
         L.orc_adc2s_dim.restype = C.c_int64
+        L.orc_build_cvs.argtypes = [C.c_int, C.c_int, _dp, _dp, C.c_int, _ip, C.c_int]
+        L.orc_build_cvs.restype = C.c_void_p
+        L.orc_cvs_dim.argtypes = [C.c_int, C.c_int, C.c_int, _ip, _ip]
+        L.orc_cvs_dim.restype = C.c_int64
+        L.orc_select_adc2s_cvs.argtypes = [C.c_int, C.c_int, C.c_int, _ip, _ip]
+        L.orc_select_adc2s_cvs.restype = C.c_int
         L.orc_synth_dipole.argtypes = [C.c_int, C.c_uint64, _dp]
         L.orc_synth_dipole.restype = C.c_int
         L.orc_modified_tm_adc2.argtypes = [C.c_int, C.c_int, _dp, _dp, _dp, C.c_int64, _ip, _dp, C.c_int]
@@ -122,11 +128,25 @@ def synth_dipole(nbas: int, seed: int) -> np.ndarray:
     return d
 
 
-def modified_tm_adc2(no: int, nv: int, e, eri, dpl, sections: int = 3) -> np.ndarray:
-    """get_modifiedtm_adc2's f-vector over the ADC(2)-s configuration list
-    (get_moment.f90:153-442), FP64 in the reference's loop and expression
+def select_cvs(no: int, nv: int, core) -> np.ndarray:
+    """The CVS kpq (select_atom_is_cvs / select_atom_d_cvs) as (ndim+1, 7) int32."""
+    core = np.ascontiguousarray(core, np.int32)
+    cnt = np.zeros(5, np.int32)
+    ndim = int(lib().orc_cvs_dim(no, nv, len(core), _p(core, _ip), _p(cnt, _ip)))
+    assert ndim > 0
+    kpq = np.zeros((ndim + 1, 7), np.int32)
+    assert lib().orc_select_adc2s_cvs(no, nv, len(core), _p(core, _ip), _p(kpq, _ip)) == 0
+    return kpq
+
+
+def modified_tm_adc2(no: int, nv: int, e, eri, dpl, sections: int = 3, kpq=None) -> np.ndarray:
+    """get_modifiedtm_adc2's f-vector over a configuration list (the ADC(2)-s
+    list by default; a CVS list skips the i=j classes as lcvs does),
+    get_moment.f90:153-442, FP64 in the reference's loop and expression
     order.  sections: 1 = singles only, 2 = doubles only, 3 = both."""
-    kpq = select(no, nv)
+    if kpq is None:
+        kpq = select(no, nv)
+    kpq = np.ascontiguousarray(kpq, np.int32)
     ndim = kpq.shape[0] - 1
     e = np.ascontiguousarray(e, np.float64)
     eri = np.ascontiguousarray(eri, np.float64)
@@ -181,6 +201,17 @@ class Matrix:
         e = np.ascontiguousarray(e, dtype=np.float64)
         eri = np.ascontiguousarray(eri, dtype=np.float64)
         return cls(lib().orc_build(no, nv, _p(e), _p(eri), nthreads))
+
+    @classmethod
+    def build_cvs(cls, no, nv, e, eri, core, nthreads=0):
+        """write_fspace_adc2_1_cvs: the CVS ADC(2)-s matrix for the core
+        orbitals core (1-based occupied indices)."""
+        e = np.ascontiguousarray(e, np.float64)
+        eri = np.ascontiguousarray(eri, np.float64)
+        core = np.ascontiguousarray(core, np.int32)
+        h = lib().orc_build_cvs(no, nv, _p(e), _p(eri), len(core), _p(core, _ip), nthreads)
+        assert h
+        return cls(h)
 
     @classmethod
     def build_direct(cls, no, nv, e, eri, nthreads=0):

@@ -417,6 +417,113 @@ static void* build_impl(int no, int nv, const double* e, const double* eri, int 
   return M;
 }
 
+// write_fspace_adc2_1_cvs (fspacetrial.f90:566-596): get_offdiag_adc2_save_cvs_omp
+// (get_matrix.f90:1323-1726) and get_diag_adc2_save (:267-311) over the CVS
+// configuration list (select_atom_is_cvs / select_atom_d_cvs, generated by the
+// shared generator's orc_select_adc2s_cvs).  The ph-ph loop runs j = 1..i-1
+// with the row i's indices first (:1452-1478); the coupling loops are C3 on
+// the a=b,i|=j doubles, C1 on spin I and C2 on spin II (:1503-1620).  COO
+// entries (oi = single i, oj = j), kept when |x| > minc.
+int64_t orc_cvs_dim(int, int, int, const int32_t*, int32_t*);
+int orc_select_adc2s_cvs(int, int, int, const int32_t*, int32_t*);
+
+void* orc_build_cvs(int no, int nv, const double* e, const double* eri, int ncore, const int32_t* core,
+                    int nthreads) {
+  System S;
+  S.no = no; S.nv = nv; S.nbas = no + nv; S.eri = eri;
+  S.e.assign(S.nbas + 1, 0.0);
+  for (int p = 1; p <= S.nbas; ++p) S.e[p] = e[p - 1];
+  int32_t cnt[5];
+  const int64_t ndim = orc_cvs_dim(no, nv, ncore, core, cnt);
+  if (ndim <= 0) return nullptr;
+  std::vector<int32_t> raw((size_t)7 * (ndim + 1));
+  if (orc_select_adc2s_cvs(no, nv, ncore, core, raw.data()) != 0) return nullptr;
+  std::vector<Conf> kpq((size_t)ndim + 1);
+  for (int64_t c = 0; c <= ndim; ++c) {
+    const int32_t* q = raw.data() + 7 * c;
+    kpq[c] = Conf{q[0], q[1], q[2], q[3], q[4], q[5], q[6]};
+  }
+  const int ndim1 = cnt[0];
+#ifdef _OPENMP
+  if (nthreads <= 0) nthreads = omp_get_max_threads();
+#else
+  nthreads = 1;
+#endif
+  OrcMatrix* M = new OrcMatrix;
+  M->ndim = ndim;
+  M->diag.assign(ndim, 0.0);
+  std::vector<double> ca((size_t)nv * nv), cb((size_t)no * no);
+#pragma omp parallel for schedule(dynamic) num_threads(nthreads)
+  for (int i = 1; i <= nv; ++i)
+    for (int j = i; j <= nv; ++j) {
+      double x = CA_ph_ph(S, no + i, no + j);
+      ca[(size_t)(i - 1) * nv + (j - 1)] = x; ca[(size_t)(j - 1) * nv + (i - 1)] = x;
+    }
+#pragma omp parallel for schedule(dynamic) num_threads(nthreads)
+  for (int i = 1; i <= no; ++i)
+    for (int j = i; j <= no; ++j) {
+      double x = CB_ph_ph(S, i, j);
+      cb[(size_t)(i - 1) * no + (j - 1)] = x; cb[(size_t)(j - 1) * no + (i - 1)] = x;
+    }
+#pragma omp parallel for schedule(dynamic) num_threads(nthreads)
+  for (int i = 1; i <= ndim1; ++i) {
+    const Conf& c = kpq[i];
+    double x = K_ph_ph(S.e[c.a], S.e[c.j]);
+    x = x + C1_ph_ph(S, c.a, c.j, c.a, c.j);
+    x = x + CA_ph_ph(S, c.a, c.a);
+    x = x + CB_ph_ph(S, c.j, c.j);
+    x = x + CC_ph_ph(S, c.a, c.j, c.a, c.j);
+    M->diag[i - 1] = x;
+  }
+  for (int64_t i = ndim1 + 1; i <= ndim; ++i) {
+    const Conf& c = kpq[i];
+    M->diag[i - 1] = K_2p2h_2p2h(S.e[c.a], S.e[c.b], S.e[c.j], S.e[c.k]);
+  }
+  struct Buf { std::vector<double> h; std::vector<int32_t> j; };
+  const int nloops = 4;
+  std::vector<std::vector<Buf>> bufs(nloops, std::vector<Buf>(ndim1 + 1));
+  const int64_t off3 = ndim1, off4 = off3 + cnt[3], off5 = off4 + cnt[4];
+#pragma omp parallel for schedule(dynamic) num_threads(nthreads)
+  for (int i = 1; i <= ndim1; ++i) {
+    const Conf& ci = kpq[i];
+    const int a = ci.a, k = ci.j;
+    for (int L = 0; L < nloops; ++L) {
+      Buf& B = bufs[L][i];
+      int64_t j0, j1;
+      switch (L) {
+        case 0: j0 = 1; j1 = i - 1; break;
+        case 1: j0 = off3 + 1; j1 = off3 + cnt[3]; break;
+        case 2: j0 = off4 + 1; j1 = off4 + cnt[4]; break;
+        default: j0 = off5 + 1; j1 = off5 + cnt[4]; break;
+      }
+      for (int64_t j = j0; j <= j1; ++j) {
+        const Conf& cj = kpq[j];
+        double x;
+        switch (L) {
+          case 0:
+            x = C1_ph_ph(S, a, k, cj.a, cj.j);
+            if (k == cj.j) x = x + ca[(size_t)(a - no - 1) * nv + (cj.a - no - 1)];
+            if (a == cj.a) x = x + cb[(size_t)(k - 1) * no + (cj.j - 1)];
+            x = x + CC_ph_ph(S, a, k, cj.a, cj.j);
+            break;
+          case 1: x = C3_ph_2p2h(S, a, k, cj.a, cj.j, cj.k); break;
+          case 2: x = C1_ph_2p2h(S, a, k, cj.a, cj.b, cj.j, cj.k); break;
+          default: x = C2_ph_2p2h(S, a, k, cj.a, cj.b, cj.j, cj.k); break;
+        }
+        if (std::fabs(x) > minc) { B.h.push_back(x); B.j.push_back((int32_t)j); }
+      }
+    }
+  }
+  for (int L = 0; L < nloops; ++L)
+    for (int i = 1; i <= ndim1; ++i) {
+      Buf& B = bufs[L][i];
+      for (size_t t = 0; t < B.h.size(); ++t) {
+        M->h.push_back(B.h[t]); M->oi.push_back(i); M->oj.push_back(B.j[t]);
+      }
+    }
+  return M;
+}
+
 int64_t orc_matrix_ndim(void* m) { return ((OrcMatrix*)m)->ndim; }
 int64_t orc_matrix_nnz(void* m) { return (int64_t)((OrcMatrix*)m)->h.size(); }
 
