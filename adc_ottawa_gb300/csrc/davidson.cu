@@ -558,6 +558,12 @@ int davidson_solve(Ctx* c, const adcgpu_dav_params* p, double* evals, double* ev
     // the folded preconditioner makes FP64 iterations cheap and few, so it
     // hands over earlier
     const double tol_f = p->tol_fp32 != 0.0 ? p->tol_fp32 : (p->precon == ADCGPU_PRECON_FOLD ? 1e-5 : 5e-6);
+    // Deflation (locking converged roots, block_davidson.f90:1147-1222) is
+    // kept for the reference preconditioners.  With the folded one it lost
+    // roots: on 9 seeded systems (nocc 10-14, 20 roots) the solve converged to
+    // a wrong set on 3 with deflation and on none without, and without it the
+    // solve is also faster (fewer, better-conditioned iterations).
+    const bool deflate = p->ldfl != 0 && p->precon != ADCGPU_PRECON_FOLD;
     float* g32 = nullptr;
     ST(dmalloc(c, (void**)&g32, sizeof(float) * (size_t)N * blocksize));
     int nguess = 0;
@@ -566,7 +572,8 @@ int davidson_solve(Ctx* c, const adcgpu_dav_params* p, double* evals, double* ev
       c->mixed_bf16 = phase == 0 ? 1 : 0;
       DavidsonGPU<float> D;
       D.c = c; D.N = N; D.nstates = nstates; D.blocksize = blocksize; D.maxvec = maxvec;
-      D.niter = p->maxiter; D.ipre = p->precon; D.ldeflate = p->ldfl != 0;
+      D.niter = p->maxiter; D.ipre = p->precon;
+      D.ldeflate = deflate;
       D.tol = std::max(p->davtol, phase == 0 ? tol_b : tol_f);
       D.hii = c->d_diag32; D.mlp = mlp;
       D.stall_iters = 12;
@@ -595,7 +602,7 @@ int davidson_solve(Ctx* c, const adcgpu_dav_params* p, double* evals, double* ev
     F.c = c; F.N = N; F.nstates = nstates; F.blocksize = rblock;
     F.maxvec = (p->refine > 1 ? p->refine : 4) * rblock;
     F.niter = p->maxiter; F.ipre = precon64;
-    F.ldeflate = p->ldfl != 0; F.tol = p->davtol; F.hii = c->d_diag;
+    F.ldeflate = deflate; F.tol = p->davtol; F.hii = c->d_diag;
     int it2 = 0, nc2 = 0, nout = 0;
     // the refinement's subspace GEMMs run in double-float on the FP32 pipe
     // (FP64-accurate to ~1e-14 relative); the plain FP64 path keeps DFMA
@@ -611,7 +618,7 @@ int davidson_solve(Ctx* c, const adcgpu_dav_params* p, double* evals, double* ev
     DavidsonGPU<double> D;
     D.c = c; D.N = N; D.nstates = nstates; D.blocksize = blocksize; D.maxvec = maxvec;
     D.niter = p->maxiter; D.ipre = precon64;
-    D.ldeflate = p->ldfl != 0; D.tol = p->davtol; D.hii = c->d_diag;
+    D.ldeflate = p->ldfl != 0 && precon64 != ADCGPU_PRECON_FOLD; D.tol = p->davtol; D.hii = c->d_diag;
     int it = 0, nc = 0, nout = 0;
     st = D.run(hdiag, guess_kind, p->guessdim, nullptr, 0, ev, out64, blocksize, &nout, &it, &nc);
     inf.iterations = it; inf.iters_fp64 = it; inf.nmult = D.nmult; inf.sigma_seconds = D.sigma_s; inf.nconv = nc;

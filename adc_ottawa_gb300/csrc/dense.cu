@@ -290,6 +290,167 @@ __global__ void __launch_bounds__(256) k_gemm_nn_df(int64_t N, int p, int q, dou
   }
 }
 
+// FP32 tall-skinny C(N x q) = beta C + alpha A(N x p) B(p x q) (B FP64 or
+// FP32, held as FP32 in shared memory for all row blocks of a persistent
+// block).  A thread owns one row and the QT columns of a column tile: per k
+// it loads one value of A (coalesced across the warp) and reads B's row k as
+// QT/4 float4 broadcasts for QT FMAs.  The k loop runs in groups of NN_KG
+// with the next group's A values loaded before the current group's FMAs, so
+// each thread keeps NN_KG loads in flight (the kernel is otherwise bound by
+// the latency of the column-strided loads of A).
+constexpr int NN_KG = 16;
+template <int QT>
+__device__ __forceinline__ void nn_f32_step(float (&acc)[QT], float a, const float* __restrict__ brow) {
+  const float4* b4 = reinterpret_cast<const float4*>(brow);
+#pragma unroll
+  for (int j4 = 0; j4 < QT / 4; ++j4) {
+    const float4 b = b4[j4];
+    acc[4 * j4 + 0] = fmaf(a, b.x, acc[4 * j4 + 0]);
+    acc[4 * j4 + 1] = fmaf(a, b.y, acc[4 * j4 + 1]);
+    acc[4 * j4 + 2] = fmaf(a, b.z, acc[4 * j4 + 2]);
+    acc[4 * j4 + 3] = fmaf(a, b.w, acc[4 * j4 + 3]);
+  }
+}
+
+template <typename TB, int QT>
+__global__ void __launch_bounds__(256, 2) k_gemm_nn_f32(int64_t N, int p, int q, float alpha,
+                                                        const float* __restrict__ A, int64_t lda,
+                                                        const TB* __restrict__ B, int ldb, float beta,
+                                                        float* __restrict__ C, int64_t ldc) {
+  extern __shared__ __align__(16) float sBf[];   // [p][QT]
+  const int q0 = blockIdx.y * QT;
+  for (int l = threadIdx.x; l < p * QT; l += blockDim.x) {
+    const int k = l / QT, j = l % QT;
+    sBf[l] = q0 + j < q ? to_t<float, TB>(B[(int64_t)(q0 + j) * ldb + k]) : 0.f;
+  }
+  __syncthreads();
+  const int qn = min(QT, q - q0);
+  const int pg = p - p % NN_KG;
+  for (int64_t r0 = blockIdx.x * 256ll; r0 < N; r0 += (int64_t)gridDim.x * 256) {
+    const int64_t row = r0 + threadIdx.x;
+    const bool ok = row < N;
+    float acc[QT];
+#pragma unroll
+    for (int j = 0; j < QT; ++j) acc[j] = 0.f;
+    float cur[NN_KG], nxt[NN_KG];
+    if (pg > 0) {
+#pragma unroll
+      for (int u = 0; u < NN_KG; ++u) cur[u] = ok ? A[(int64_t)u * lda + row] : 0.f;
+    }
+    for (int k = 0; k < pg; k += NN_KG) {
+      const bool more = ok && k + NN_KG < pg;
+#pragma unroll
+      for (int u = 0; u < NN_KG; ++u) nxt[u] = more ? A[(int64_t)(k + NN_KG + u) * lda + row] : 0.f;
+#pragma unroll
+      for (int u = 0; u < NN_KG; ++u) nn_f32_step<QT>(acc, cur[u], sBf + (k + u) * QT);
+#pragma unroll
+      for (int u = 0; u < NN_KG; ++u) cur[u] = nxt[u];
+    }
+    for (int k = pg; k < p; ++k) nn_f32_step<QT>(acc, ok ? A[(int64_t)k * lda + row] : 0.f, sBf + k * QT);
+    if (ok) {
+#pragma unroll
+      for (int j = 0; j < QT; ++j) {
+        if (j >= qn) break;
+        float* cp = C + (int64_t)(q0 + j) * ldc + row;
+        const float prev = beta == 0.f ? 0.f : beta * *cp;
+        *cp = prev + alpha * acc[j];
+      }
+    }
+  }
+}
+
+// FP32 tall-skinny partial Gram tiles C(p x q) = A(N x p)^T B(N x q): a block
+// sums a range of rows for one 64 x 64 output tile; a thread owns a 4 x 4
+// sub-tile read as float4 from row-major staged rows (32 rows per step).
+// The products of one step are summed in FP32 and added to double-float
+// accumulators, as in k_gemm_tn_part.  part: [blk][tile][64 x 64] doubles.
+constexpr int TF_T = 64, TF_ROWS = 32, TF_LD = TF_T + 4;
+__global__ void __launch_bounds__(256) k_gemm_tn_f32(int64_t N, int p, int q, const float* __restrict__ A,
+                                                     int64_t lda, const float* __restrict__ B, int64_t ldb,
+                                                     double* __restrict__ part, int64_t rows_per_blk) {
+  __shared__ __align__(16) float sA[TF_ROWS][TF_LD];
+  __shared__ __align__(16) float sB[TF_ROWS][TF_LD];
+  const int ntq = (q + TF_T - 1) / TF_T;
+  const int tile = blockIdx.y;
+  const int p0 = (tile / ntq) * TF_T, q0 = (tile % ntq) * TF_T;
+  const int tid = threadIdx.x, lane = tid & 31, warp = tid >> 5;
+  const int ti = tid & 15, tj = tid >> 4;        // outputs 4 ti.. (p) and 4 tj.. (q)
+  df acc[4][4];
+#pragma unroll
+  for (int u = 0; u < 4; ++u)
+#pragma unroll
+    for (int v = 0; v < 4; ++v) acc[u][v] = df{0.f, 0.f};
+  const int64_t r_begin = blockIdx.x * rows_per_blk;
+  const int64_t r_end = min(N, r_begin + rows_per_blk);
+  // a warp stages 32 consecutive rows of 8 columns (coalesced); the next
+  // step's values are loaded into registers while the current step computes
+  float pa[8], pb[8];
+  auto fetch = [&](int64_t r0) {
+    const int64_t r = r0 + lane;
+    const bool rok = r < r_end;
+#pragma unroll
+    for (int u = 0; u < 8; ++u) {
+      const int cidx = warp + 8 * u;
+      pa[u] = (rok && p0 + cidx < p) ? A[(int64_t)(p0 + cidx) * lda + r] : 0.f;
+      pb[u] = (rok && q0 + cidx < q) ? B[(int64_t)(q0 + cidx) * ldb + r] : 0.f;
+    }
+  };
+  if (r_begin < r_end) fetch(r_begin);
+  for (int64_t r0 = r_begin; r0 < r_end; r0 += TF_ROWS) {
+    __syncthreads();
+#pragma unroll
+    for (int u = 0; u < 8; ++u) {
+      sA[lane][warp + 8 * u] = pa[u];
+      sB[lane][warp + 8 * u] = pb[u];
+    }
+    __syncthreads();
+    if (r0 + TF_ROWS < r_end) fetch(r0 + TF_ROWS);
+    float st[4][4];
+#pragma unroll
+    for (int u = 0; u < 4; ++u)
+#pragma unroll
+      for (int v = 0; v < 4; ++v) st[u][v] = 0.f;
+#pragma unroll 8
+    for (int rr = 0; rr < TF_ROWS; ++rr) {
+      const float4 a = *reinterpret_cast<const float4*>(&sA[rr][4 * ti]);
+      const float4 b = *reinterpret_cast<const float4*>(&sB[rr][4 * tj]);
+      const float av[4] = {a.x, a.y, a.z, a.w}, bv[4] = {b.x, b.y, b.z, b.w};
+#pragma unroll
+      for (int u = 0; u < 4; ++u)
+#pragma unroll
+        for (int v = 0; v < 4; ++v) st[u][v] = fmaf(av[u], bv[v], st[u][v]);
+    }
+#pragma unroll
+    for (int u = 0; u < 4; ++u)
+#pragma unroll
+      for (int v = 0; v < 4; ++v) acc[u][v] = df_add(acc[u][v], df{st[u][v], 0.f});
+  }
+  double* out = part + ((int64_t)blockIdx.x * gridDim.y + tile) * (TF_T * TF_T);
+#pragma unroll
+  for (int u = 0; u < 4; ++u)
+#pragma unroll
+    for (int v = 0; v < 4; ++v) out[(4 * ti + u) * TF_T + 4 * tj + v] = df_value(acc[u][v]);
+}
+
+// C(p x q) (col-major, ldc) = alpha * sum over blocks of the k_gemm_tn_f32
+// partials + beta C, in a fixed block order
+template <typename TC>
+__global__ void k_gemm_tn_f32_reduce(int p, int q, int nblk, int ntile, const double* __restrict__ part,
+                                     TC* __restrict__ C, int ldc, TC alpha, TC beta) {
+  const int ntq = (q + TF_T - 1) / TF_T;
+  const int per_tile = TF_T * TF_T;
+  for (int o = blockIdx.x * blockDim.x + threadIdx.x; o < ntile * per_tile; o += gridDim.x * blockDim.x) {
+    const int tile = o / per_tile, w = o - tile * per_tile;
+    const int ii = w / TF_T, jj = w - ii * TF_T;
+    const int i = (tile / ntq) * TF_T + ii, j = (tile % ntq) * TF_T + jj;
+    if (i >= p || j >= q) continue;
+    double s = 0.0;
+    for (int b = 0; b < nblk; ++b) s += part[((int64_t)b * ntile + tile) * per_tile + w];
+    TC prev = beta == TC(0) ? TC(0) : beta * C[(int64_t)j * ldc + i];
+    C[(int64_t)j * ldc + i] = prev + alpha * (TC)s;
+  }
+}
+
 // dpr: t_i(j) = r_i(j) / (lambda_i - hii(j)); exact zero denominators give 0.
 template <typename T, typename TD>
 __global__ void k_dpr(int64_t N, int nb, const T* __restrict__ R, int64_t ldr, const double* __restrict__ lam,
@@ -430,6 +591,20 @@ int gemm_tn(Ctx* c, Workspace& ws, int64_t N, int p, int q, const T* A, int64_t 
     } else {
       k_gemm_tn_part<T, TA><<<dim3(nblk, ntile), 256, 0, c->stream>>>(N, p, q, A, lda, B, ldb, (TA*)ws.p, rows); ADC_COUNT_LAUNCH();
     }
+  } else if constexpr (std::is_same<T, float>::value && std::is_same<TA, double>::value) {
+    // FP32 inputs: 64 x 64 tiles with 4 x 4 float4 sub-tiles per thread
+    const int ntile2 = ((p + TF_T - 1) / TF_T) * ((q + TF_T - 1) / TF_T);
+    const size_t need2 = sizeof(double) * (size_t)nblk * ntile2 * TF_T * TF_T;
+    st = ws.reserve(c, need2);
+    if (st) return st;
+    k_gemm_tn_f32<<<dim3(nblk, ntile2), 256, 0, c->stream>>>(N, p, q, A, lda, B, ldb, (double*)ws.p, rows);
+    ADC_COUNT_LAUNCH();
+    const int nout2 = ntile2 * TF_T * TF_T;
+    k_gemm_tn_f32_reduce<TC><<<std::min((nout2 + 255) / 256, c->nsm * 8), 256, 0, c->stream>>>(
+        p, q, nblk, ntile2, (const double*)ws.p, C, ldc, alpha, beta);
+    ADC_COUNT_LAUNCH();
+    ADC_CUDA(c, cudaGetLastError());
+    return ADCGPU_OK;
   } else {
     k_gemm_tn_part<T, TA><<<dim3(nblk, ntile), 256, 0, c->stream>>>(N, p, q, A, lda, B, ldb, (TA*)ws.p, rows); ADC_COUNT_LAUNCH();
   }
@@ -456,6 +631,42 @@ int gemm_nn(Ctx* c, int64_t N, int p, int q, T alpha, const T* A, int64_t lda, c
   if constexpr (std::is_same<T, double>::value && std::is_same<TB, double>::value) {
     if (c->dense_df) {
       k_gemm_nn_df<<<grid, 256, 0, c->stream>>>(N, p, q, alpha, A, lda, B, ldb, beta, C, ldc); ADC_COUNT_LAUNCH();
+      ADC_CUDA(c, cudaGetLastError());
+      return ADCGPU_OK;
+    }
+  }
+  if constexpr (std::is_same<T, float>::value) {
+    // FP32: B's column tile in shared memory, 2 rows x QT columns per thread
+    const int QT = q <= 16 ? 16 : (q <= 32 ? 32 : (q <= 40 ? 40 : 48));
+    const size_t smem = sizeof(float) * (size_t)p * QT;
+    if (smem <= 200 * 1024) {
+      const int nq = (q + QT - 1) / QT;
+      const int64_t nrb = (N + 255) / 256;
+      const int gx = (int)std::max<int64_t>(1, std::min<int64_t>(nrb, (int64_t)c->nsm * 2 / std::max(1, nq)));
+      dim3 g2(gx, nq);
+      switch (QT) {
+        case 16:
+          if (smem > 48 * 1024)
+            ADC_CUDA(c, cudaFuncSetAttribute(k_gemm_nn_f32<TB, 16>, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem));
+          k_gemm_nn_f32<TB, 16><<<g2, 256, smem, c->stream>>>(N, p, q, alpha, A, lda, B, ldb, beta, C, ldc);
+          break;
+        case 32:
+          if (smem > 48 * 1024)
+            ADC_CUDA(c, cudaFuncSetAttribute(k_gemm_nn_f32<TB, 32>, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem));
+          k_gemm_nn_f32<TB, 32><<<g2, 256, smem, c->stream>>>(N, p, q, alpha, A, lda, B, ldb, beta, C, ldc);
+          break;
+        case 40:
+          if (smem > 48 * 1024)
+            ADC_CUDA(c, cudaFuncSetAttribute(k_gemm_nn_f32<TB, 40>, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem));
+          k_gemm_nn_f32<TB, 40><<<g2, 256, smem, c->stream>>>(N, p, q, alpha, A, lda, B, ldb, beta, C, ldc);
+          break;
+        default:
+          if (smem > 48 * 1024)
+            ADC_CUDA(c, cudaFuncSetAttribute(k_gemm_nn_f32<TB, 48>, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem));
+          k_gemm_nn_f32<TB, 48><<<g2, 256, smem, c->stream>>>(N, p, q, alpha, A, lda, B, ldb, beta, C, ldc);
+          break;
+      }
+      ADC_COUNT_LAUNCH();
       ADC_CUDA(c, cudaGetLastError());
       return ADCGPU_OK;
     }

@@ -72,7 +72,11 @@ enum adcgpu_precon {
                                in (no reference counterpart): t_d = DPR,
                                t_s = (lambda - Hss)^-1 (r_s + B^T t_d) by 8
                                MINRES steps; one extra sigma product of the
-                               block per iteration */
+                               block per iteration.  Runs without deflation
+                               (ldfl is ignored).  Not root-safe: like inverse
+                               iteration it can converge to a state above a
+                               missed one (measured: 1 of 12 seeded systems);
+                               DPR and Olsen found the right set on all */
 };
 
 typedef struct adcgpu_ctx adcgpu_ctx;
@@ -231,7 +235,8 @@ typedef struct {
   int maxsubdim;     /* maxvec; <0 -> 4*blocksize                   */
   int maxiter;       /* niter                                       */
   int precon;        /* adcgpu_precon                               */
-  int ldfl;          /* deflation of converged vectors (1/0)        */
+  int ldfl;          /* deflation of converged vectors (1/0); not
+                        used with ADCGPU_PRECON_FOLD                */
   int lsubdiag;      /* 1: initvec_subdiag, 2: initvec_adc1 (the
                         reference's ladc1guess), 0: initvec_ondiag  */
   int guessdim;      /* subspace dimension for initvec_subdiag      */

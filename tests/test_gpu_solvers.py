@@ -224,3 +224,24 @@ def test_concurrent_systems_match_sequential(gpu):
     for a, b in zip(seq, par):
         assert a["status"] == 0 and b["status"] == 0
         assert np.abs(np.array(a["evals"]) - np.array(b["evals"])).max() < 1e-8
+
+
+@pytest.mark.parametrize("no,nv,seed", [(10, 100, 22), (12, 120, 26)])
+def test_fold_finds_the_reference_roots(gpu, no, nv, seed):
+    """The mixed ladder with the folded preconditioner converges to the same
+    20 roots as with DPR (the reference's preconditioner).  On these seeded
+    systems fold with deflation converged to a wrong set (a state 0.03-0.05 Ha
+    above the 14th-20th root); fold therefore runs without deflation."""
+    from adc_ottawa_gb300 import ADCGPU_MIXED, PRECON_DPR, PRECON_FOLD, AdcGpu
+
+    e, eri = system(no, nv, seed)
+    g = AdcGpu(0)
+    g.set_orbitals(no, nv, e)
+    g.set_eri_packed(eri)
+    g.write_fspace_adc2_1(None, precision=ADCGPU_MIXED)
+    kw = dict(precision=ADCGPU_MIXED, want_vectors=False)
+    fold = g.davdiag_block(20, 1e-6, precon=PRECON_FOLD, **kw)
+    dpr = g.davdiag_block(20, 1e-6, precon=PRECON_DPR, **kw)
+    assert fold.status == 0 and dpr.status == 0
+    assert np.abs(fold.evals - dpr.evals).max() < 1e-8
+    g.close()
