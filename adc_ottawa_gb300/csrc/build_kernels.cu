@@ -104,27 +104,41 @@ __global__ void k_ca(Eri E, const double* __restrict__ e, double* __restrict__ c
   ca[(int64_t)a1 * nv + a] = x;
 }
 
-// CB_ph_ph(k,k1), adc_ph.f90:819-912 ("dumbed down" branch), k <= k1.
-__global__ void k_cb(Eri E, const double* __restrict__ e, double* __restrict__ cb) {
+// CB_ph_ph(k,k1), adc_ph.f90:819-912 ("dumbed down" branch), k <= k1, in two
+// passes: every term of the (r, s, u) sum of one pair evaluated in parallel
+// (the reference's expression, operation by operation), then the terms summed
+// in the reference's loop order by one thread per pair.  The result is bit
+// for bit that of the serial loop while the divisions run on all SMs.
+// terms: [pair][(r*nv + s)*no + u], pairs k <= k1 enumerated row by row.
+__global__ void k_cb_terms(Eri E, const double* __restrict__ e, const int2* __restrict__ pairs, int npairs,
+                           double* __restrict__ terms) {
   const int no = E.no, nv = E.nv;
-  int t = blockIdx.x * blockDim.x + threadIdx.x;
-  if (t >= no * no) return;
-  int k = t / no, k1 = t % no;
-  if (k > k1) return;
-  const double ek = e[k], ek1 = e[k1];
+  const int64_t nt = (int64_t)nv * nv * no;
+  for (int64_t x = blockIdx.x * (int64_t)blockDim.x + threadIdx.x; x < npairs * nt;
+       x += (int64_t)gridDim.x * blockDim.x) {
+    const int pi = (int)(x / nt);
+    const int64_t t = x % nt;
+    const int u = (int)(t % no), s = (int)((t / no) % nv), r = (int)(t / ((int64_t)no * nv));
+    const int k = pairs[pi].x, k1 = pairs[pi].y;
+    const double ek = e[k], ek1 = e[k1];
+    double eicd = e[u] - e[no + r] - e[no + s];
+    double DB = (eicd + 0.5 * (ek + ek1)) / ((eicd + ek) * (eicd + ek1));
+    double term = 0.0;
+    term = term + E.VOVO(r, k, s, u) * (2.0 * E.VOVO(r, k1, s, u) - E.VOVO(s, k1, r, u));
+    term = term + E.VOVO(r, u, s, k) * (2.0 * E.VOVO(s, k1, r, u) - E.VOVO(r, k1, s, u));
+    terms[x] = DB * term;
+  }
+}
+
+__global__ void k_cb_sum(const double* __restrict__ terms, const int2* __restrict__ pairs, int npairs, int64_t nt,
+                         int no, double* __restrict__ cb) {
+  const int pi = blockIdx.x * blockDim.x + threadIdx.x;
+  if (pi >= npairs) return;
+  const double* tp = terms + (int64_t)pi * nt;
   double acc = 0.0;
-  for (int r = 0; r < nv; ++r)
-    for (int s = 0; s < nv; ++s)
-      for (int u = 0; u < no; ++u) {
-        double eicd = e[u] - e[no + r] - e[no + s];
-        double DB = (eicd + 0.5 * (ek + ek1)) / ((eicd + ek) * (eicd + ek1));
-        double term = 0.0;
-        term = term + E.VOVO(r, k, s, u) * (2.0 * E.VOVO(r, k1, s, u) - E.VOVO(s, k1, r, u));
-        term = term + E.VOVO(r, u, s, k) * (2.0 * E.VOVO(s, k1, r, u) - E.VOVO(r, k1, s, u));
-        term = DB * term;
-        acc = acc + term;
-      }
-  double x = -0.5 * acc;
+  for (int64_t t = 0; t < nt; ++t) acc = acc + tp[t];
+  const double x = -0.5 * acc;
+  const int k = pairs[pi].x, k1 = pairs[pi].y;
   cb[k * no + k1] = x;
   cb[k1 * no + k] = x;
 }
@@ -623,6 +637,36 @@ int coupling_values(Ctx* c, double* buf, int64_t vbase, int64_t row0, int64_t ro
   return ADCGPU_OK;
 }
 
+// CB_ph_ph for all k <= k1 (two passes: k_cb_terms + k_cb_sum; pairs in
+// batches that keep the term buffer near 1 GiB)
+static int compute_cb(Ctx* c, const Eri& E, double* d_cb) {
+  const int no = E.no, nv = E.nv;
+  const int64_t nt = (int64_t)nv * nv * no;
+  std::vector<int2> pairs;
+  for (int k = 0; k < no; ++k)
+    for (int k1 = k; k1 < no; ++k1) pairs.push_back(make_int2(k, k1));
+  const int np = (int)pairs.size();
+  const int batch = (int)std::max<int64_t>(1, std::min<int64_t>(np, ((int64_t)1 << 27) / nt));
+  int2* d_pairs = nullptr;
+  double* d_terms = nullptr;
+  int st = dmalloc(c, (void**)&d_pairs, sizeof(int2) * np);
+  if (!st) st = dmalloc(c, (void**)&d_terms, sizeof(double) * (size_t)batch * nt);
+  if (!st && cudaMemcpyAsync(d_pairs, pairs.data(), sizeof(int2) * np, cudaMemcpyHostToDevice, c->stream) != cudaSuccess)
+    st = set_err(c, ADCGPU_CUDA_ERROR, "CB pairs");
+  for (int p0 = 0; !st && p0 < np; p0 += batch) {
+    const int nb = std::min(batch, np - p0);
+    k_cb_terms<<<grid_for(c, (int64_t)nb * nt, 256), 256, 0, c->stream>>>(E, c->d_e, d_pairs + p0, nb, d_terms);
+    ADC_COUNT_LAUNCH();
+    k_cb_sum<<<(nb + 31) / 32, 32, 0, c->stream>>>(d_terms, d_pairs + p0, nb, nt, no, d_cb);
+    ADC_COUNT_LAUNCH();
+    if (cudaGetLastError() != cudaSuccess) st = set_err(c, ADCGPU_CUDA_ERROR, "CB kernels");
+  }
+  if (!st && cudaStreamSynchronize(c->stream) != cudaSuccess) st = set_err(c, ADCGPU_CUDA_ERROR, "CB kernels");
+  dfree(c, d_terms);
+  dfree(c, d_pairs);
+  return st;
+}
+
 int build_matrix(Ctx* c) {
   const Geometry& G = c->geom;
   const int no = G.no, nv = G.nv;
@@ -663,7 +707,7 @@ int build_matrix(Ctx* c) {
     ADC_COUNT_LAUNCH();
   } else {
     k_ca<<<(int)((nv * (int64_t)nv + 127) / 128), 128, 0, s>>>(E, c->d_e, d_ca); ADC_COUNT_LAUNCH();
-    k_cb<<<(no * no + 63) / 64, 64, 0, s>>>(E, c->d_e, d_cb); ADC_COUNT_LAUNCH();
+    ST(compute_cb(c, E, d_cb));
     k_cc_tables<false><<<grid_for(c, n1 * n1, 256), 256, 0, s>>>(E, c->d_e, d_X, d_D1); ADC_COUNT_LAUNCH();
     ADC_CUDA(c, cudaGetLastError());
     k_phph<false><<<tiles, dim3(PT, PT), 0, s>>>(E, c->d_e, d_X, d_D1, d_ca, d_cb, c->d_A, c->d_diag, d_kept);
@@ -785,7 +829,7 @@ int build_matrix_cvs(Ctx* c, const int32_t* kpq, int64_t ndim, int ncore, const 
     if (n2 > 0)
       ADC_CUDA(c, cudaMemcpyAsync(d_cols, kpq + 7 * (cn1 + 1), sizeof(int32_t) * 7 * n2, cudaMemcpyHostToDevice, s));
     k_ca<<<(int)((nv * (int64_t)nv + 127) / 128), 128, 0, s>>>(E, c->d_e, d_ca); ADC_COUNT_LAUNCH();
-    k_cb<<<(no * no + 63) / 64, 64, 0, s>>>(E, c->d_e, d_cb); ADC_COUNT_LAUNCH();
+    ST(compute_cb(c, E, d_cb));
     k_cc_tables<false><<<grid_for(c, n1 * n1, 256), 256, 0, s>>>(E, c->d_e, d_X, d_D1); ADC_COUNT_LAUNCH();
     k_phph_cvs<<<grid_for(c, (int64_t)cn1 * cn1, 128), 128, 0, s>>>(E, c->d_e, d_X, d_D1, d_ca, d_cb, d_sidx, cn1,
                                                                      c->d_Ac, c->d_diag, d_kept);

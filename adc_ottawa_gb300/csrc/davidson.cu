@@ -601,7 +601,11 @@ int davidson_solve(Ctx* c, const adcgpu_dav_params* p, double* evals, double* ev
                        : ((p->refine_block >= nstates && p->refine_block <= blocksize) ? p->refine_block : blocksize);
     F.c = c; F.N = N; F.nstates = nstates; F.blocksize = rblock;
     F.maxvec = (p->refine > 1 ? p->refine : 4) * rblock;
-    F.niter = p->maxiter; F.ipre = precon64;
+    // the learned correction is trained on whole FP64 solves; from the FP32
+    // phase's Ritz block (residuals near 1e-5) it stalled (100 FP64
+    // iterations without convergence at nocc=16/nvirt=180), so the
+    // refinement uses its DPR fallback
+    F.niter = p->maxiter; F.ipre = precon64 == ADCGPU_PRECON_MLP ? ADCGPU_PRECON_DPR : precon64;
     F.ldeflate = deflate; F.tol = p->davtol; F.hii = c->d_diag;
     int it2 = 0, nc2 = 0, nout = 0;
     // the refinement's subspace GEMMs run in double-float on the FP32 pipe

@@ -622,6 +622,22 @@ template <> struct Vec4<df> {
   }
 };
 
+// Vec4 with the two 16-byte halves of a double-float group loaded in the
+// order given by h (0: first half first).  Lanes that read the same bank set
+// are given opposite h, so each quarter-warp's 16-byte loads fall on disjoint
+// banks; for the one-word types the load is Vec4::ld.
+template <typename S> struct Vec4h {
+  __device__ __forceinline__ static void ld(const S* p, S (&v)[4], int) { Vec4<S>::ld(p, v); }
+};
+template <> struct Vec4h<df> {
+  __device__ __forceinline__ static void ld(const df* p, df (&v)[4], int h) {
+    const float4* q = reinterpret_cast<const float4*>(p);
+    const float4 first = q[h], second = q[1 - h];
+    const float4 q0 = h ? second : first, q1 = h ? first : second;
+    v[0] = df{q0.x, q0.y}; v[1] = df{q0.z, q0.w}; v[2] = df{q1.x, q1.y}; v[3] = df{q1.z, q1.w};
+  }
+};
+
 // 8 values to 16-byte aligned shared memory as vector stores
 template <typename S> struct Store8;
 template <> struct Store8<float> {
@@ -691,6 +707,7 @@ __global__ void __launch_bounds__(256, 1) k_sigma_tile(GeomDev g, const int2* __
                                                     int64_t ld1) {
   typedef typename AR::S S;
   constexpr int RT = TILE_RT;
+  static_assert((MT & (MT - 1)) == 0, "the W1 accumulator swizzle needs a power-of-two column tile");
   extern __shared__ __align__(16) unsigned char smem_raw[];
   const int no = g.no, nv = g.nv, noP = g.noP, nvP = g.nvP;
   const int64_t n1 = g.n1;
@@ -776,7 +793,7 @@ __global__ void __launch_bounds__(256, 1) k_sigma_tile(GeomDev g, const int2* __
         for (int k4 = ks; k4 < K / 4; k4 += SPL) {
           S a[4][4], x[CT][4];
 #pragma unroll
-          for (int i = 0; i < 4; ++i) Vec4<S>::ld(sCD + (r0 + i) * CDS + 4 * k4, a[i]);
+          for (int i = 0; i < 4; ++i) Vec4h<S>::ld(sCD + (r0 + i) * CDS + 4 * k4, a[i], mt & 1);
 #pragma unroll
           for (int cc = 0; cc < CT; ++cc) Vec4<S>::ld(sX + (c0 + cc) * KP + 4 * k4, x[cc]);
 #pragma unroll
@@ -819,18 +836,24 @@ __global__ void __launch_bounds__(256, 1) k_sigma_tile(GeomDev g, const int2* __
 #pragma unroll 2
         for (int rr = 0; rr < RT; ++rr) {
           S a[4], v[4];
-          Vec4<S>::ld(sCD + rr * CDS + 4 * kq, a);
+          Vec4h<S>::ld(sCD + rr * CDS + 4 * kq, a, (kq >> 2) & 1);
           Vec4<S>::ld(sV2 + rr * MT + 4 * cg, v);
 #pragma unroll
           for (int i = 0; i < 4; ++i)
 #pragma unroll
             for (int cc = 0; cc < 4; ++cc) AR::fma(sm[i][cc], a[i], v[cc]);
         }
+        // sW1 row k holds column c at c ^ (k/4 mod MT): consecutive kq of a
+        // warp then touch different banks
+        const int swz = kq & (MT - 1);
 #pragma unroll
         for (int i = 0; i < 4; ++i) {
-          S* w = sW1 + (4 * kq + i) * MT + 4 * cg;
+          S* w = sW1 + (4 * kq + i) * MT;
 #pragma unroll
-          for (int cc = 0; cc < 4; ++cc) w[cc] = AR::add(w[cc], sm[i][cc]);
+          for (int cc = 0; cc < 4; ++cc) {
+            const int pos = (4 * cg + cc) ^ swz;
+            w[pos] = AR::add(w[pos], sm[i][cc]);
+          }
         }
       }
       // W1 (A): runs of equal a' reduced, then added atomically
@@ -853,7 +876,7 @@ __global__ void __launch_bounds__(256, 1) k_sigma_tile(GeomDev g, const int2* __
     }
     __syncthreads();
     for (int o = tid; o < K * MT; o += 256) {
-      const int k = o / MT, c = o - k * MT;
+      const int k = o / MT, c = (o - k * MT) ^ ((k >> 2) & (MT - 1));
       const int seg = k / nvP, a = k - seg * nvP;
       const T v = AR::value(sW1[o]);
       if (a < nv && c < mcols && v != T(0))

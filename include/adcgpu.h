@@ -67,7 +67,8 @@ enum adcgpu_precision {
 enum adcgpu_precon {
   ADCGPU_PRECON_DPR = 1,    /* dpr   block_davidson.f90:1288-1342 */
   ADCGPU_PRECON_OLSEN = 2,  /* olsen block_davidson.f90:1346-1419 */
-  ADCGPU_PRECON_MLP = 3,    /* learned correction, DPR as fallback */
+  ADCGPU_PRECON_MLP = 3,    /* learned correction, DPR as fallback (and in
+                               the FP64 refinement of ADCGPU_MIXED) */
   ADCGPU_PRECON_FOLD = 4    /* singles block with the doubles residual folded
                                in (no reference counterpart): t_d = DPR,
                                t_s = (lambda - Hss)^-1 (r_s + B^T t_d) by 8
