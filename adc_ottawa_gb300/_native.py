@@ -108,6 +108,7 @@ SIGNATURES = {
                                         C.POINTER(C.c_int)]),
     "adcgpu_sigma_autotune": (C.c_int, [_vp, C.c_int, C.POINTER(C.c_int), C.POINTER(C.c_int), _dp]),
     "adcgpu_sigma_set_shape": (C.c_int, [_vp, C.c_int, C.c_int, C.c_int]),
+    "adcgpu_gram_f32": (C.c_int, [_vp, C.c_int64, C.c_int, C.c_int, _vp, C.c_int64, _vp, C.c_int64, _vp, C.c_int]),
 }
 
 _lib = None

@@ -32,7 +32,9 @@ SOURCES = [
     ("build_kernels.cu", ["--fmad=false"]),
     ("sigma.cu", []),
     ("sigma_umma.cu", []),
+    ("sigma_ab.cu", []),
     ("dense.cu", []),
+    ("dense_umma.cu", []),
     ("precond_fold.cu", []),
     ("davidson.cu", []),
     ("lanczos.cu", []),

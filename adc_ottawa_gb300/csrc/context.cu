@@ -138,6 +138,7 @@ int adcgpu_ctx_destroy(adcgpu_ctx* h) {
   free_matrix(c);
   free_eri(c);
   free_mlp(c);
+  gram_free(c);
   dfree(c, c->d_e);
   dfree(c, c->d_sil);
   dfree(c, c->d_dpl);

@@ -592,6 +592,10 @@ int gemm_tn(Ctx* c, Workspace& ws, int64_t N, int p, int q, const T* A, int64_t 
       k_gemm_tn_part<T, TA><<<dim3(nblk, ntile), 256, 0, c->stream>>>(N, p, q, A, lda, B, ldb, (TA*)ws.p, rows); ADC_COUNT_LAUNCH();
     }
   } else if constexpr (std::is_same<T, float>::value && std::is_same<TA, double>::value) {
+    if constexpr (std::is_same<TC, double>::value) {
+      // the tensor cores (three BF16 slices per value), q <= 48
+      if (gram_umma_usable(c, N, p, q)) return gram_umma(c, ws, N, p, q, A, lda, B, ldb, C, ldc, alpha, beta);
+    }
     // FP32 inputs: 64 x 64 tiles with 4 x 4 float4 sub-tiles per thread
     const int ntile2 = ((p + TF_T - 1) / TF_T) * ((q + TF_T - 1) / TF_T);
     const size_t need2 = sizeof(double) * (size_t)nblk * ntile2 * TF_T * TF_T;

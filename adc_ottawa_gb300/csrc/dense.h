@@ -47,4 +47,11 @@ int residuals(Ctx* c, Workspace& ws, int64_t N, int nb, const T* X, const T* WY,
 template <typename TS, typename TD>
 int convert(Ctx* c, const TS* x, TD* y, int64_t n);
 
+// Tensor-core Gram product of FP32 inputs (dense_umma.cu): C(p x q, FP64,
+// ldc) = beta C + alpha A^T B for q <= 48, FP32-accurate products.
+bool gram_umma_usable(Ctx* c, int64_t N, int p, int q);
+int gram_umma(Ctx* c, Workspace& ws, int64_t N, int p, int q, const float* A, int64_t lda, const float* B,
+              int64_t ldb, double* C, int ldc, double alpha, double beta);
+
+
 }  // namespace adcgpu

@@ -298,6 +298,8 @@ struct Ctx {
   std::unordered_map<void*, size_t> dev_allocs;   // dmalloc pointer -> size
   // learned preconditioner (MlpState, mlp.cu); DPR is used when absent
   void* mlp = nullptr;
+  // tensor-core Gram products (GramPlan, dense_umma.cu): error word, switch
+  void* gram = nullptr;
   // CVS matrix (write_fspace_adc2_1_cvs): singles on core holes only; the
   // ph-ph block dense (diagonal included), the coupling block as CSR over the
   // doubles rows (kept entries, column = CVS single index)
@@ -409,6 +411,8 @@ struct SigmaPlan {
   void* umma = nullptr;       // tensor-core pass plan (sigma_umma.cu), built on first use
   int umma_item_rows = 4096;  // rows per tensor-core work item (autotuned)
   int umma_off = 0;           // 1: the tensor-core pass is not used
+  void* ab = nullptr;         // compact segment-A/B tables (sigma_ab.cu), built on first use
+  int ab_off = 0;             // 1: segments A/B through pass 2 / pass 3 instead
   std::vector<DirectChunk> dchunks;   // direct path: chunks with their work-list ranges
 };
 int prepare_desc(Ctx* c);
@@ -418,15 +422,27 @@ int sigma_fp64(Ctx* c, int m, const double* dV, int64_t ldv, double* dW, int64_t
 int sigma_fp32(Ctx* c, int m, const float* dV, int64_t ldv, float* dW, int64_t ldw);
 int prepare_mixed(Ctx* c);
 void free_mlp(Ctx* c);
+// dense_umma.cu: release the tensor-core Gram state; switch it off (1) or on
+void gram_free(Ctx* c);
+int gram_set_off(Ctx* c, int off);
 
 // sigma_umma.cu : the tensor-core (tcgen05) pass of the BF16 sigma product
 bool umma_supported(const Ctx* c);
 int umma_prepare(Ctx* c, void*& handle, int item_rows);
 void umma_free(Ctx* c, void*& handle);
 int umma_launch(Ctx* c, void* handle, const float* V, int64_t ldv, int m, float* W, int64_t ldw, double* W1,
-                int64_t ld1);
+                int64_t ld1, int seg_a);
 int umma_runs(void* handle, const int2** runs, int* nruns);
 int umma_check(Ctx* c, void* handle);
+
+// sigma_ab.cu : segments A and B of the mixed-precision sigma product in
+// compact form (tables copied from the BF16 or FP32 value store on first use)
+bool ab_supported(const Ctx* c);
+void ab_free(Ctx* c, void*& handle);
+void ab_invalidate(void* handle);
+template <typename TV>
+int ab_launch(Ctx* c, void*& handle, const TV* Bt, bool do_a, const float* V, int64_t ldv, int m, float* W,
+              int64_t ldw, double* W1, int64_t ld1);
 
 // hostla.cpp : dense host linear algebra (FP64)
 // Symmetric eigen-decomposition (Householder tridiagonalisation + implicit QL).

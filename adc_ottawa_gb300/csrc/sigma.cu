@@ -1392,12 +1392,19 @@ int sigma_impl(Ctx* c, int m, const T* dV, int64_t ldv, T* dW, int64_t ldw, cons
         const int2* runs = nullptr;
         int nruns = 0;
         ST(umma_runs(plan->umma, &runs, &nruns));
+        const bool ab = !P->ab_off && ab_supported(c);
         for (; c0 < m;) {
           const int nc = std::min(m - c0, 48);
           const T* V = dV + (int64_t)c0 * ldv;
           T* W = dW + (int64_t)c0 * ldw;
           TAcc* W1 = W1base + (int64_t)c0 * n1;
-          ST(umma_launch(c, plan->umma, V, ldv, nc, W, ldw, W1, n1));
+          ST(umma_launch(c, plan->umma, V, ldv, nc, W, ldw, W1, n1, ab ? 0 : 1));
+          if (ab) {
+            // segments A and B in compact form, W2 rows updated in place
+            ST(ab_launch<TV>(c, plan->ab, BtP, true, V, ldv, nc, W, ldw, W1, n1));
+            c0 += nc;
+            continue;
+          }
           for (int b0 = 0; P->nitems && b0 < nc;) {
             const int lb = nc - b0, mc = lb >= 8 ? 8 : (lb >= 4 ? 4 : (lb >= 2 ? 2 : 1));
             ST((launch_p2<T, TV, TAcc>(c, g, P, mc, BtP, V + (int64_t)b0 * ldv, ldv, W + (int64_t)b0 * ldw, ldw,
@@ -1441,6 +1448,14 @@ int sigma_impl(Ctx* c, int m, const T* dV, int64_t ldv, T* dW, int64_t ldw, cons
       if (mt == 16) ST((launch_tile<T, TV, TAcc, 16>(c, g, P, BtP, diag, V, ldv, ncols, W, ldw, W1, ld1, smem)));
       else ST((launch_tile<T, TV, TAcc, 8>(c, g, P, BtP, diag, V, ldv, ncols, W, ldw, W1, ld1, smem)));
       ADC_CUDA(c, cudaGetLastError());
+      if constexpr (std::is_same<T, float>::value && std::is_same<TV, float>::value) {
+        if (!P->ab_off && !c->direct && ab_supported(c)) {
+          // segment B (the tile did segment A) in compact form
+          ST(ab_launch<TV>(c, plan->ab, BtP, false, V, ldv, ncols, W, ldw, W1, ld1));
+          c0 += ncols;
+          continue;
+        }
+      }
       // segment B: pass 2 over the same columns
       int b0 = 0;
       while (P->nitems && b0 < ncols) {
@@ -1604,6 +1619,7 @@ void free_sigma_plan(Ctx* c) {
   dfree(c, plan->d_titems);
   dfree(c, plan->d_acc);
   umma_free(c, plan->umma);
+  ab_free(c, plan->ab);
   delete plan;
   c->sigma_plan = nullptr;
 }
@@ -1620,6 +1636,8 @@ int prepare_mixed(Ctx* c) {
   k_to_bf16<<<c->nsm * 8, 256, 0, c->stream>>>(c->d_Bt, (__nv_bfloat16*)c->d_Bt16, G.off[5]); ADC_COUNT_LAUNCH();
   k_to_f32<<<c->nsm * 8, 256, 0, c->stream>>>(c->d_Bt, c->d_Bt32, G.off[5]); ADC_COUNT_LAUNCH();
   ADC_CUDA(c, cudaGetLastError());
+  // the value stores were rewritten: the compact segment-A/B tables follow
+  if (SigmaPlan* plan = reinterpret_cast<SigmaPlan*>(c->sigma_plan)) ab_invalidate(plan->ab);
   return ADCGPU_OK;
 }
 
@@ -1711,6 +1729,14 @@ extern "C" int adcgpu_sigma_set_shape(adcgpu_ctx* h, int chunk, int mc_fp64, int
   plan->staged = ((mc_fp64 | mc_fp32) & 8) ? 1 : 0;
   plan->tiled = ((mc_fp64 | mc_fp32) & 16) ? 0 : (((mc_fp64 | mc_fp32) & 32) ? 2 : 1);
   plan->umma_off = ((mc_fp64 | mc_fp32) & 64) ? 1 : 0;
+  // 128: segments A/B through pass 2 and pass 3 instead of the compact kernels
+  plan->ab_off = ((mc_fp64 | mc_fp32) & 128) ? 1 : 0;
+  // 256: a mixed-precision matrix's sigma product reads the FP32 value store
+  // (the Davidson ladder's FP32 phase) instead of the BF16 one
+  c->mixed_bf16 = ((mc_fp64 | mc_fp32) & 256) ? 0 : 1;
+  // 512: the FP32 Gram products (V^T W) on the CUDA cores instead of the
+  // tensor cores
+  gram_set_off(c, ((mc_fp64 | mc_fp32) & 512) ? 1 : 0);
   plan->mc_cap[0] = std::min(mc_fp64 & 7, 2);
   plan->mc_cap[1] = std::min(mc_fp32 & 7, 4);
   return build_chunks(c, chunk);

@@ -26,14 +26,18 @@
 //                        N = 2 NP, K = 128 rows) into D2[slot], summed over
 //                        the item.
 //   warps 2-9          : X and V2 operands (hi/lo split into swizzled
-//                        shared memory), the W2 part of segment A and the
-//                        diagonal term on the CUDA cores, the D1 epilogue
-//                        (W2 rows) and, at the end of an item, D2 into the
-//                        FP64 W1 accumulator.  Thread = tile row = TMEM
-//                        lane; two warps per lane quarter split the columns.
-// Segment B stays with pass 2 (k_sigma_p2 in sigma.cu), the W1 part of
-// segment A with k_sigma_p3 and the dense singles block with k_singles_gemm.  Every wait is bounded: a lost arrival sets the
-// error word and the kernel ends (the host reports ADCGPU_DEVICE_TIMEOUT).
+//                        shared memory), the diagonal term (and, with
+//                        seg_a, the W2 part of segment A) on the CUDA cores,
+//                        the D1 epilogue (W2 rows) and, at the end of an
+//                        item, D2 into the FP64 W1 accumulator.  Thread =
+//                        tile row = TMEM lane; two warps per lane quarter
+//                        split the columns.
+// Segments A and B run after this pass in the compact A/B kernels
+// (sigma_ab.cu); without them (seg_a set), segment B runs in pass 2
+// (k_sigma_p2 in sigma.cu) and the W1 part of segment A in k_sigma_p3.  The
+// dense singles block is k_singles_gemm.  Every wait is bounded: a lost
+// arrival sets the error word and the kernel ends (the host reports
+// ADCGPU_DEVICE_TIMEOUT).
 #include <cuda.h>
 #include <cudaTypedefs.h>
 #include <cuda_bf16.h>
@@ -94,7 +98,7 @@ __global__ void __launch_bounds__(UMMA_THREADS, 1)
     k_sigma_umma(GeomDev g, const int2* __restrict__ items, int nitems, const __grid_constant__ UmmaMaps maps,
                  const __nv_bfloat16* __restrict__ Bt, const float* __restrict__ diag, const float* __restrict__ V,
                  int64_t ldv, int mcols, float* __restrict__ W, int64_t ldw, double* __restrict__ W1, int64_t ld1,
-                 int* __restrict__ err) {
+                 int seg_a, int* __restrict__ err) {
   constexpr int N2 = 2 * NP;                       // MMA N (hi | lo)
   constexpr int BOXB = umma_box_bytes(NP);
   constexpr uint32_t TCOLS = umma_tmem_cols<NP>();
@@ -326,7 +330,7 @@ __global__ void __launch_bounds__(UMMA_THREADS, 1)
         float sa[UMMA_NOP];
 #pragma unroll
         for (int k = 0; k < UMMA_NOP; ++k) sa[k] = 0.f;
-        if (valid) {
+        if (valid && seg_a) {
           const __nv_bfloat16* rp = Bt + g.off[cls] + (int64_t)(row - g.start[cls]) * L;
 #pragma unroll
           for (int k8 = 0; k8 < UMMA_NOP; k8 += 8) {
@@ -348,7 +352,7 @@ __global__ void __launch_bounds__(UMMA_THREADS, 1)
         // the same a' (most of them: a' changes once per run of nv - 1 - a'
         // rows) share one cooperative load of those V values, spread over
         // the lanes (k fastest: coalesced) and broadcast by shuffles.
-        {
+        if (seg_a) {
           constexpr unsigned FULL = 0xffffffffu;
           constexpr int NVL = (NH * UMMA_NOP + 31) / 32;
           unsigned pending = __ballot_sync(FULL, valid);
@@ -484,7 +488,7 @@ size_t umma_smem_bytes(int nslot) {
 
 template <int NP>
 int launch_umma_np(Ctx* c, UmmaPlan* u, const float* V, int64_t ldv, int m, float* W, int64_t ldw, double* W1,
-                   int64_t ld1) {
+                   int64_t ld1, int seg_a) {
   const int smax = smem_optin_max(c);
   int nslot = umma_nslot<NP>(smax);
   nslot = std::min(nslot, 6);
@@ -497,7 +501,7 @@ int launch_umma_np(Ctx* c, UmmaPlan* u, const float* V, int64_t ldv, int m, floa
     ADC_CUDA(c, cudaFuncSetAttribute(kern, cudaFuncAttributeMaxDynamicSharedMemorySize, smax));
     kern<<<grid, UMMA_THREADS, smem, c->stream>>>(g, u->d_items, u->nitems, u->maps,
                                                   (const __nv_bfloat16*)c->d_Bt16, c->d_diag32, V, ldv, m, W, ldw, W1,
-                                                  ld1, u->d_err);
+                                                  ld1, seg_a, u->d_err);
     ADC_COUNT_LAUNCH();
     ADC_CUDA(c, cudaGetLastError());
     return ADCGPU_OK;
@@ -601,14 +605,16 @@ int umma_runs(void* handle, const int2** runs, int* nruns) {
   return ADCGPU_OK;
 }
 
-// The C|D products and the W2 part of segment A for m <= 48 columns.
+// The C|D products and, when seg_a is set, the W2 part of segment A for
+// m <= 48 columns (otherwise segment A is left to the compact A/B kernels of
+// sigma_ab.cu).
 int umma_launch(Ctx* c, void* handle, const float* V, int64_t ldv, int m, float* W, int64_t ldw, double* W1,
-                int64_t ld1) {
+                int64_t ld1, int seg_a) {
   UmmaPlan* u = reinterpret_cast<UmmaPlan*>(handle);
   if (!u || m <= 0 || m > 48) return set_err(c, ADCGPU_BAD_INPUT, "tensor-core sigma pass: columns");
-  if (m <= 16) return launch_umma_np<16>(c, u, V, ldv, m, W, ldw, W1, ld1);
-  if (m <= 32) return launch_umma_np<32>(c, u, V, ldv, m, W, ldw, W1, ld1);
-  return launch_umma_np<48>(c, u, V, ldv, m, W, ldw, W1, ld1);
+  if (m <= 16) return launch_umma_np<16>(c, u, V, ldv, m, W, ldw, W1, ld1, seg_a);
+  if (m <= 32) return launch_umma_np<32>(c, u, V, ldv, m, W, ldw, W1, ld1, seg_a);
+  return launch_umma_np<48>(c, u, V, ldv, m, W, ldw, W1, ld1, seg_a);
 }
 
 // Reads the kernel's error word (waits for the stream) and clears it.

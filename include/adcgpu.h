@@ -465,8 +465,22 @@ int adcgpu_sigma_autotune(adcgpu_ctx* ctx, int m, int* best_chunk, int* best_mc,
 /* Applies a launch shape (e.g. from the autotuner's cache).  In mc_fp64 /
    mc_fp32, bits 0-2 give the columns per pass, bit 3 selects the staged
    per-warp pass 1, bit 4 the per-warp pass 1 instead of the tiled one, bit
-   5 the CUDA-core tiled pass 1 instead of the tensor-core one (BF16 values). */
+   5 the CUDA-core tiled pass 1 instead of the tensor-core one (BF16 values),
+   bit 6 switches the tcgen05 sigma pass off, bit 7 runs segments A/B through
+   the per-(slab, b') pass 2 and per-run pass 3 instead of the compact
+   kernels, bit 8 makes a mixed-precision matrix's sigma product read the
+   FP32 value store instead of the BF16 one, bit 9 keeps the FP32 Gram
+   products (adcgpu_gram_f32 and the solvers' V^T W) on the CUDA cores. */
 int adcgpu_sigma_set_shape(adcgpu_ctx* ctx, int chunk, int mc_fp64, int mc_fp32);
+
+/* The solvers' tall-skinny Gram product on device FP32 arrays: C(p x q,
+   FP64, column-major, ldc) = A(N x p, lda)^T B(N x q, ldb), as calcrmat's
+   dgemm (block_davidson.f90:954-967) and the projections of the block
+   orthogonalisation (:1226-1284) form it on the mixed-precision phases.  For
+   q <= 48 it runs on the tensor cores (each value split into three BF16
+   slices, FP32-accurate products); otherwise on the CUDA cores. */
+int adcgpu_gram_f32(adcgpu_ctx* ctx, int64_t N, int p, int q, const void* dA, int64_t lda, const void* dB,
+                    int64_t ldb, double* dC, int ldc);
 
 #ifdef __cplusplus
 }

@@ -86,3 +86,55 @@ def test_umma_mixed_davidson_matches_oracle(gpu):
     assert res.status == 0 and st == 0
     assert np.abs(res.evals - ev).max() < 1e-6
     g.close()
+
+
+def _sigma_flags(g, x, ld, flags):
+    import torch
+
+    from adc_ottawa_gb300._native import lib
+
+    assert lib().adcgpu_sigma_set_shape(g._h, 64, 2, 4 | flags) == 0
+    w = torch.full_like(x, 3.0)
+    torch.cuda.synchronize()
+    st = lib().adcgpu_sigma_device(g._h, x.shape[0], C.c_void_p(x.data_ptr()), C.c_void_p(w.data_ptr()), ld)
+    assert st == 0, lib().adcgpu_last_error(g._h)
+    out = w.cpu().numpy().T
+    assert lib().adcgpu_sigma_set_shape(g._h, 64, 2, 4) == 0
+    return out
+
+
+@pytest.mark.parametrize("no,nv,seed", [(6, 40, 3), (10, 110, 2024), (3, 37, 9)])
+def test_compact_segments_match_pass2_and_oracle(gpu, no, nv, seed):
+    """Segments A and B in compact form (csrc/sigma_ab.cu: per-slab tables
+    of the entries that do not depend on the other virtual index, plus the
+    stored coincident entries) against the per-(slab, b') pass 2 and the
+    per-run pass 3 over the same values: BF16 values on the tensor-core pass
+    (flag 128 switches the compact kernels off) and FP32 values on the tiled
+    pass (flag 256), at 1e-5 relative; both against the oracle's FP64
+    product at the value precision.  Column counts cover partial 4-column
+    groups, more than one 48-column pass and a padded leading dimension;
+    (3, 37) gives noP = 8 and an odd number of virtuals."""
+    import torch
+
+    g, e, eri = _mixed(no, nv, seed)
+    N = g.ndim
+    ref = oracle.Matrix.build(no, nv, e, eri)
+    gen = torch.Generator(device="cuda").manual_seed(7 * no + nv)
+    for fp32_values in (False, True):
+        base = 256 if fp32_values else 0
+        for m, pad in ((1, 0), (6, 2), (16, 0), (21, 3), (40, 0), (53, 1)):
+            ld = N + pad
+            x = torch.randn(m, ld, device="cuda", dtype=torch.float32, generator=gen)
+            w_ab = _sigma_flags(g, x, ld, base)
+            w_p2 = _sigma_flags(g, x, ld, base | 128)
+            assert np.all(w_ab[N:] == 3.0), "padding rows written"
+            w_ab, w_p2 = w_ab[:N], w_p2[:N]
+            assert np.isfinite(w_ab).all()
+            scale = np.abs(w_p2).max()
+            assert np.abs(w_ab - w_p2).max() <= SAME_TOL * scale, (fp32_values, m, np.abs(w_ab - w_p2).max() / scale)
+            if m in (6, 40):
+                xs = x.cpu().numpy().T[:N].astype(np.float64)
+                w64 = ref.matvec(xs)
+                tol = 1e-5 if fp32_values else BF16_TOL
+                assert np.abs(w_ab - w64).max() <= tol * np.abs(w64).max(), (fp32_values, m)
+    g.close()
