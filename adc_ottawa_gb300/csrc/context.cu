@@ -71,7 +71,8 @@ static void free_matrix(Ctx* c) {
   join_diag_order(c);
   c->diag_order.clear();
   void** ps[] = {(void**)&c->d_diag, (void**)&c->d_A, (void**)&c->d_Bt, (void**)&c->d_A32, (void**)&c->d_Bt16,
-                 (void**)&c->d_Bt32, (void**)&c->d_diag32, (void**)&c->d_rowcount, &c->d_ws};
+                 (void**)&c->d_Bt32, (void**)&c->d_diag32, (void**)&c->d_rowcount, &c->d_ws,
+                 (void**)&c->d_Bt16s[0], (void**)&c->d_Bt16s[1]};
   for (void** p : ps) {
     dfree(c, *p);
     *p = nullptr;

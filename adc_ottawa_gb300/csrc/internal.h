@@ -271,6 +271,8 @@ struct Ctx {
   float* d_A32 = nullptr;         // mixed-precision copies
   uint16_t* d_Bt16 = nullptr;     // bf16 bits of B^T values
   float* d_Bt32 = nullptr;        // fp32 B^T values (when bf16 is not safe)
+  uint16_t* d_Bt16s[2] = {nullptr, nullptr};   // mid and lo BF16 slices of the fp32 values
+                                               // (hi = d_Bt16), for the tcgen05 FP32-value pass
   float* d_diag32 = nullptr;
   int mixed_bf16 = 1;             // 1: B^T stored as bf16, 0: fp32
   int dense_df = 0;               // FP64 GEMMs in double-float on the FP32 pipe
@@ -408,6 +410,8 @@ struct SigmaPlan {
   int ntitems = 0;
   void* d_acc = nullptr;      // FP64 accumulator of the singles rows (FP32 path)
   size_t acc_bytes = 0;
+  void* d_sk = nullptr;       // split-K partials of the FP32 singles block
+  size_t sk_bytes = 0;
   void* umma = nullptr;       // tensor-core pass plan (sigma_umma.cu), built on first use
   int umma_item_rows = 4096;  // rows per tensor-core work item (autotuned)
   int umma_off = 0;           // 1: the tensor-core pass is not used
@@ -434,6 +438,10 @@ int umma_launch(Ctx* c, void* handle, const float* V, int64_t ldv, int m, float*
                 int64_t ld1, int seg_a);
 int umma_runs(void* handle, const int2** runs, int* nruns);
 int umma_check(Ctx* c, void* handle);
+bool umma_geometry_ok(const Geometry& G);
+bool umma3_supported(const Ctx* c);
+int umma3_launch(Ctx* c, void* handle, const float* V, int64_t ldv, int m, float* W, int64_t ldw, double* W1,
+                 int64_t ld1);
 
 // sigma_ab.cu : segments A and B of the mixed-precision sigma product in
 // compact form (tables copied from the BF16 or FP32 value store on first use)

@@ -1185,7 +1185,8 @@ __global__ void __launch_bounds__(256) k_singles(int n1, const T* __restrict__ A
 template <typename T>
 __global__ void __launch_bounds__(128) k_singles_gemm(int n1, const T* __restrict__ A, const T* __restrict__ diag,
                                                       const T* __restrict__ V, int64_t ldv, T* __restrict__ W,
-                                                      int64_t ldw, int m) {
+                                                      int64_t ldw, int m, T* __restrict__ part = nullptr,
+                                                      int kchunk = 0) {
   __shared__ __align__(16) T sA[32][36];   // sA[k][r]
   __shared__ T sV[32][33];                 // sV[k][c]
   const int tid = threadIdx.x;
@@ -1194,15 +1195,18 @@ __global__ void __launch_bounds__(128) k_singles_gemm(int n1, const T* __restric
   T acc[4][2];
 #pragma unroll
   for (int i = 0; i < 4; ++i) { acc[i][0] = T(0); acc[i][1] = T(0); }
-  for (int k0 = 0; k0 < n1; k0 += 32) {
+  // split K (part != null): this block sums k in [kbeg, kend) into part
+  const int kbeg = part ? blockIdx.z * kchunk : 0;
+  const int kend = part ? min(n1, kbeg + kchunk) : n1;
+  for (int k0 = kbeg; k0 < kend; k0 += 32) {
     __syncthreads();
 #pragma unroll
     for (int l = tid; l < 32 * 32; l += 128) {
       const int kk = l & 31, rr = l >> 5;
       const int r = r0 + rr, k = k0 + kk;
-      sA[kk][rr] = (r < n1 && k < n1) ? A[(int64_t)r * n1 + k] : T(0);
+      sA[kk][rr] = (r < n1 && k < kend) ? A[(int64_t)r * n1 + k] : T(0);
       const int c = c0 + rr;
-      sV[kk][rr] = (c < m && k < n1) ? V[(int64_t)c * ldv + k] : T(0);
+      sV[kk][rr] = (c < m && k < kend) ? V[(int64_t)c * ldv + k] : T(0);
     }
     __syncthreads();
 #pragma unroll 8
@@ -1222,8 +1226,23 @@ __global__ void __launch_bounds__(128) k_singles_gemm(int n1, const T* __restric
 #pragma unroll
     for (int i = 0; i < 4; ++i) {
       const int r = r0 + 4 * ty + i;
-      if (r < n1) W[(int64_t)c * ldw + r] = diag[r] * V[(int64_t)c * ldv + r] + acc[i][j];
+      if (r >= n1) continue;
+      if (part) part[((int64_t)blockIdx.z * m + c) * n1 + r] = acc[i][j];
+      else W[(int64_t)c * ldw + r] = diag[r] * V[(int64_t)c * ldv + r] + acc[i][j];
     }
+  }
+}
+
+// W1 = diag V1 + the split-K partials, summed in a fixed order
+template <typename T>
+__global__ void k_singles_reduce(int n1, int m, int ks, const T* __restrict__ part, const T* __restrict__ diag,
+                                 const T* __restrict__ V, int64_t ldv, T* __restrict__ W, int64_t ldw) {
+  for (int64_t i = blockIdx.x * (int64_t)blockDim.x + threadIdx.x; i < (int64_t)n1 * m;
+       i += (int64_t)gridDim.x * blockDim.x) {
+    const int c = (int)(i / n1), r = (int)(i - (int64_t)c * n1);
+    T acc = diag[r] * V[(int64_t)c * ldv + r];
+    for (int z = 0; z < ks; ++z) acc += part[((int64_t)z * m + c) * n1 + r];
+    W[(int64_t)c * ldw + r] = acc;
   }
 }
 
@@ -1232,6 +1251,41 @@ void launch_singles(Ctx* c, int m, const T* A, const T* diag, const T* V, int64_
   const int n1 = (int)c->geom.n1;
   dim3 grid((n1 + 31) / 32, (m + 31) / 32);
   k_singles_gemm<T><<<grid, 128, 0, c->stream>>>(n1, A, diag, V, ldv, W, ldw, m); ADC_COUNT_LAUNCH();
+}
+
+// FP32 singles block with K split over about four blocks per SM: the
+// unsplit grid has only (n1/32) x (m/32) blocks, each walking all n1 values
+// of k, which leaves the product latency-bound.  The partials go to the
+// plan's scratch and are summed in a fixed order.
+int launch_singles_split(Ctx* c, int m, const float* A, const float* diag, const float* V, int64_t ldv, float* W,
+                         int64_t ldw) {
+  const int n1 = (int)c->geom.n1;
+  const int base = ((n1 + 31) / 32) * ((m + 31) / 32);
+  const int ks = std::max(1, std::min(16, (4 * c->nsm + base - 1) / base));
+  SigmaPlan* plan = reinterpret_cast<SigmaPlan*>(c->sigma_plan);
+  if (ks == 1 || !plan) {
+    launch_singles<float>(c, m, A, diag, V, ldv, W, ldw);
+    return ADCGPU_OK;
+  }
+  const int kchunk = ((n1 + ks - 1) / ks + 31) / 32 * 32;
+  const int ksu = (n1 + kchunk - 1) / kchunk;
+  const size_t need = sizeof(float) * (size_t)ksu * m * n1;
+  if (plan->sk_bytes < need) {
+    dfree(c, plan->d_sk);
+    plan->d_sk = nullptr;
+    plan->sk_bytes = 0;
+    ST(dmalloc(c, &plan->d_sk, need));
+    plan->sk_bytes = need;
+  }
+  float* part = reinterpret_cast<float*>(plan->d_sk);
+  dim3 grid((n1 + 31) / 32, (m + 31) / 32, ksu);
+  k_singles_gemm<float><<<grid, 128, 0, c->stream>>>(n1, A, diag, V, ldv, W, ldw, m, part, kchunk);
+  ADC_COUNT_LAUNCH();
+  k_singles_reduce<float><<<std::min((n1 * m + 255) / 256, c->nsm * 8), 256, 0, c->stream>>>(n1, m, ksu, part, diag,
+                                                                                          V, ldv, W, ldw);
+  ADC_COUNT_LAUNCH();
+  ADC_CUDA(c, cudaGetLastError());
+  return ADCGPU_OK;
 }
 
 // Close the statistics window of the previous sigma call (its stop event
@@ -1345,7 +1399,8 @@ int sigma_impl(Ctx* c, int m, const T* dV, int64_t ldv, T* dW, int64_t ldw, cons
   ADC_CUDA(c, cudaEventRecord(c->st_ev0, s));
   GeomDev g = to_dev(G);
   // singles block first (plain stores), then the coupling adds atomically
-  launch_singles<T>(c, m, A, diag, dV, ldv, dW, ldw);
+  if constexpr (sizeof(T) == 4) ST(launch_singles_split(c, m, A, diag, dV, ldv, dW, ldw));
+  else launch_singles<T>(c, m, A, diag, dV, ldv, dW, ldw);
   ADC_CUDA(c, cudaGetLastError());
   SigmaPlan* plan = reinterpret_cast<SigmaPlan*>(c->sigma_plan);
   if (!plan) return set_err(c, ADCGPU_NO_MATRIX, "sigma plan missing");
@@ -1416,6 +1471,25 @@ int sigma_impl(Ctx* c, int m, const T* dV, int64_t ldv, T* dW, int64_t ldw, cons
             ST((launch_p3<TV>(c, g, runs, nruns, mc, BtP, V + (int64_t)b0 * ldv, ldv, W1 + (int64_t)b0 * n1, n1)));
             b0 += mc;
           }
+          c0 += nc;
+        }
+        umma_used = true;
+      }
+    }
+    if constexpr (std::is_same<T, float>::value && std::is_same<TV, float>::value) {
+      // FP32 values on the tensor cores: the values and vectors as three BF16
+      // slices each (sigma_umma.cu), segments A/B in compact form from the
+      // FP32 store, up to 32 columns per matrix pass
+      if (allow_umma && P->tiled == 1 && !P->umma_off && !P->ab_off && !c->direct && umma3_supported(c) &&
+          ab_supported(c)) {
+        ST(umma_prepare(c, plan->umma, plan->umma_item_rows));
+        for (; c0 < m;) {
+          const int nc = std::min(m - c0, 32);
+          const T* V = dV + (int64_t)c0 * ldv;
+          T* W = dW + (int64_t)c0 * ldw;
+          TAcc* W1 = W1base + (int64_t)c0 * n1;
+          ST(umma3_launch(c, plan->umma, V, ldv, nc, W, ldw, W1, n1));
+          ST(ab_launch<TV>(c, plan->ab, BtP, true, V, ldv, nc, W, ldw, W1, n1));
           c0 += nc;
         }
         umma_used = true;
@@ -1548,6 +1622,18 @@ __global__ void k_to_f32(const double* __restrict__ x, float* __restrict__ y, in
   for (int64_t i = blockIdx.x * (int64_t)blockDim.x + threadIdx.x; i < n; i += (int64_t)gridDim.x * blockDim.x)
     y[i] = (float)x[i];
 }
+// mid and lo BF16 slices of the FP32 values: x32 = hi + mid + lo to ~2^-25
+// relative, hi the BF16 store (x32 - hi is exact in FP32)
+__global__ void k_bf16_slices(const float* __restrict__ x32, const __nv_bfloat16* __restrict__ hi,
+                              __nv_bfloat16* __restrict__ mid, __nv_bfloat16* __restrict__ lo, int64_t n) {
+  for (int64_t i = blockIdx.x * (int64_t)blockDim.x + threadIdx.x; i < n; i += (int64_t)gridDim.x * blockDim.x) {
+    const float r = x32[i] - __bfloat162float(hi[i]);
+    const __nv_bfloat16 m = __float2bfloat16(r);
+    mid[i] = m;
+    lo[i] = __float2bfloat16(r - __bfloat162float(m));
+  }
+}
+
 __global__ void k_to_bf16(const double* __restrict__ x, __nv_bfloat16* __restrict__ y, int64_t n) {
   for (int64_t i = blockIdx.x * (int64_t)blockDim.x + threadIdx.x; i < n; i += (int64_t)gridDim.x * blockDim.x)
     y[i] = __double2bfloat16(x[i]);
@@ -1618,6 +1704,7 @@ void free_sigma_plan(Ctx* c) {
   dfree(c, plan->d_items);
   dfree(c, plan->d_titems);
   dfree(c, plan->d_acc);
+  dfree(c, plan->d_sk);
   umma_free(c, plan->umma);
   ab_free(c, plan->ab);
   delete plan;
@@ -1636,6 +1723,17 @@ int prepare_mixed(Ctx* c) {
   k_to_bf16<<<c->nsm * 8, 256, 0, c->stream>>>(c->d_Bt, (__nv_bfloat16*)c->d_Bt16, G.off[5]); ADC_COUNT_LAUNCH();
   k_to_f32<<<c->nsm * 8, 256, 0, c->stream>>>(c->d_Bt, c->d_Bt32, G.off[5]); ADC_COUNT_LAUNCH();
   ADC_CUDA(c, cudaGetLastError());
+  // the FP32 values as three BF16 slices for the tcgen05 FP32-value pass
+  // (shapes the tensor-core pass takes only)
+  if (umma_geometry_ok(G)) {
+    for (int t = 0; t < 2; ++t)
+      if (!c->d_Bt16s[t] && (st = dmalloc(c, (void**)&c->d_Bt16s[t], sizeof(uint16_t) * G.off[5]))) return st;
+    k_bf16_slices<<<c->nsm * 8, 256, 0, c->stream>>>(c->d_Bt32, (const __nv_bfloat16*)c->d_Bt16,
+                                                     (__nv_bfloat16*)c->d_Bt16s[0], (__nv_bfloat16*)c->d_Bt16s[1],
+                                                     G.off[5]);
+    ADC_COUNT_LAUNCH();
+    ADC_CUDA(c, cudaGetLastError());
+  }
   // the value stores were rewritten: the compact segment-A/B tables follow
   if (SigmaPlan* plan = reinterpret_cast<SigmaPlan*>(c->sigma_plan)) ab_invalidate(plan->ab);
   return ADCGPU_OK;
@@ -1756,7 +1854,7 @@ int singles_block_product(Ctx* c, int m, const double* V, int64_t ldv, double* W
 }
 int singles_block_product(Ctx* c, int m, const float* V, int64_t ldv, float* W, int64_t ldw) {
   if (!c->d_A32 || !c->d_diag32) return set_err(c, ADCGPU_NO_MATRIX, "FP32 singles block missing");
-  launch_singles<float>(c, m, c->d_A32, c->d_diag32, V, ldv, W, ldw);
+  ST(launch_singles_split(c, m, c->d_A32, c->d_diag32, V, ldv, W, ldw));
   ADC_CUDA(c, cudaGetLastError());
   return ADCGPU_OK;
 }

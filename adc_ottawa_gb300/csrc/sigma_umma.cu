@@ -65,7 +65,7 @@ constexpr int UMMA_ITEM_ROWS_DEFAULT = 4096;  // rows per work item (a piece of 
 // tensor maps of the five classes' B^T values (rows x L BF16, boxes of 64 x
 // 128, 128-byte swizzle), passed by value to the kernel
 struct UmmaMaps {
-  CUtensorMap m[5];
+  CUtensorMap m[3][5];   // [value slice][class]; slices 1, 2 only for the FP32-value pass
 };
 
 namespace {
@@ -77,21 +77,25 @@ enum Bar {
 
 __device__ __forceinline__ bool failed(const int* err) { return *(const volatile int*)err != 0; }
 
-__host__ __device__ constexpr int umma_box_bytes(int NP) { return 2 * NP * 128; }   // one X / V2 box
+// one X / V2 box: XS vector slices of NP columns, 64 values each
+__host__ __device__ constexpr int umma_box_bytes(int NP, int XS) { return XS * NP * 128; }
 
-template <int NP>
+template <int NP, int XS>
 __host__ __device__ constexpr int umma_nslot(int smax) {
   // X (6 boxes) + V2 (2 boxes) + barriers and bookkeeping + alignment slack
-  return (smax - 1024 - 1024 - 8 * umma_box_bytes(NP)) / UMMA_SLOT_BYTES;
+  return (smax - 1024 - 1024 - 8 * umma_box_bytes(NP, XS)) / UMMA_SLOT_BYTES;
 }
 
-template <int NP>
+template <int NP, int XS>
 __host__ __device__ constexpr int umma_tmem_cols() {
-  // D1 x 2, D2 x 3 groups, 2 NP columns each
-  return 5 * 2 * NP <= 256 ? 256 : 512;
+  // D1 x 2, D2 x 3 groups, XS NP columns each
+  return 5 * XS * NP <= 256 ? 256 : 512;
 }
 
-template <int NP, int NSLOT>
+// VS value slices (1: the BF16 store; 3: BF16 slices of the FP32 values,
+// hi + mid + lo) and XS vector slices (2: hi | lo; 3: hi | mid | lo).  The
+// slices of a product are accumulated by the same MMA chain.
+template <int NP, int NSLOT, int VS, int XS>
 // 320 threads: some SM sub-partitions hold three of the ten warps, so a
 // thread may use at most 16384 / 96 -> 168 registers
 __global__ void __launch_bounds__(UMMA_THREADS, 1)
@@ -99,9 +103,9 @@ __global__ void __launch_bounds__(UMMA_THREADS, 1)
                  const __nv_bfloat16* __restrict__ Bt, const float* __restrict__ diag, const float* __restrict__ V,
                  int64_t ldv, int mcols, float* __restrict__ W, int64_t ldw, double* __restrict__ W1, int64_t ld1,
                  int seg_a, int* __restrict__ err) {
-  constexpr int N2 = 2 * NP;                       // MMA N (hi | lo)
-  constexpr int BOXB = umma_box_bytes(NP);
-  constexpr uint32_t TCOLS = umma_tmem_cols<NP>();
+  constexpr int N2 = XS * NP;                      // MMA N (the vector slices side by side)
+  constexpr int BOXB = umma_box_bytes(NP, XS);
+  constexpr uint32_t TCOLS = umma_tmem_cols<NP, XS>();
   extern __shared__ __align__(1024) unsigned char smem_raw[];
   unsigned char* base = (unsigned char*)(((uintptr_t)smem_raw + 1023) & ~(uintptr_t)1023);
   unsigned char* sX = base;                                   // 6 boxes [N2 rows x 64 k]
@@ -143,10 +147,11 @@ __global__ void __launch_bounds__(UMMA_THREADS, 1)
         const int K = (cls >= 2 ? 2 : 1) * nvP;
         const int nslot = (K + 2 * UMMA_BOX - 1) / (2 * UMMA_BOX);
         const int offC = twoa ? 2 * noP : noP;
-        const CUtensorMap* tm = &maps.m[cls];
         for (int row0 = item.x; ok && row0 < item.y; row0 += UMMA_ROWS) {
           const int y = (int)(row0 - g.start[cls]);
+          for (int vs = 0; vs < VS && ok; ++vs)
           for (int s = 0; s < nslot; ++s, ++use) {
+            const CUtensorMap* tm = &maps.m[vs][cls];
             const int ri = (int)(use % NSLOT);
             const uint32_t ph = (use / NSLOT) & 1u;
             ok = !failed(err) && mbar_wait(&slot_empty[ri], ph ^ 1u, err, 1);
@@ -190,6 +195,7 @@ __global__ void __launch_bounds__(UMMA_THREADS, 1)
           ok = mbar_wait(&bars[B_D1EMPTY0 + db], ((tile >> 1) & 1u) ^ 1u, err, 4);
           ok = ok && mbar_wait(&bars[B_V2FULL], tile & 1u, err, 5);
           fence_after_sync();
+          for (int vs = 0; vs < VS && ok; ++vs)
           for (int s = 0; ok && s < nslot; ++s, ++use) {
             const int ri = (int)(use % NSLOT);
             const uint32_t ph = (use / NSLOT) & 1u;
@@ -204,7 +210,7 @@ __global__ void __launch_bounds__(UMMA_THREADS, 1)
               for (int ks = 0; ks < 4; ++ks) {
                 const uint64_t ad = sdesc(slot + b * (UMMA_SLOT_BYTES / 2) + ks * 32, 16, 1024, LAYOUT_SW128);
                 const uint64_t bd = sdesc(sXa + box * BOXB + ks * 32, 16, 1024, LAYOUT_SW128);
-                mma_bf16(tD1[db], ad, bd, idK, (box | ks) ? 1u : 0u);
+                mma_bf16(tD1[db], ad, bd, idK, (vs | box | ks) ? 1u : 0u);
               }
             }
             // W1 part: the slot's 128 values of a as MN-major A (two 64-wide
@@ -212,7 +218,7 @@ __global__ void __launch_bounds__(UMMA_THREADS, 1)
             for (int ks = 0; ks < 8; ++ks) {
               const uint64_t ad = sdesc(slot + ks * 2048, UMMA_SLOT_BYTES / 2, 1024, LAYOUT_SW128);
               const uint64_t bd = sdesc(sVa + (ks >> 2) * BOXB + (ks & 3) * 32, 16, 1024, LAYOUT_SW128);
-              mma_bf16(tD2 + (uint32_t)s * N2, ad, bd, idM, (first_tile && ks == 0) ? 0u : 1u);
+              mma_bf16(tD2 + (uint32_t)s * N2, ad, bd, idM, (first_tile && vs == 0 && ks == 0) ? 0u : 1u);
             }
             mma_commit(&slot_empty[ri]);
           }
@@ -259,11 +265,14 @@ __global__ void __launch_bounds__(UMMA_THREADS, 1)
 #pragma unroll
       for (int j = 0; j < NP / 2; ++j) {
         const int c = cbeg + j;
-        const __nv_bfloat16 h = __float2bfloat16(v2[j]);
-        const __nv_bfloat16 l = __float2bfloat16(v2[j] - __bfloat162float(h));
         unsigned char* bx = sV2 + (r >> 6) * BOXB;
-        *reinterpret_cast<__nv_bfloat16*>(bx + sw128_off(c, r & 63)) = h;
-        *reinterpret_cast<__nv_bfloat16*>(bx + sw128_off(NP + c, r & 63)) = l;
+        float rem = v2[j];
+#pragma unroll
+        for (int t = 0; t < XS; ++t) {
+          const __nv_bfloat16 h = __float2bfloat16(rem);
+          *reinterpret_cast<__nv_bfloat16*>(bx + sw128_off(t * NP + c, r & 63)) = h;
+          rem -= __bfloat162float(h);
+        }
       }
       fence_proxy_async();
       mbar_arrive(&bars[B_V2FULL]);
@@ -276,7 +285,7 @@ __global__ void __launch_bounds__(UMMA_THREADS, 1)
       const int nslot = (K + 2 * UMMA_BOX - 1) / (2 * UMMA_BOX);
       const int64_t L = g.len[cls];
       const int kp = r0.kp, lp = r0.lp;
-      // X of this item: hi at rows c, lo at rows NP + c of each box
+      // X of this item: slice t of column c at row t NP + c of each box
       ok = mbar_wait(&bars[B_XEMPTY], (nitem & 1u) ^ 1u, err, 7);
       if (!ok) break;
       // eight independent loads in flight per thread, then the stores
@@ -296,11 +305,14 @@ __global__ void __launch_bounds__(UMMA_THREADS, 1)
           const int o = o0 + 256 * u;
           if (o >= XTOT) break;
           const int c = o / (UMMA_MAX_BOXES * UMMA_BOX), k = o - c * (UMMA_MAX_BOXES * UMMA_BOX);
-          const __nv_bfloat16 h = __float2bfloat16(xv[u]);
-          const __nv_bfloat16 l = __float2bfloat16(xv[u] - __bfloat162float(h));
           unsigned char* bx = sX + (k >> 6) * BOXB;
-          *reinterpret_cast<__nv_bfloat16*>(bx + sw128_off(c, k & 63)) = h;
-          *reinterpret_cast<__nv_bfloat16*>(bx + sw128_off(NP + c, k & 63)) = l;
+          float rem = xv[u];
+#pragma unroll
+          for (int t = 0; t < XS; ++t) {
+            const __nv_bfloat16 h = __float2bfloat16(rem);
+            *reinterpret_cast<__nv_bfloat16*>(bx + sw128_off(t * NP + c, k & 63)) = h;
+            rem -= __bfloat162float(h);
+          }
         }
       }
       fence_proxy_async();
@@ -394,6 +406,12 @@ __global__ void __launch_bounds__(UMMA_THREADS, 1)
           float hi[8], lo[8];
           tmem_ld8(tD1[db] + lane_off + (uint32_t)(cbeg + j0), hi);
           tmem_ld8(tD1[db] + lane_off + (uint32_t)(NP + cbeg + j0), lo);
+          if (XS == 3) {
+            float lo2[8];
+            tmem_ld8(tD1[db] + lane_off + (uint32_t)(2 * NP + cbeg + j0), lo2);
+#pragma unroll
+            for (int j = 0; j < 8; ++j) lo[j] += lo2[j];
+          }
 #pragma unroll
           for (int j = 0; j < 8; ++j) {
             const int c = cbeg + j0 + j;
@@ -423,6 +441,12 @@ __global__ void __launch_bounds__(UMMA_THREADS, 1)
           float hi[8], lo[8];
           tmem_ld8(tD2 + (uint32_t)s * N2 + lane_off + (uint32_t)(cbeg + j0), hi);
           tmem_ld8(tD2 + (uint32_t)s * N2 + lane_off + (uint32_t)(NP + cbeg + j0), lo);
+          if (XS == 3) {
+            float lo2[8];
+            tmem_ld8(tD2 + (uint32_t)s * N2 + lane_off + (uint32_t)(2 * NP + cbeg + j0), lo2);
+#pragma unroll
+            for (int j = 0; j < 8; ++j) lo[j] += lo2[j];
+          }
 #pragma unroll
           for (int j = 0; j < 8; ++j) {
             const int c = cbeg + j0 + j;
@@ -453,6 +477,7 @@ __global__ void __launch_bounds__(UMMA_THREADS, 1)
 struct UmmaPlan {
   UmmaMaps maps;
   const void* maps_for = nullptr;   // the B^T array the maps describe
+  const void* slices_for = nullptr; // the mid slice array the slice maps describe (FP32-value pass)
   int2* d_items = nullptr;          // tensor-core work items (row ranges inside one slab)
   int nitems = 0;
   int2* d_runs = nullptr;           // pass-3 runs: (first row, rows) of equal a' in one slab
@@ -480,20 +505,20 @@ PFN_cuTensorMapEncodeTiled_v12000 encode_fn() {
   return fn;
 }
 
-template <int NP>
+template <int NP, int XS>
 size_t umma_smem_bytes(int nslot) {
-  return 1024 + (size_t)(UMMA_MAX_BOXES + 2) * umma_box_bytes(NP) + (size_t)nslot * UMMA_SLOT_BYTES +
+  return 1024 + (size_t)(UMMA_MAX_BOXES + 2) * umma_box_bytes(NP, XS) + (size_t)nslot * UMMA_SLOT_BYTES +
          (size_t)(B_SLOT0 + 2 * nslot) * 8 + 16;
 }
 
-template <int NP>
+template <int NP, int VS, int XS>
 int launch_umma_np(Ctx* c, UmmaPlan* u, const float* V, int64_t ldv, int m, float* W, int64_t ldw, double* W1,
                    int64_t ld1, int seg_a) {
   const int smax = smem_optin_max(c);
-  int nslot = umma_nslot<NP>(smax);
-  nslot = std::min(nslot, 6);
+  int nslot = umma_nslot<NP, XS>(smax);
+  nslot = std::min(nslot, VS == 1 ? 6 : 4);
   if (nslot < 2) return set_err(c, ADCGPU_UNSUPPORTED, "tensor-core sigma pass: shared memory too small");
-  const size_t smem = umma_smem_bytes<NP>(nslot);
+  const size_t smem = umma_smem_bytes<NP, XS>(nslot);
   if (smem > (size_t)smax) return set_err(c, ADCGPU_UNSUPPORTED, "tensor-core sigma pass: shared memory too small");
   const GeomDev g = to_dev(c->geom);
   const int grid = std::max(1, std::min(u->nitems, c->nsm));
@@ -506,12 +531,20 @@ int launch_umma_np(Ctx* c, UmmaPlan* u, const float* V, int64_t ldv, int m, floa
     ADC_CUDA(c, cudaGetLastError());
     return ADCGPU_OK;
   };
-  switch (nslot) {
-    case 2: return go(k_sigma_umma<NP, 2>);
-    case 3: return go(k_sigma_umma<NP, 3>);
-    case 4: return go(k_sigma_umma<NP, 4>);
-    case 5: return go(k_sigma_umma<NP, 5>);
-    default: return go(k_sigma_umma<NP, 6>);
+  if constexpr (VS == 1) {
+    switch (nslot) {
+      case 2: return go(k_sigma_umma<NP, 2, VS, XS>);
+      case 3: return go(k_sigma_umma<NP, 3, VS, XS>);
+      case 4: return go(k_sigma_umma<NP, 4, VS, XS>);
+      case 5: return go(k_sigma_umma<NP, 5, VS, XS>);
+      default: return go(k_sigma_umma<NP, 6, VS, XS>);
+    }
+  } else {
+    switch (nslot) {
+      case 2: return go(k_sigma_umma<NP, 2, VS, XS>);
+      case 3: return go(k_sigma_umma<NP, 3, VS, XS>);
+      default: return go(k_sigma_umma<NP, 4, VS, XS>);
+    }
   }
 }
 
@@ -525,8 +558,15 @@ bool umma_supported(const Ctx* c) {
     return false;
   }
   // segment A in registers (noP <= 24), C|D of at most six 64-value boxes
-  return major >= 10 && G.noP <= UMMA_NOP && 2 * G.nvP <= UMMA_MAX_BOXES * UMMA_BOX && G.no >= 2 && G.nv >= 2 &&
-         c->d_Bt16 != nullptr && encode_fn() != nullptr;
+  return major >= 10 && umma_geometry_ok(G) && c->d_Bt16 != nullptr && encode_fn() != nullptr;
+}
+
+bool umma_geometry_ok(const Geometry& G) {
+  return G.noP <= UMMA_NOP && 2 * G.nvP <= UMMA_MAX_BOXES * UMMA_BOX && G.no >= 2 && G.nv >= 2;
+}
+
+bool umma3_supported(const Ctx* c) {
+  return umma_supported(c) && c->d_Bt16s[0] != nullptr && c->d_Bt16s[1] != nullptr;
 }
 
 void umma_free(Ctx* c, void*& handle) {
@@ -543,6 +583,7 @@ void umma_free(Ctx* c, void*& handle) {
 // Work items, pass-3 runs and the tensor maps of the BF16 B^T values.
 int umma_prepare(Ctx* c, void*& handle, int item_rows) {
   if (handle && reinterpret_cast<UmmaPlan*>(handle)->maps_for == c->d_Bt16 &&
+      reinterpret_cast<UmmaPlan*>(handle)->slices_for == c->d_Bt16s[0] &&
       reinterpret_cast<UmmaPlan*>(handle)->item_rows == item_rows)
     return ADCGPU_OK;
   umma_free(c, handle);
@@ -578,22 +619,29 @@ int umma_prepare(Ctx* c, void*& handle, int item_rows) {
   u->nruns = (int)runs.size();
   PFN_cuTensorMapEncodeTiled_v12000 enc = encode_fn();
   if (!enc) return set_err(c, ADCGPU_UNSUPPORTED, "cuTensorMapEncodeTiled unavailable");
-  for (int cls = 0; cls < 5; ++cls) {
-    const int64_t rows = G.start[cls + 1] - G.start[cls];
-    std::memset(&u->maps.m[cls], 0, sizeof(CUtensorMap));
-    if (rows <= 0) continue;
-    void* basep = (void*)((const __nv_bfloat16*)c->d_Bt16 + G.off[cls]);
-    cuuint64_t gdim[2] = {(cuuint64_t)G.len[cls], (cuuint64_t)rows};
-    cuuint64_t gstr[1] = {(cuuint64_t)G.len[cls] * 2};
-    cuuint32_t box[2] = {UMMA_BOX, UMMA_ROWS};
-    cuuint32_t es[2] = {1, 1};
-    CUresult r = enc(&u->maps.m[cls], CU_TENSOR_MAP_DATA_TYPE_BFLOAT16, 2, basep, gdim, gstr, box, es,
-                     CU_TENSOR_MAP_INTERLEAVE_NONE, CU_TENSOR_MAP_SWIZZLE_128B, CU_TENSOR_MAP_L2_PROMOTION_L2_256B,
-                     CU_TENSOR_MAP_FLOAT_OOB_FILL_NONE);
-    if (r != CUDA_SUCCESS)
-      return set_err(c, ADCGPU_CUDA_ERROR, "cuTensorMapEncodeTiled failed for class " + std::to_string(cls));
+  // slice 0: the BF16 store; slices 1, 2: the mid and lo BF16 slices of the
+  // FP32 values (when the matrix has them)
+  const uint16_t* arrays[3] = {c->d_Bt16, c->d_Bt16s[0], c->d_Bt16s[1]};
+  std::memset(&u->maps, 0, sizeof(UmmaMaps));
+  for (int v = 0; v < 3; ++v) {
+    if (!arrays[v]) continue;
+    for (int cls = 0; cls < 5; ++cls) {
+      const int64_t rows = G.start[cls + 1] - G.start[cls];
+      if (rows <= 0) continue;
+      void* basep = (void*)((const __nv_bfloat16*)arrays[v] + G.off[cls]);
+      cuuint64_t gdim[2] = {(cuuint64_t)G.len[cls], (cuuint64_t)rows};
+      cuuint64_t gstr[1] = {(cuuint64_t)G.len[cls] * 2};
+      cuuint32_t box[2] = {UMMA_BOX, UMMA_ROWS};
+      cuuint32_t es[2] = {1, 1};
+      CUresult r = enc(&u->maps.m[v][cls], CU_TENSOR_MAP_DATA_TYPE_BFLOAT16, 2, basep, gdim, gstr, box, es,
+                       CU_TENSOR_MAP_INTERLEAVE_NONE, CU_TENSOR_MAP_SWIZZLE_128B, CU_TENSOR_MAP_L2_PROMOTION_L2_256B,
+                       CU_TENSOR_MAP_FLOAT_OOB_FILL_NONE);
+      if (r != CUDA_SUCCESS)
+        return set_err(c, ADCGPU_CUDA_ERROR, "cuTensorMapEncodeTiled failed for class " + std::to_string(cls));
+    }
   }
   u->maps_for = c->d_Bt16;
+  u->slices_for = c->d_Bt16s[0];
   return ADCGPU_OK;
 }
 
@@ -612,9 +660,22 @@ int umma_launch(Ctx* c, void* handle, const float* V, int64_t ldv, int m, float*
                 int64_t ld1, int seg_a) {
   UmmaPlan* u = reinterpret_cast<UmmaPlan*>(handle);
   if (!u || m <= 0 || m > 48) return set_err(c, ADCGPU_BAD_INPUT, "tensor-core sigma pass: columns");
-  if (m <= 16) return launch_umma_np<16>(c, u, V, ldv, m, W, ldw, W1, ld1, seg_a);
-  if (m <= 32) return launch_umma_np<32>(c, u, V, ldv, m, W, ldw, W1, ld1, seg_a);
-  return launch_umma_np<48>(c, u, V, ldv, m, W, ldw, W1, ld1, seg_a);
+  if (m <= 16) return launch_umma_np<16, 1, 2>(c, u, V, ldv, m, W, ldw, W1, ld1, seg_a);
+  if (m <= 32) return launch_umma_np<32, 1, 2>(c, u, V, ldv, m, W, ldw, W1, ld1, seg_a);
+  return launch_umma_np<48, 1, 2>(c, u, V, ldv, m, W, ldw, W1, ld1, seg_a);
+}
+
+// The C|D products of the FP32-value matrix for m <= 32 columns: the values
+// as three BF16 slices (the BF16 store, then the mid and lo slices), the
+// vectors as three BF16 slices; segments A and B are left to the compact
+// kernels.
+int umma3_launch(Ctx* c, void* handle, const float* V, int64_t ldv, int m, float* W, int64_t ldw, double* W1,
+                 int64_t ld1) {
+  UmmaPlan* u = reinterpret_cast<UmmaPlan*>(handle);
+  if (!u || m <= 0 || m > 32) return set_err(c, ADCGPU_BAD_INPUT, "tensor-core FP32-value sigma pass: columns");
+  if (!u->slices_for) return set_err(c, ADCGPU_UNSUPPORTED, "tensor-core FP32-value sigma pass: no value slices");
+  if (m <= 16) return launch_umma_np<16, 3, 3>(c, u, V, ldv, m, W, ldw, W1, ld1, 0);
+  return launch_umma_np<32, 3, 3>(c, u, V, ldv, m, W, ldw, W1, ld1, 0);
 }
 
 // Reads the kernel's error word (waits for the stream) and clears it.
