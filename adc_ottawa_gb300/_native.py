@@ -98,6 +98,7 @@ SIGNATURES = {
     "adcgpu_device_bytes": (C.c_int64, [_vp]),
     "adcgpu_set_fp64_arith": (C.c_int, [_vp, C.c_int]),
     "adcgpu_sigma_stats": (C.c_int, [_vp, _dp, C.c_int]),
+    "adcgpu_sigma_stats_by_store": (C.c_int, [_vp, _dp, C.c_int]),
     "adcgpu_mlp_num_params": (C.c_int64, []),
     "adcgpu_mlp_set_params": (C.c_int, [_vp, C.POINTER(C.c_float), C.c_int64]),
     "adcgpu_mlp_get_params": (C.c_int, [_vp, C.POINTER(C.c_float), C.c_int64]),

@@ -304,6 +304,15 @@ class AdcGpu:
         self._check(lib().adcgpu_sigma_stats(self._h, ptr(out), int(reset)), "sigma_stats")
         return {"calls": int(out[0]), "ms": float(out[1]), "alg_bytes": float(out[2]), "columns": int(out[3])}
 
+    def sigma_stats_by_store(self, reset: bool = False) -> dict:
+        """sigma_stats split by the value store the calls read (the mixed
+        ladder's BF16, FP32 and FP64 phases)."""
+        out = np.zeros(12)
+        self._check(lib().adcgpu_sigma_stats_by_store(self._h, ptr(out), int(reset)), "sigma_stats_by_store")
+        return {name: {"calls": int(out[4 * k]), "ms": float(out[4 * k + 1]), "alg_bytes": float(out[4 * k + 2]),
+                       "columns": int(out[4 * k + 3])}
+                for k, name in enumerate(("bf16", "fp32", "fp64"))}
+
     def device_bytes(self) -> int:
         return int(lib().adcgpu_device_bytes(self._h))
 

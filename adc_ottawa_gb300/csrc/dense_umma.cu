@@ -103,9 +103,6 @@ __global__ void __launch_bounds__(GU_THREADS, 1)
   // this thread's columns: A columns m0 + warp + 8u (u < 16), B columns
   // warp + 8u (u < NB); rows r0 + 2 lane, r0 + 2 lane + 1 of each stage
   float2 pa[GU_M / 8], pb[NB];
-  // even leading dimensions and 8-byte aligned bases: one 8-byte load per
-  // pair of rows (r is even: r_begin is a multiple of the stage height)
-  const bool vec2 = ((lda | ldb) & 1) == 0 && (((uintptr_t)A | (uintptr_t)B) & 7) == 0;
   auto fetch = [&](int i) {
     const int64_t r = r_begin + (int64_t)i * GU_K + 2 * lane;
     const bool ok0 = r < r_end, ok1 = r + 1 < r_end;
@@ -113,23 +110,15 @@ __global__ void __launch_bounds__(GU_THREADS, 1)
     for (int u = 0; u < GU_M / 8; ++u) {
       const int m = m0 + warp + 8 * u;
       const float* col = A + (int64_t)m * lda;
-      if (vec2 && ok1) {
-        pa[u] = m < p ? __ldg(reinterpret_cast<const float2*>(col + r)) : make_float2(0.f, 0.f);
-      } else {
-        pa[u].x = (m < p && ok0) ? __ldg(col + r) : 0.f;
-        pa[u].y = (m < p && ok1) ? __ldg(col + r + 1) : 0.f;
-      }
+      pa[u].x = (m < p && ok0) ? __ldg(col + r) : 0.f;
+      pa[u].y = (m < p && ok1) ? __ldg(col + r + 1) : 0.f;
     }
 #pragma unroll
     for (int u = 0; u < NB; ++u) {
       const int n = warp + 8 * u;
       const float* col = B + (int64_t)n * ldb;
-      if (vec2 && ok1) {
-        pb[u] = n < q ? __ldg(reinterpret_cast<const float2*>(col + r)) : make_float2(0.f, 0.f);
-      } else {
-        pb[u].x = (n < q && ok0) ? __ldg(col + r) : 0.f;
-        pb[u].y = (n < q && ok1) ? __ldg(col + r + 1) : 0.f;
-      }
+      pb[u].x = (n < q && ok0) ? __ldg(col + r) : 0.f;
+      pb[u].y = (n < q && ok1) ? __ldg(col + r + 1) : 0.f;
     }
   };
   auto store = [&](int s) {

@@ -296,6 +296,8 @@ struct Ctx {
   bool st_pending = false;
   double st_pending_bytes = 0.0;
   int st_pending_cols = 0;
+  int st_pending_kind = 0;        // value store of the pending call: 0 BF16, 1 FP32, 2 FP64
+  double st_by[3][4] = {};        // per value store: calls, ms, algorithmic bytes, columns
   int64_t dev_bytes = 0;          // sum of the live dmalloc sizes
   std::unordered_map<void*, size_t> dev_allocs;   // dmalloc pointer -> size
   // learned preconditioner (MlpState, mlp.cu); DPR is used when absent
@@ -417,6 +419,7 @@ struct SigmaPlan {
   int umma_off = 0;           // 1: the tensor-core pass is not used
   void* ab = nullptr;         // compact segment-A/B tables (sigma_ab.cu), built on first use
   int ab_off = 0;             // 1: segments A/B through pass 2 / pass 3 instead
+  int umma3_on = 0;           // 1: FP32 values on the tcgen05 pass (three BF16 slices)
   std::vector<DirectChunk> dchunks;   // direct path: chunks with their work-list ranges
 };
 int prepare_desc(Ctx* c);

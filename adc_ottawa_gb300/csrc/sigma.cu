@@ -1299,6 +1299,8 @@ void sigma_stats_flush(Ctx* c) {
   c->st_bytes += c->st_pending_bytes;
   c->st_cols += c->st_pending_cols;
   c->st_calls += 1;
+  double* by = c->st_by[c->st_pending_kind];
+  by[0] += 1.0; by[1] += ms; by[2] += c->st_pending_bytes; by[3] += c->st_pending_cols;
   c->st_pending = false;
 }
 
@@ -1480,8 +1482,8 @@ int sigma_impl(Ctx* c, int m, const T* dV, int64_t ldv, T* dW, int64_t ldw, cons
       // FP32 values on the tensor cores: the values and vectors as three BF16
       // slices each (sigma_umma.cu), segments A/B in compact form from the
       // FP32 store, up to 32 columns per matrix pass
-      if (allow_umma && P->tiled == 1 && !P->umma_off && !P->ab_off && !c->direct && umma3_supported(c) &&
-          ab_supported(c)) {
+      if (allow_umma && P->umma3_on && P->tiled == 1 && !P->umma_off && !P->ab_off && !c->direct &&
+          umma3_supported(c) && ab_supported(c)) {
         ST(umma_prepare(c, plan->umma, plan->umma_item_rows));
         for (; c0 < m;) {
           const int nc = std::min(m - c0, 32);
@@ -1608,6 +1610,7 @@ int sigma_impl(Ctx* c, int m, const T* dV, int64_t ldv, T* dW, int64_t ldw, cons
   if (umma_used) ST(umma_check(c, plan->umma));
   c->st_pending = true;
   c->st_pending_cols = m;
+  c->st_pending_kind = std::is_same<TV, __nv_bfloat16>::value ? 0 : (std::is_same<TV, float>::value ? 1 : 2);
   // algorithmic bytes of one sparse product of m columns, counted as for a
   // CSR matrix: every kept coupling value once with a 4-byte column index,
   // the dense singles block as n1^2 values, n1+1 row pointers, the FP64
@@ -1739,13 +1742,28 @@ int prepare_mixed(Ctx* c) {
   return ADCGPU_OK;
 }
 
+extern "C" int adcgpu_sigma_stats_by_store(adcgpu_ctx* h, double* out, int reset) {
+  Ctx* c = reinterpret_cast<Ctx*>(h);
+  if (!c || !out) return ADCGPU_BAD_INPUT;
+  cudaSetDevice(c->device);
+  sigma_stats_flush(c);
+  for (int k = 0; k < 3; ++k)
+    for (int j = 0; j < 4; ++j) out[4 * k + j] = c->st_by[k][j];
+  if (reset)
+    for (auto& b : c->st_by) for (double& x : b) x = 0.0;
+  return ADCGPU_OK;
+}
+
 extern "C" int adcgpu_sigma_stats(adcgpu_ctx* h, double* out, int reset) {
   Ctx* c = reinterpret_cast<Ctx*>(h);
   if (!c || !out) return ADCGPU_BAD_INPUT;
   cudaSetDevice(c->device);
   sigma_stats_flush(c);
   out[0] = (double)c->st_calls; out[1] = c->st_ms; out[2] = c->st_bytes; out[3] = (double)c->st_cols;
-  if (reset) { c->st_calls = 0; c->st_cols = 0; c->st_ms = 0.0; c->st_bytes = 0.0; }
+  if (reset) {
+    c->st_calls = 0; c->st_cols = 0; c->st_ms = 0.0; c->st_bytes = 0.0;
+    for (auto& b : c->st_by) for (double& x : b) x = 0.0;
+  }
   return ADCGPU_OK;
 }
 
@@ -1804,6 +1822,7 @@ extern "C" int adcgpu_sigma_autotune(adcgpu_ctx* h, int m, int* best_chunk, int*
   }
   sigma_stats_flush(c);
   c->st_calls = 0; c->st_cols = 0; c->st_ms = 0.0; c->st_bytes = 0.0;
+  for (auto& b : c->st_by) for (double& x : b) x = 0.0;
   plan->mc_cap[mixed ? 1 : 0] = bm;
   plan->staged = bs;
   plan->tiled = bt;
@@ -1835,6 +1854,10 @@ extern "C" int adcgpu_sigma_set_shape(adcgpu_ctx* h, int chunk, int mc_fp64, int
   // 512: the FP32 Gram products (V^T W) on the CUDA cores instead of the
   // tensor cores
   gram_set_off(c, ((mc_fp64 | mc_fp32) & 512) ? 1 : 0);
+  // 1024: FP32 values on the tcgen05 pass as three BF16 slices (off by
+  // default: its TMEM sums of ~1,100 slice products per element carry about
+  // 1e-5 relative error, above the FP32 phase's target)
+  plan->umma3_on = ((mc_fp64 | mc_fp32) & 1024) ? 1 : 0;
   plan->mc_cap[0] = std::min(mc_fp64 & 7, 2);
   plan->mc_cap[1] = std::min(mc_fp32 & 7, 4);
   return build_chunks(c, chunk);

@@ -251,6 +251,7 @@ def run_gb300(args):
     barrier(world)
     clocks = clk.stop()
     launches = int(lib().adcgpu_kernel_launches()) - launches0
+    by_store = g.sigma_stats_by_store()
     stats = g.sigma_stats(reset=True)
     t_step = allmax(statistics.mean(times), world)
     r = results[-1]
@@ -348,7 +349,8 @@ def run_gb300(args):
                      "traffic": per_launch_bytes * TRAFFIC_PER_ALG_BYTE,
                      "traffic_source": TRAFFIC_SOURCE,
                      "alg_bytes_per_launch": per_launch_bytes, "launches": stats["calls"],
-                     "avg_launch_ms": stats["ms"] / max(stats["calls"], 1), "peak_source": src},
+                     "avg_launch_ms": stats["ms"] / max(stats["calls"], 1), "peak_source": src,
+                     "by_value_store": by_store_roofline(by_store, hbm)},
         "clocks": clocks,
         "e2e": e2e,
         "cpu_baseline": cpu,
@@ -357,6 +359,24 @@ def run_gb300(args):
     if rank == 0:
         print(json.dumps(line), flush=True)
     g.close()
+
+
+def by_store_roofline(by_store, hbm):
+    """The sigma calls of the timed solves split by the value store they read
+    (the mixed ladder's phases: BF16 values on the tcgen05 pass, FP32 values
+    as three BF16 slices on the tcgen05 pass, FP64 values in double-float on
+    the FP32 pipe), each as algorithmic GB/s against the HBM peak."""
+    out = {}
+    for k, v in by_store.items():
+        if v["calls"] == 0:
+            continue
+        gbs = v["alg_bytes"] / (v["ms"] * 1e-3) / 1e9 if v["ms"] > 0 else 0.0
+        out[k] = {"calls": v["calls"], "avg_ms": v["ms"] / v["calls"], "avg_columns": v["columns"] / v["calls"],
+                  "achieved_gbs": gbs, "frac": gbs / hbm, "share_of_sigma_ms": None}
+    tot = sum(v["ms"] for v in by_store.values())
+    for k in out:
+        out[k]["share_of_sigma_ms"] = by_store[k]["ms"] / tot if tot > 0 else None
+    return out
 
 
 def workload_config(no, nv, ndim):

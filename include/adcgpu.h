@@ -440,6 +440,12 @@ uint64_t adcgpu_kernel_launches(void);
    reset != 0 clears the counters after reading. */
 int adcgpu_sigma_stats(adcgpu_ctx* ctx, double* out4, int reset);
 
+/* The same four figures for each value store the calls read: out[0..3]
+   BF16 values, out[4..7] FP32 values, out[8..11] FP64 values (the mixed
+   ladder's three phases).  reset != 0 clears them (adcgpu_sigma_stats with
+   reset clears them too). */
+int adcgpu_sigma_stats_by_store(adcgpu_ctx* ctx, double* out12, int reset);
+
 /* Allocation-free sigma product on device buffers, for callers that must
    not allocate device memory while they run: a host application whose
    device-memory budget is fixed in advance (the rest of the device belongs
@@ -470,7 +476,9 @@ int adcgpu_sigma_autotune(adcgpu_ctx* ctx, int m, int* best_chunk, int* best_mc,
    the per-(slab, b') pass 2 and per-run pass 3 instead of the compact
    kernels, bit 8 makes a mixed-precision matrix's sigma product read the
    FP32 value store instead of the BF16 one, bit 9 keeps the FP32 Gram
-   products (adcgpu_gram_f32 and the solvers' V^T W) on the CUDA cores. */
+   products (adcgpu_gram_f32 and the solvers' V^T W) on the CUDA cores, bit
+   10 runs the FP32 values on the tcgen05 pass as three BF16 slices instead
+   of the CUDA-core tile (off by default: about 1e-5 relative error). */
 int adcgpu_sigma_set_shape(adcgpu_ctx* ctx, int chunk, int mc_fp64, int mc_fp32);
 
 /* The solvers' tall-skinny Gram product on device FP32 arrays: C(p x q,

@@ -111,7 +111,9 @@ def test_compact_segments_match_pass2_and_oracle(gpu, no, nv, seed):
     per-run pass 3 over the same values: BF16 values on the tensor-core pass
     (flag 128 switches the compact kernels off) and FP32 values on the tiled
     pass (flag 256), at 1e-5 relative; both against the oracle's FP64
-    product at the value precision.  Column counts cover partial 4-column
+    product at the value precision.  FP32 values on the tcgen05 pass as
+    three BF16 slices (flag 1024, off by default) are held to the same
+    bounds.  Column counts cover partial 4-column
     groups, more than one 48-column pass and a padded leading dimension;
     (3, 37) gives noP = 8 and an odd number of virtuals."""
     import torch
@@ -120,8 +122,7 @@ def test_compact_segments_match_pass2_and_oracle(gpu, no, nv, seed):
     N = g.ndim
     ref = oracle.Matrix.build(no, nv, e, eri)
     gen = torch.Generator(device="cuda").manual_seed(7 * no + nv)
-    for fp32_values in (False, True):
-        base = 256 if fp32_values else 0
+    for fp32_values, base in ((False, 0), (True, 256), (True, 256 | 1024)):
         for m, pad in ((1, 0), (6, 2), (16, 0), (21, 3), (40, 0), (53, 1)):
             ld = N + pad
             x = torch.randn(m, ld, device="cuda", dtype=torch.float32, generator=gen)
