@@ -61,6 +61,10 @@ constexpr int UMMA_MAX_BOXES = 6;           // K <= 384
 constexpr int UMMA_THREADS = 320;             // producer, MMA issuer, 8 epilogue warps
 constexpr int UMMA_NOP = 16;                  // segment A lengths (noP) up to 16 (nocc <= 16)
 constexpr int UMMA_ITEM_ROWS_DEFAULT = 4096;  // rows per work item (a piece of one slab)
+// rows per work item of the FP32-value main pass: the W1 sums of an item run
+// in one TMEM chain (8 MMA steps per 128-row tile), and shorter chains keep
+// the tensor cores' truncating FP32 accumulation near FP32 rounding
+constexpr int UMMA_ITEM_ROWS_SHORT = 512;
 
 // tensor maps of the five classes' B^T values (rows x L BF16, boxes of 64 x
 // 128, 128-byte swizzle), passed by value to the kernel
@@ -102,7 +106,7 @@ __global__ void __launch_bounds__(UMMA_THREADS, 1)
     k_sigma_umma(GeomDev g, const int2* __restrict__ items, int nitems, const __grid_constant__ UmmaMaps maps,
                  const __nv_bfloat16* __restrict__ Bt, const float* __restrict__ diag, const float* __restrict__ V,
                  int64_t ldv, int mcols, float* __restrict__ W, int64_t ldw, double* __restrict__ W1, int64_t ld1,
-                 int seg_a, int* __restrict__ err) {
+                 int seg_a, int vbase, int w2_add, int* __restrict__ err) {
   constexpr int N2 = XS * NP;                      // MMA N (the vector slices side by side)
   constexpr int BOXB = umma_box_bytes(NP, XS);
   constexpr uint32_t TCOLS = umma_tmem_cols<NP, XS>();
@@ -151,7 +155,7 @@ __global__ void __launch_bounds__(UMMA_THREADS, 1)
           const int y = (int)(row0 - g.start[cls]);
           for (int vs = 0; vs < VS && ok; ++vs)
           for (int s = 0; s < nslot; ++s, ++use) {
-            const CUtensorMap* tm = &maps.m[vs][cls];
+            const CUtensorMap* tm = &maps.m[vbase + vs][cls];
             const int ri = (int)(use % NSLOT);
             const uint32_t ph = (use / NSLOT) & 1u;
             ok = !failed(err) && mbar_wait(&slot_empty[ri], ph ^ 1u, err, 1);
@@ -357,9 +361,14 @@ __global__ void __launch_bounds__(UMMA_THREADS, 1)
             }
           }
         }
-        const float dg = valid ? diag[n1 + d] : 0.f;
+        // w2_add: a second pass over other value slices adds to the W2 rows
+        // the first pass stored (which hold the diagonal term already)
+        const float dg = (valid && !w2_add) ? diag[n1 + d] : 0.f;
 #pragma unroll
-        for (int j = 0; j < NH; ++j) w2[j] = dg * v2[j];
+        for (int j = 0; j < NH; ++j) {
+          const int c = cbeg + j;
+          w2[j] = w2_add ? ((valid && c < mcols) ? W[(int64_t)c * ldw + n1 + d] : 0.f) : dg * v2[j];
+        }
         // segment A: sum_k A[row, k] V[(a', k), c].  The lanes of a warp with
         // the same a' (most of them: a' changes once per run of nv - 1 - a'
         // rows) share one cooperative load of those V values, spread over
@@ -480,6 +489,8 @@ struct UmmaPlan {
   const void* slices_for = nullptr; // the mid slice array the slice maps describe (FP32-value pass)
   int2* d_items = nullptr;          // tensor-core work items (row ranges inside one slab)
   int nitems = 0;
+  int2* d_items_s = nullptr;        // short items (UMMA_ITEM_ROWS_SHORT rows): the FP32-value main pass
+  int nitems_s = 0;
   int2* d_runs = nullptr;           // pass-3 runs: (first row, rows) of equal a' in one slab
   int nruns = 0;
   int* d_err = nullptr;             // device error word of the kernel's bounded waits
@@ -513,25 +524,27 @@ size_t umma_smem_bytes(int nslot) {
 
 template <int NP, int VS, int XS>
 int launch_umma_np(Ctx* c, UmmaPlan* u, const float* V, int64_t ldv, int m, float* W, int64_t ldw, double* W1,
-                   int64_t ld1, int seg_a) {
+                   int64_t ld1, int seg_a, int vbase = 0, int w2_add = 0, bool short_items = false) {
+  const int2* items = short_items ? u->d_items_s : u->d_items;
+  const int nitems = short_items ? u->nitems_s : u->nitems;
   const int smax = smem_optin_max(c);
   int nslot = umma_nslot<NP, XS>(smax);
-  nslot = std::min(nslot, VS == 1 ? 6 : 4);
+  nslot = std::min(nslot, (VS == 1 && XS == 2) ? 6 : 4);
   if (nslot < 2) return set_err(c, ADCGPU_UNSUPPORTED, "tensor-core sigma pass: shared memory too small");
   const size_t smem = umma_smem_bytes<NP, XS>(nslot);
   if (smem > (size_t)smax) return set_err(c, ADCGPU_UNSUPPORTED, "tensor-core sigma pass: shared memory too small");
   const GeomDev g = to_dev(c->geom);
-  const int grid = std::max(1, std::min(u->nitems, c->nsm));
+  const int grid = std::max(1, std::min(nitems, c->nsm));
   auto go = [&](auto kern) -> int {
     ADC_CUDA(c, cudaFuncSetAttribute(kern, cudaFuncAttributeMaxDynamicSharedMemorySize, smax));
-    kern<<<grid, UMMA_THREADS, smem, c->stream>>>(g, u->d_items, u->nitems, u->maps,
+    kern<<<grid, UMMA_THREADS, smem, c->stream>>>(g, items, nitems, u->maps,
                                                   (const __nv_bfloat16*)c->d_Bt16, c->d_diag32, V, ldv, m, W, ldw, W1,
-                                                  ld1, seg_a, u->d_err);
+                                                  ld1, seg_a, vbase, w2_add, u->d_err);
     ADC_COUNT_LAUNCH();
     ADC_CUDA(c, cudaGetLastError());
     return ADCGPU_OK;
   };
-  if constexpr (VS == 1) {
+  if constexpr (VS == 1 && XS == 2) {
     switch (nslot) {
       case 2: return go(k_sigma_umma<NP, 2, VS, XS>);
       case 3: return go(k_sigma_umma<NP, 3, VS, XS>);
@@ -573,6 +586,7 @@ void umma_free(Ctx* c, void*& handle) {
   UmmaPlan* u = reinterpret_cast<UmmaPlan*>(handle);
   if (!u) return;
   dfree(c, u->d_items);
+  dfree(c, u->d_items_s);
   dfree(c, u->d_runs);
   dfree(c, u->d_err);
   if (u->h_err) cudaFreeHost(u->h_err);
@@ -591,7 +605,7 @@ int umma_prepare(Ctx* c, void*& handle, int item_rows) {
   UmmaPlan* u = new UmmaPlan;
   handle = u;
   u->item_rows = item_rows;
-  std::vector<int2> items, runs;
+  std::vector<int2> items, items_s, runs;
   for (int cls = 0; cls < 5; ++cls) {
     const int64_t r0 = G.start[cls], r1 = G.start[cls + 1], sl = G.slab_len(cls);
     const bool twoa = (cls == 1 || cls >= 3);
@@ -599,6 +613,9 @@ int umma_prepare(Ctx* c, void*& handle, int item_rows) {
       const int64_t npc = (sl + item_rows - 1) / item_rows, per = (sl + npc - 1) / npc;
       for (int64_t a = s0; a < s0 + sl; a += per)
         items.push_back(make_int2((int)a, (int)std::min<int64_t>(a + per, s0 + sl)));
+      const int64_t npcs = (sl + UMMA_ITEM_ROWS_SHORT - 1) / UMMA_ITEM_ROWS_SHORT, pers = (sl + npcs - 1) / npcs;
+      for (int64_t a = s0; a < s0 + sl; a += pers)
+        items_s.push_back(make_int2((int)a, (int)std::min<int64_t>(a + pers, s0 + sl)));
       if (twoa) {
         for (int ap = 0; ap + 1 < G.nv; ++ap)
           runs.push_back(make_int2((int)(s0 + pair_index(ap, ap + 1, G.nv)), G.nv - 1 - ap));
@@ -609,6 +626,9 @@ int umma_prepare(Ctx* c, void*& handle, int item_rows) {
   }
   int st;
   if ((st = dmalloc(c, (void**)&u->d_items, sizeof(int2) * items.size()))) return st;
+  if ((st = dmalloc(c, (void**)&u->d_items_s, sizeof(int2) * items_s.size()))) return st;
+  ADC_CUDA(c, h2d(c, u->d_items_s, items_s.data(), sizeof(int2) * items_s.size()));
+  u->nitems_s = (int)items_s.size();
   if ((st = dmalloc(c, (void**)&u->d_runs, sizeof(int2) * runs.size()))) return st;
   if ((st = dmalloc(c, (void**)&u->d_err, sizeof(int)))) return st;
   ADC_CUDA(c, cudaMallocHost((void**)&u->h_err, sizeof(int)));
@@ -665,17 +685,24 @@ int umma_launch(Ctx* c, void* handle, const float* V, int64_t ldv, int m, float*
   return launch_umma_np<48, 1, 2>(c, u, V, ldv, m, W, ldw, W1, ld1, seg_a);
 }
 
-// The C|D products of the FP32-value matrix for m <= 32 columns: the values
-// as three BF16 slices (the BF16 store, then the mid and lo slices), the
-// vectors as three BF16 slices; segments A and B are left to the compact
-// kernels.
+// The C|D products of the FP32-value matrix for m <= 32 columns, in two
+// passes whose TMEM sums stay short: (1) the BF16 store (the leading 8 bits
+// of each value) against the vectors as three BF16 slices, over short work
+// items, storing W2 with the diagonal term; (2) the mid and lo value slices
+// (2^-9 of the value and below) against the vectors as hi | lo, adding to
+// W2.  The second pass's accumulation error is relative to its small
+// products.  Segments A and B are left to the compact kernels.
 int umma3_launch(Ctx* c, void* handle, const float* V, int64_t ldv, int m, float* W, int64_t ldw, double* W1,
                  int64_t ld1) {
   UmmaPlan* u = reinterpret_cast<UmmaPlan*>(handle);
   if (!u || m <= 0 || m > 32) return set_err(c, ADCGPU_BAD_INPUT, "tensor-core FP32-value sigma pass: columns");
   if (!u->slices_for) return set_err(c, ADCGPU_UNSUPPORTED, "tensor-core FP32-value sigma pass: no value slices");
-  if (m <= 16) return launch_umma_np<16, 3, 3>(c, u, V, ldv, m, W, ldw, W1, ld1, 0);
-  return launch_umma_np<32, 3, 3>(c, u, V, ldv, m, W, ldw, W1, ld1, 0);
+  if (m <= 16) {
+    ST((launch_umma_np<16, 1, 3>(c, u, V, ldv, m, W, ldw, W1, ld1, 0, 0, 0, true)));
+    return launch_umma_np<16, 2, 2>(c, u, V, ldv, m, W, ldw, W1, ld1, 0, 1, 1, false);
+  }
+  ST((launch_umma_np<32, 1, 3>(c, u, V, ldv, m, W, ldw, W1, ld1, 0, 0, 0, true)));
+  return launch_umma_np<32, 2, 2>(c, u, V, ldv, m, W, ldw, W1, ld1, 0, 1, 1, false);
 }
 
 // Reads the kernel's error word (waits for the stream) and clears it.
