@@ -1854,10 +1854,9 @@ extern "C" int adcgpu_sigma_set_shape(adcgpu_ctx* h, int chunk, int mc_fp64, int
   // 512: the FP32 Gram products (V^T W) on the CUDA cores instead of the
   // tensor cores
   gram_set_off(c, ((mc_fp64 | mc_fp32) & 512) ? 1 : 0);
-  // 1024: FP32 values on the tcgen05 pass as three BF16 slices (off by
-  // default: its TMEM sums of ~1,100 slice products per element carry about
-  // 1e-5 relative error, above the FP32 phase's target)
-  plan->umma3_on = ((mc_fp64 | mc_fp32) & 1024) ? 1 : 0;
+  // 1024: FP32 values on the CUDA-core tile instead of the two tcgen05
+  // passes over BF16 slices
+  plan->umma3_on = ((mc_fp64 | mc_fp32) & 1024) ? 0 : 1;
   plan->mc_cap[0] = std::min(mc_fp64 & 7, 2);
   plan->mc_cap[1] = std::min(mc_fp32 & 7, 4);
   return build_chunks(c, chunk);

@@ -37,13 +37,20 @@ sys.path.insert(0, HERE)
 
 NO, NV, SEED, NROOTS, TOL = 16, 180, 7, 20, 1e-6
 METRIC = "time-to-converge 20 roots (mixed+learned vs FP64 GPU) at 1e-6 Ha; matvec GB/s"
-# DRAM bytes moved by the sigma kernels per sigma call, relative to the
-# algorithmic bytes of the call: from ncu (dram__bytes_read.sum +
-# dram__bytes_write.sum of one-kernel captures, profiles/); the solve's mix
-# of calls is assumed to keep the ratio
-TRAFFIC_PER_ALG_BYTE = 1.98
-TRAFFIC_SOURCE = ("ncu DRAM bytes per sigma call at nocc=10/nvirt=110 as a ratio (1.98) of the algorithmic "
-                  "bytes, applied to this workload")
+# DRAM bytes moved by the kernels of one sigma call per algorithmic byte,
+# by value store, from one-kernel ncu captures (dram__bytes_read.sum +
+# dram__bytes_write.sum, --clock-control none) at nocc=10/nvirt=110 summed
+# over the kernels of a call (profiles/): BF16 values, 48 columns: tcgen05
+# pass 0.485 GB + compact segments 0.266 GB against 1.03 GB algorithmic;
+# FP32 values, 40 columns: 2.5 passes of the FP32 tile (0.67 GB each) + compact
+# segment B (0.09 GB per 16 columns) against 1.29 GB; FP64 values, 30 columns:
+# two passes of the double-float tile (1.27 GB each) + pass 2 (0.12 GB per 4
+# columns) against 1.93 GB.  The index-free store reads no column indices, so
+# a ratio below 1 is possible; above 1 means the store is read once per
+# column group of the tile.
+TRAFFIC_PER_ALG_BYTE = {"bf16": 0.73, "fp32": 1.48, "fp64": 1.78}
+TRAFFIC_SOURCE = ("ncu one-kernel captures at nocc=10/nvirt=110 (DRAM bytes of each kernel of a sigma call, summed, "
+                  "per algorithmic byte, by value store), applied to this workload's calls")
 
 
 def parse():
@@ -363,7 +370,8 @@ def run_gb300(args):
         "roofline": {"bound": "hbm", "kernel": "sigma product (all sigma kernels of one call), every call of the "
                      "timed solves", "achieved": achieved,
                      "peak": hbm, "unit": "GB/s", "frac": achieved / hbm,
-                     "traffic": per_launch_bytes * TRAFFIC_PER_ALG_BYTE,
+                     "traffic": sum(v["alg_bytes"] * TRAFFIC_PER_ALG_BYTE[k] for k, v in by_store.items())
+                     / max(stats["calls"], 1),
                      "traffic_source": TRAFFIC_SOURCE,
                      "alg_bytes_per_launch": per_launch_bytes, "launches": stats["calls"],
                      "avg_launch_ms": stats["ms"] / max(stats["calls"], 1), "peak_source": src,
