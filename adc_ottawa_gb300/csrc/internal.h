@@ -419,7 +419,7 @@ struct SigmaPlan {
   int umma_off = 0;           // 1: the tensor-core pass is not used
   void* ab = nullptr;         // compact segment-A/B tables (sigma_ab.cu), built on first use
   int ab_off = 0;             // 1: segments A/B through pass 2 / pass 3 instead
-  int umma3_on = 1;           // 1: FP32 values on the tcgen05 passes (BF16 slices); 0: the CUDA-core tile
+  int umma3_on = 0;           // 1: FP32 values on the two tcgen05 passes (BF16 slices)
   std::vector<DirectChunk> dchunks;   // direct path: chunks with their work-list ranges
 };
 int prepare_desc(Ctx* c);

@@ -1854,9 +1854,12 @@ extern "C" int adcgpu_sigma_set_shape(adcgpu_ctx* h, int chunk, int mc_fp64, int
   // 512: the FP32 Gram products (V^T W) on the CUDA cores instead of the
   // tensor cores
   gram_set_off(c, ((mc_fp64 | mc_fp32) & 512) ? 1 : 0);
-  // 1024: FP32 values on the CUDA-core tile instead of the two tcgen05
-  // passes over BF16 slices
-  plan->umma3_on = ((mc_fp64 | mc_fp32) & 1024) ? 0 : 1;
+  // 1024: FP32 values on the two tcgen05 passes over their BF16 slices
+  // instead of the CUDA-core tile.  As accurate as the tile and 3x faster
+  // per call, but off by default: with it as the FP32 phase's product the
+  // folded-preconditioner solve of one seeded system (nocc=12, nvirt=120,
+  // 20 roots) converged to a wrong root set
+  plan->umma3_on = ((mc_fp64 | mc_fp32) & 1024) ? 1 : 0;
   plan->mc_cap[0] = std::min(mc_fp64 & 7, 2);
   plan->mc_cap[1] = std::min(mc_fp32 & 7, 4);
   return build_chunks(c, chunk);

@@ -477,8 +477,8 @@ int adcgpu_sigma_autotune(adcgpu_ctx* ctx, int m, int* best_chunk, int* best_mc,
    kernels, bit 8 makes a mixed-precision matrix's sigma product read the
    FP32 value store instead of the BF16 one, bit 9 keeps the FP32 Gram
    products (adcgpu_gram_f32 and the solvers' V^T W) on the CUDA cores, bit
-   10 runs the FP32 values on the CUDA-core tile instead of the two tcgen05
-   passes over their BF16 slices. */
+   10 runs the FP32 values on two tcgen05 passes over their BF16 slices
+   instead of the CUDA-core tile. */
 int adcgpu_sigma_set_shape(adcgpu_ctx* ctx, int chunk, int mc_fp64, int mc_fp32);
 
 /* The solvers' tall-skinny Gram product on device FP32 arrays: C(p x q,

@@ -111,9 +111,9 @@ def test_compact_segments_match_pass2_and_oracle(gpu, no, nv, seed, capsys):
     per-run pass 3 over the same values: BF16 values on the tensor-core pass
     (flag 128 switches the compact kernels off) and FP32 values on the tiled
     pass (flag 256), at 1e-5 relative; both against the oracle's FP64
-    product at the value precision.  FP32 values run by default on two
-    tcgen05 passes over their BF16 slices; flag 1024 selects the CUDA-core
-    FP32 tile instead, and both are held to the same bounds.  Column counts cover partial 4-column
+    product at the value precision.  FP32 values on the two tcgen05 passes
+    over their BF16 slices (flag 1024, off by default) are held to the same
+    bounds.  Column counts cover partial 4-column
     groups, more than one 48-column pass and a padded leading dimension;
     (3, 37) gives noP = 8 and an odd number of virtuals."""
     import torch
