@@ -13,6 +13,11 @@
 !   propagate_fvec       -> propagate_fvec_gpu        (fvecprop.f90:27)
 !   chebyshev_auto_order_domain
 !                        -> chebyshev_auto_order_domain_gpu (chebyspec.f90:25)
+!   write_fspace_adc2_1_cvs
+!                        -> write_fspace_adc2_1_cvs_gpu (fspacetrial.f90:566)
+!   get_modifiedtm_adc2  -> get_modifiedtm_adc2_gpu   (get_moment.f90:153)
+!   fill_stvc            -> fill_stvc_gpu             (fspacetrial.f90:1255)
+!   hxvec_incore         -> hxvec_gpu                 (block_davidson.f90:844)
 !
 ! A non-zero status from the library is turned into errmsg +
 ! error_control, as the reference does for its own failures.
@@ -150,6 +155,44 @@ module adcgpu_iface
        type(c_ptr), value    :: ctx
        integer(c_int), value :: mode
      end function adcgpu_set_fp64_arith
+
+     integer(c_int) function adcgpu_build_adc2s_cvs(ctx, ndim, kpq, ncore, core, noffd, flag) &
+          bind(C, name="adcgpu_build_adc2s_cvs")
+       import :: c_int, c_ptr, c_int32_t, c_int64_t, c_char
+       type(c_ptr), value            :: ctx
+       integer(c_int), value         :: ndim, ncore
+       integer(c_int32_t)            :: kpq(*), core(*)
+       integer(c_int64_t)            :: noffd
+       character(kind=c_char), value :: flag
+     end function adcgpu_build_adc2s_cvs
+
+     integer(c_int) function adcgpu_set_dipole(ctx, dpl) bind(C, name="adcgpu_set_dipole")
+       import :: c_int, c_ptr, c_double
+       type(c_ptr), value :: ctx
+       real(c_double)     :: dpl(*)
+     end function adcgpu_set_dipole
+
+     integer(c_int) function adcgpu_modified_tm_adc2(ctx, ndim, kpq, mtm) bind(C, name="adcgpu_modified_tm_adc2")
+       import :: c_int, c_ptr, c_int32_t, c_double
+       type(c_ptr), value    :: ctx
+       integer(c_int), value :: ndim
+       integer(c_int32_t)    :: kpq(*)
+       real(c_double)        :: mtm(*)
+     end function adcgpu_modified_tm_adc2
+
+     integer(c_int) function adcgpu_fill_stvc(ndim, vctr, lmain, stvc_lbl) bind(C, name="adcgpu_fill_stvc")
+       import :: c_int, c_int32_t, c_double
+       integer(c_int), value :: ndim, lmain
+       real(c_double)        :: vctr(*)
+       integer(c_int32_t)    :: stvc_lbl(*)
+     end function adcgpu_fill_stvc
+
+     integer(c_int) function adcgpu_sigma(ctx, m, v, w) bind(C, name="adcgpu_sigma")
+       import :: c_int, c_ptr, c_double
+       type(c_ptr), value    :: ctx
+       integer(c_int), value :: m
+       real(c_double)        :: v(*), w(*)
+     end function adcgpu_sigma
 
      type(c_ptr) function adcgpu_last_error(ctx) bind(C, name="adcgpu_last_error")
        import :: c_ptr
@@ -370,5 +413,73 @@ contains
     endif
     deallocate(auto)
   end subroutine chebyshev_auto_order_domain_gpu
+
+!#######################################################################
+! write_fspace_adc2_1_cvs (fspacetrial.f90:566-596): the CVS matrix of the
+! core-hole list icore(1:ncore) (parameters.f90), kept on the device, with
+! the SCRATCH files as for write_fspace_adc2_1_gpu.  The library checks that
+! kpq is the list select_atom_is_cvs / select_atom_d_cvs produce.
+
+  subroutine write_fspace_adc2_1_cvs_gpu(ndim, kpq, noffdel, chr)
+    use parameters, only: nbas, nocc, icore, ncore
+    integer, intent(in)                                 :: ndim
+    integer, dimension(7,0:nBas**2*nOcc**2), intent(in) :: kpq
+    integer*8, intent(out)                              :: noffdel
+    character(1), intent(in)                            :: chr
+    integer(c_int)     :: st
+    integer(c_int64_t) :: n
+    call adcgpu_init
+    st = adcgpu_build_adc2s_cvs(gpu_ctx, int(ndim,c_int), kpq, int(ncore,c_int), icore, n, chr)
+    call adcgpu_check(st, 'write_fspace_adc2_1_cvs')
+    noffdel = n
+    st = adcgpu_write_hmlt_files(gpu_ctx, 'SCRATCH'//c_null_char, chr)
+    call adcgpu_check(st, 'write_hmlt_files')
+  end subroutine write_fspace_adc2_1_cvs_gpu
+
+!#######################################################################
+! get_modifiedtm_adc2 (get_moment.f90:153-442): the f-vector of the dipole
+! component held in dpl (parameters.f90, as the reference's caller sets it),
+! for an ADC(2)-s or CVS kpq.  ista is accepted for the reference's
+! argument list; the f-vector is that of the ground state, as there.
+
+  subroutine get_modifiedtm_adc2_gpu(ndim, kpq, mtm, ista)
+    use parameters, only: dp, dpl
+    integer, intent(in)                      :: ndim, ista
+    integer, dimension(7,0:*), intent(in)    :: kpq
+    real(dp), dimension(ndim), intent(out)   :: mtm
+    integer(c_int) :: st
+    call adcgpu_init
+    st = adcgpu_set_dipole(gpu_ctx, dpl)
+    call adcgpu_check(st, 'set_dipole')
+    st = adcgpu_modified_tm_adc2(gpu_ctx, int(ndim,c_int), kpq, mtm)
+    call adcgpu_check(st, 'get_modifiedtm_adc2')
+  end subroutine get_modifiedtm_adc2_gpu
+
+!#######################################################################
+! fill_stvc (fspacetrial.f90:1255-1270): stvc_lbl(1:lmain) = the indices of
+! the lmain largest vctr(i)**2 in the order of dsortindxa1('D').
+
+  subroutine fill_stvc_gpu(ndim, vctr)
+    use parameters, only: dp, lmain, stvc_lbl
+    integer, intent(in)                  :: ndim
+    real(dp), dimension(ndim), intent(in) :: vctr
+    integer(c_int) :: st
+    st = adcgpu_fill_stvc(int(ndim,c_int), vctr, int(lmain,c_int), stvc_lbl)
+    call adcgpu_check(st, 'fill_stvc')
+  end subroutine fill_stvc_gpu
+
+!#######################################################################
+! hxvec_incore (block_davidson.f90:844-883): W = H V for m columns of the
+! matrix the context holds (host arrays, ndim x m).
+
+  subroutine hxvec_gpu(ndim, m, v, w)
+    use parameters, only: dp
+    integer, intent(in)                     :: ndim, m
+    real(dp), dimension(ndim,m), intent(in)  :: v
+    real(dp), dimension(ndim,m), intent(out) :: w
+    integer(c_int) :: st
+    st = adcgpu_sigma(gpu_ctx, int(m,c_int), v, w)
+    call adcgpu_check(st, 'hxvec_incore')
+  end subroutine hxvec_gpu
 
 end module adcgpu_iface
