@@ -479,7 +479,7 @@ def _secondary_line(metric, value, unit, steps, warmup, config, **extra):
 
 
 def run_lanczos(args):
-    """Config 2 block Lanczos: b = 10 seeded uniform start vectors, 300 cycles
+    """Block Lanczos on the nocc=10/nvirt=110 matrix: b = 10 seeded uniform start vectors, 300 cycles
     (nvec = 3000), FP64 throughout, T and its eigenvalues returned."""
     from adc_ottawa_gb300 import ADCGPU_FP64, AdcGpu, synth_system, synth_uniform_block
 
@@ -605,7 +605,7 @@ def run_cheb(args):
 
 
 def run_batch(args):
-    """Config 4 batch: 64 seeded systems, nocc ~ U{4..12}, nvirt ~ U{30..120},
+    """Batch: 64 seeded systems, nocc ~ U{4..12}, nvirt ~ U{30..120},
     8 roots to 1e-6, mixed precision with the folded preconditioner, solved
     concurrently (one stream per system)."""
     from adc_ottawa_gb300 import PRECON_FOLD, batch

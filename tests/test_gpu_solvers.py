@@ -21,7 +21,7 @@ def cfg1(gpu):
 @pytest.mark.parametrize("precon", [1, 2])
 @pytest.mark.parametrize("ldfl", [True, False])
 def test_davidson_config1(cfg1, precon, ldfl):
-    """Config 1: 6 roots, tol 1e-8: eigenvalues within 1e-8 Ha of the oracle."""
+    """nocc=5, nvirt=19, 6 roots, tol 1e-8: eigenvalues within 1e-8 Ha of the oracle."""
     g, ref = cfg1
     res = g.davdiag_block(6, 1e-8, precon=precon, ldfl=ldfl)
     st, ev, _, info = ref.davidson(6, 1e-8, precon=precon, deflate=ldfl)
