@@ -39,14 +39,34 @@ def _solve_one(args):
             "iterations": r.iterations, "evals": r.evals.tolist(), "seconds": time.perf_counter() - t0}
 
 
+def work_estimate(no: int, nv: int) -> float:
+    """Relative cost of one system: the stored coupling values a sigma
+    product streams, about N (2 nocc + 2 nvirt) for N configurations."""
+    return float(api.adc2s_dim(no, nv)[0]) * (2 * no + 2 * nv)
+
+
+def schedule(systems, workers: int):
+    """Longest-processing-time-first order for a pool of `workers` streams:
+    the systems sorted by decreasing work estimate (stable for equal ones),
+    so the large systems start first and the small ones fill the tail.
+    Returns the indices into `systems` in submission order."""
+    del workers   # the greedy pool assigns each next job to the first free worker
+    return sorted(range(len(systems)), key=lambda i: -work_estimate(systems[i][0], systems[i][1]))
+
+
 def solve_many(systems, nroots: int = 8, tol: float = 1e-6, precision: int = api.ADCGPU_MIXED,
                precon: int = api.PRECON_DPR, workers: int = 8):
-    """Solves all systems concurrently; returns per-system results and the
-    wall time of the whole batch."""
+    """Solves all systems concurrently, largest first (`schedule`); returns
+    the per-system results in the order of `systems` and the wall time of
+    the whole batch."""
     t = time.perf_counter()
-    jobs = [(no, nv, seed, nroots, tol, precision, precon) for no, nv, seed in systems]
+    order = schedule(systems, workers)
+    jobs = {i: (*systems[i], nroots, tol, precision, precon) for i in order}
+    res = [None] * len(systems)
     with cf.ThreadPoolExecutor(max_workers=workers) as ex:
-        res = list(ex.map(_solve_one, jobs))
+        futs = {ex.submit(_solve_one, jobs[i]): i for i in order}
+        for f in cf.as_completed(futs):
+            res[futs[f]] = f.result()
     return res, time.perf_counter() - t
 
 

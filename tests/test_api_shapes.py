@@ -33,3 +33,17 @@ def test_wrong_shapes_are_refused(built, fake, call):
     with pytest.raises(AdcGpuError) as ei:
         call(fake)
     assert ei.value.code == 12
+
+
+def test_batch_schedule_largest_first():
+    """The batch driver submits systems largest first (by the stored values a
+    sigma product streams) and returns results in the caller's order."""
+    from adc_ottawa_gb300 import batch
+
+    systems = batch.seeded_systems(64)
+    order = batch.schedule(systems, 8)
+    assert sorted(order) == list(range(64))
+    w = [batch.work_estimate(systems[i][0], systems[i][1]) for i in order]
+    assert all(a >= b for a, b in zip(w, w[1:]))
+    # the smallest system's work is a small fraction of the largest's
+    assert w[-1] < 0.05 * w[0]
